@@ -1,0 +1,308 @@
+#!/usr/bin/env python3
+"""Benchmark: ms-to-fixpoint of FP64 iterated domain propagation on GB300.
+
+Workload (default): the large power-law MIP -- m=2,000,000 rows, n=1,500,000
+variables, Zipf(1.8) row lengths clipped to [2, 20,000] plus 32 rows of
+100,000 non-zeros, FP64 coefficients +-LogUniform[1e-2, 1e3], 50% integer
+variables in [0, U{1..20}], 10% one-sided infinite bounds, 30% equality rows,
+x0-based sides (seeded synthetic data standing in for MIPLIB).
+
+A step is one propagation of that instance from its initial bounds to the
+fixpoint (or the 100-round cap) with device-resident data: one persistent
+megakernel launch. `value` is ms per step; `e2e` is the same propagation
+through the reference-facing C call propagateConstraintsGPUAtomicDouble with
+host buffers (upload, layout, propagation and download inside the timed
+region). `--impl reference` times the reference's CPU algorithm (the oracle
+port of cpu_omp: Jacobi rounds on every host core) on the same instance.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gdp|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gpu-domain-propagator_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOAD = ("power-law MIP: m=2,000,000 rows, n=1,500,000 vars, Zipf(1.8) row lengths in [2,20000] "
+            "+ 32 rows x 100,000 nnz, coef +-LogUniform[1e-2,1e3], 30% equality rows; seed 1000+rank")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gdp", "reference"], default="gdp")
+    ap.add_argument("--sync", choices=["megakernel", "cpu_loop", "gpu_loop"], default="megakernel")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink m/n (testing only; the bench line is m=2M)")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget-s", type=float, default=30.0)
+    ap.add_argument("--max-rounds", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "gdp" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_instance(args, rank):
+    import gdpgen
+    m = int(2_000_000 * args.scale)
+    n = int(1_500_000 * args.scale)
+    kw = {}
+    if args.scale < 1.0:
+        kw = dict(len_max=max(16, int(20000 * args.scale)), dense_len=max(32, int(100_000 * args.scale)))
+    t0 = time.perf_counter()
+    mip = gdpgen.random_mip(1, seed=1000 + rank, m=m, n=n, **kw)
+    return mip, time.perf_counter() - t0
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(mip, gpu_rounds: int, budget_s: float, max_rounds: int):
+    """The oracle port of the reference's cpu_omp (Jacobi rounds, OpenMP on
+    every host core), timed on the same instance. Runs to the fixpoint when a
+    2-round probe projects it within the budget, else reports the projection."""
+    import oracle
+    cores = os.cpu_count() or 1
+    probe_rounds = 2
+    r = oracle.propagate(mip, oracle.JACOBI, max_rounds=probe_rounds, nthreads=cores)
+    per_round = r.seconds / max(1, r.rounds)
+    projected = per_round * max(1, gpu_rounds)
+    if projected <= budget_s:
+        full = oracle.propagate(mip, oracle.JACOBI, max_rounds=max_rounds, nthreads=cores)
+        return {"value": full.seconds * 1e3, "unit": "ms", "cores": cores, "kind": "port",
+                "sample": f"full propagation to fixpoint ({full.rounds} rounds), Jacobi schedule "
+                          f"(the reference's cpu_omp round function), {cores} threads",
+                "rounds": full.rounds}
+    return {"value": projected * 1e3, "unit": "ms", "cores": cores, "kind": "port",
+            "sample": f"first {r.rounds} rounds timed ({r.seconds:.2f} s, all rows marked), "
+                      f"scaled to the GPU's {gpu_rounds} rounds; Jacobi schedule, {cores} threads",
+            "rounds": gpu_rounds}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    mip, _ = make_instance(args, rank)
+    import oracle
+    cores = os.cpu_count() or 1
+    times, rounds = [], 0
+    for i in range(args.warmup + args.steps):
+        r = oracle.propagate(mip, oracle.JACOBI, max_rounds=max(2, min(args.max_rounds or 100, 3)),
+                             nthreads=cores)
+        if i >= args.warmup:
+            times.append(r.seconds / max(1, r.rounds))
+        rounds = r.rounds
+    # full-propagation round count (for scaling the per-round sample to ms-to-fixpoint)
+    probe = oracle.propagate(mip, oracle.JACOBI, max_rounds=args.max_rounds, nthreads=cores)
+    per_round = statistics.median(times)
+    value = probe.seconds * 1e3
+    line = {"metric": "ms-to-fixpoint", "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": probe.rounds,
+                       "parallelism": "replicas"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port",
+                             "sample": f"{probe.rounds}-round propagation to fixpoint; median per-round time of "
+                                       f"{args.steps} timed 3-round samples = {per_round * 1e3:.1f} ms; "
+                                       f"Jacobi schedule (reference cpu_omp round function), {cores} threads"},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+
+    import torch
+
+    import gdp
+    torch.cuda.set_device(local)
+    sync = {"megakernel": gdp.MEGAKERNEL, "cpu_loop": gdp.CPU_LOOP, "gpu_loop": gdp.GPU_LOOP}[args.sync]
+    mip, gen_s = make_instance(args, rank)
+    t0 = time.perf_counter()
+    ctx = gdp.Context(mip, sync_type=sync, max_rounds=args.max_rounds)
+    ctx_s = time.perf_counter() - t0
+    layout = ctx.layout()
+    stream = torch.cuda.current_stream()
+    d_lb0 = torch.tensor(mip.lb, dtype=torch.float64, device="cuda")
+    d_ub0 = torch.tensor(mip.ub, dtype=torch.float64, device="cuda")
+    d_lb = torch.empty_like(d_lb0)
+    d_ub = torch.empty_like(d_ub0)
+
+    def step():
+        d_lb.copy_(d_lb0)
+        d_ub.copy_(d_ub0)
+        return ctx.propagate_device(d_lb.data_ptr(), d_ub.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        st = step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = Clocks(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        stats.append(step())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    total_ms = ev0.elapsed_time(ev1)
+    ms_step = max_over_ranks(ws, total_ms / args.steps)
+
+    rounds = stats[-1]["rounds"]
+    bytes_per_step = stats[-1]["bytes_algorithmic"]
+    kernel_ms = statistics.median(s["device_ms"] for s in stats)  # megakernel launch duration (events)
+    launches = int(sum(s["kernel_launches"] for s in stats))
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = bytes_per_step / (kernel_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "megakernel_traffic.json"
+    if tfile.exists():
+        try:
+            tr = json.loads(tfile.read_text())
+            traffic = tr.get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+
+    # end to end through the reference-facing C call, host buffers
+    e2e_ms = []
+    for _ in range(max(1, args.e2e_steps)):
+        lb, ub = list(), list()
+        t1 = time.perf_counter()
+        lbs, ubs, _ = gdp.propagate(mip, sync_type=sync, max_rounds=args.max_rounds)
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    h2d = (mip.nnz * 12 + (mip.m + 1) * 4 + mip.m * 16 + mip.n * 20)
+    d2h = mip.n * 16
+
+    line = {"metric": "ms-to-fixpoint", "value": ms_step, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": rounds,
+                       "converged": bool(stats[-1]["converged"]), "infeasible": bool(stats[-1]["infeasible"]),
+                       "sync": args.sync, "layout": layout, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (CSR %.0f MB vs 129 MB L2)" % (mip.nnz * 12 / 1e6),
+                       "scale": args.scale},
+            "hbm_gbs": achieved, "nnz_per_s": mip.nnz * rounds / (ms_step * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "kernel": "k_megakernel", "bytes_per_launch": bytes_per_step,
+                         "launch_ms": kernel_ms},
+            "e2e": {"value": statistics.median(e2e_ms), "unit": "ms", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk,
+            "setup_s": {"generate": gen_s, "context": ctx_s}}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(mip, rounds, args.cpu_budget_s, args.max_rounds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

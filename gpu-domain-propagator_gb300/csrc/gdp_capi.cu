@@ -1,0 +1,252 @@
+// gdp_capi.cu -- the extern "C" surface of libgdp_gb300.so: the reference's
+// interface.h symbols (include/interface.h of the reference, implemented in
+// its src/interface.cu:18-354) and the extended API of gdp_ext.h.
+#include <chrono>
+#include <exception>
+#include <new>
+
+#include "gdp_context.h"
+#include "interface.h"
+
+using gdp::Context;
+
+struct gdp_context {
+    Context impl;
+};
+
+namespace {
+
+// The reference's CALL_AND_HANDLE (src/interface.cu:7-16): exceptions become
+// GDP_ERROR; here with the message kept for gdp_last_error().
+template <class F>
+GDP_RETCODE guarded(F &&f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        gdp::set_error("host allocation failed");
+        return GDP_ERROR;
+    } catch (const std::exception &e) {
+        gdp::set_error(e.what());
+        return GDP_ERROR;
+    } catch (...) {
+        gdp::set_error("unknown exception");
+        return GDP_ERROR;
+    }
+}
+
+GDP_RETCODE propagate_once_impl(int n_cons, int n_vars, int nnz, const int *col, const int *row_ptr,
+                                const double *val, const double *lhs, const double *rhs,
+                                double *lbs, double *ubs, const int *vartypes,
+                                const gdp_options *opts, gdp_stats *stats) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (stats) *stats = gdp_stats{};
+    // reference GPU_propagator.cuh:113-116: empty problems are a no-op
+    if (n_cons == 0 || n_vars == 0 || nnz == 0) {
+        if (stats) { stats->converged = 1; stats->infeasible_var = -1; }
+        return GDP_OKAY;
+    }
+    if (!lbs || !ubs) { gdp::set_error("null lbs/ubs"); return GDP_ERROR; }
+    Context ctx;
+    GDP_RETCODE rc = ctx.init(n_cons, n_vars, nnz, col, row_ptr, val, lhs, rhs, vartypes, opts);
+    if (rc != GDP_OKAY) return rc;
+    rc = ctx.propagate_host(lbs, ubs, stats);
+    if (stats)
+        stats->total_ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+}  // namespace
+
+// Only the C API is exported (the library builds with -fvisibility=hidden).
+#pragma GCC visibility push(default)
+extern "C" {
+
+GDP_RETCODE gdp_default_options(gdp_options *o) {
+    if (!o) return GDP_ERROR;
+    *o = gdp_options{};
+    o->max_rounds = GDP_MAX_NUM_ROUNDS;
+    o->sync_type = CPU_LOOP;
+    o->thread_row_max = 1024;
+    o->split_tile = 4096;
+    o->device = 0;
+    return GDP_OKAY;
+}
+
+const char *gdp_last_error(void) { return gdp::last_error(); }
+
+GDP_RETCODE gdp_context_create(int n_cons, int n_vars, int nnz, const int *col, const int *row_ptr,
+                               const double *val, const double *lhs, const double *rhs,
+                               const int *vartypes, const gdp_options *opts, gdp_context **out) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!out) { gdp::set_error("null output pointer"); return GDP_ERROR; }
+        *out = nullptr;
+        if (n_cons <= 0 || n_vars <= 0 || nnz <= 0) {
+            gdp::set_error("a context needs n_cons, n_vars and nnz > 0");
+            return GDP_ERROR;
+        }
+        gdp_context *c = new gdp_context();
+        const GDP_RETCODE rc = c->impl.init(n_cons, n_vars, nnz, col, row_ptr, val, lhs, rhs, vartypes, opts);
+        if (rc != GDP_OKAY) { delete c; return rc; }
+        *out = c;
+        return GDP_OKAY;
+    });
+}
+
+GDP_RETCODE gdp_context_destroy(gdp_context *ctx) {
+    return guarded([&]() -> GDP_RETCODE {
+        delete ctx;
+        return GDP_OKAY;
+    });
+}
+
+GDP_RETCODE gdp_propagate(gdp_context *ctx, double *lbs, double *ubs, gdp_stats *stats) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!ctx || !lbs || !ubs) { gdp::set_error("null argument"); return GDP_ERROR; }
+        const auto t0 = std::chrono::steady_clock::now();
+        if (stats) *stats = gdp_stats{};
+        const GDP_RETCODE rc = ctx->impl.propagate_host(lbs, ubs, stats);
+        if (stats)
+            stats->total_ms =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    });
+}
+
+GDP_RETCODE gdp_propagate_device(gdp_context *ctx, double *d_lbs, double *d_ubs, void *stream,
+                                 gdp_stats *stats) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!ctx || !d_lbs || !d_ubs) { gdp::set_error("null argument"); return GDP_ERROR; }
+        const auto t0 = std::chrono::steady_clock::now();
+        if (stats) *stats = gdp_stats{};
+        const GDP_RETCODE rc = ctx->impl.propagate_device(d_lbs, d_ubs, (cudaStream_t)stream, stats);
+        if (stats)
+            stats->total_ms =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    });
+}
+
+GDP_RETCODE gdp_context_set_options(gdp_context *ctx, int max_rounds, int sync_type) {
+    if (!ctx) { gdp::set_error("null context"); return GDP_ERROR; }
+    if (sync_type < CPU_LOOP || sync_type > MEGAKERNEL) { gdp::set_error("Unknown sync type"); return GDP_ERROR; }
+    ctx->impl.opts.max_rounds = max_rounds > 0 ? max_rounds : GDP_MAX_NUM_ROUNDS;
+    ctx->impl.opts.sync_type = sync_type;
+    ctx->impl.P.max_rounds = ctx->impl.opts.max_rounds;
+    return GDP_OKAY;
+}
+
+GDP_RETCODE gdp_context_layout(const gdp_context *ctx, long long out[6]) {
+    if (!ctx || !out) { gdp::set_error("null argument"); return GDP_ERROR; }
+    out[0] = ctx->impl.n_srows;
+    out[1] = ctx->impl.n_slices;
+    out[2] = ctx->impl.n_lrows;
+    out[3] = ctx->impl.n_tiles;
+    out[4] = ctx->impl.sell_elems;
+    out[5] = ctx->impl.mega_grid;
+    return GDP_OKAY;
+}
+
+GDP_RETCODE gdp_propagate_once(int n_cons, int n_vars, int nnz, const int *col, const int *row_ptr,
+                               const double *val, const double *lhs, const double *rhs, double *lbs,
+                               double *ubs, const int *vartypes, const gdp_options *opts,
+                               gdp_stats *stats) {
+    return guarded([&]() {
+        return propagate_once_impl(n_cons, n_vars, nnz, col, row_ptr, val, lhs, rhs, lbs, ubs, vartypes,
+                                   opts, stats);
+    });
+}
+
+// ---- reference interface.h ------------------------------------------------
+GDP_RETCODE propagateConstraintsGPUAtomicDouble(const int n_cons, const int n_vars, const int nnz,
+                                                const int *csr_col_indices, const int *csr_row_ptrs,
+                                                const double *csr_vals, const double *lhss,
+                                                const double *rhss, double *lbs, double *ubs,
+                                                const int *vartypes, const int sync_type) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (sync_type < CPU_LOOP || sync_type > MEGAKERNEL) {
+            gdp::set_error("Unknown sync type");
+            return GDP_ERROR;
+        }
+        gdp_options o;
+        gdp_default_options(&o);
+        o.sync_type = sync_type;
+        return propagate_once_impl(n_cons, n_vars, nnz, csr_col_indices, csr_row_ptrs, csr_vals, lhss,
+                                   rhss, lbs, ubs, vartypes, &o, nullptr);
+    });
+}
+
+GDP_RETCODE propagateConstraintsGPUReductionDouble(const int n_cons, const int n_vars, const int nnz,
+                                                   const int *csr_col_indices, const int *csr_row_ptrs,
+                                                   const double *csr_vals, const double *lhss,
+                                                   const double *rhss, double *lbs, double *ubs,
+                                                   const int *vartypes) {
+    return guarded([&]() -> GDP_RETCODE {
+        gdp_options o;
+        gdp_default_options(&o);
+        return propagate_once_impl(n_cons, n_vars, nnz, csr_col_indices, csr_row_ptrs, csr_vals, lhss,
+                                   rhss, lbs, ubs, vartypes, &o, nullptr);
+    });
+}
+
+static GDP_RETCODE not_implemented(const char *what) {
+    gdp::set_error(std::string(what) + " is not implemented: this library is the FP64 GPU path only");
+    return GDP_NOTIMPLEMENTED;
+}
+
+GDP_RETCODE propagateConstraintsGPUReductionFloat(const int, const int, const int, const int *, const int *,
+                                                  const float *, const float *, const float *, float *,
+                                                  float *, const int *) {
+    return not_implemented("propagateConstraintsGPUReductionFloat");
+}
+
+GDP_RETCODE propagateConstraintsGPUAtomicFloat(const int, const int, const int, const int *, const int *,
+                                               const float *, const float *, const float *, float *, float *,
+                                               const int *, const int) {
+    return not_implemented("propagateConstraintsGPUAtomicFloat");
+}
+
+GDP_RETCODE propagateConstraintsSequentialDouble(const int, const int, const int, const int *, const int *,
+                                                 const double *, const double *, const double *, double *,
+                                                 double *, const int *) {
+    return not_implemented("propagateConstraintsSequentialDouble");
+}
+
+GDP_RETCODE propagateConstraintsSequentialFloat(const int, const int, const int, const int *, const int *,
+                                                const float *, const float *, const float *, float *,
+                                                float *, const int *) {
+    return not_implemented("propagateConstraintsSequentialFloat");
+}
+
+GDP_RETCODE propagateConstraintsFullOMPDouble(const int, const int, const int, const int *, const int *,
+                                              const double *, const double *, const double *, double *,
+                                              double *, const int *) {
+    return not_implemented("propagateConstraintsFullOMPDouble");
+}
+
+GDP_RETCODE propagateConstraintsFullOMPFloat(const int, const int, const int, const int *, const int *,
+                                             const float *, const float *, const float *, float *, float *,
+                                             const int *) {
+    return not_implemented("propagateConstraintsFullOMPFloat");
+}
+
+GDP_RETCODE propagateConstraintsSequentialDisjointDouble(const int, const int, const int, const int *,
+                                                         const int *, const double *, const double *,
+                                                         const double *, double *, double *, const int *) {
+    return not_implemented("propagateConstraintsSequentialDisjointDouble");
+}
+
+GDP_RETCODE sequentialPropagateWithMeasureDouble(const int, const int, const int, const int *, const int *,
+                                                 const double *, const double *, const double *, double *,
+                                                 double *, const int *) {
+    return not_implemented("sequentialPropagateWithMeasureDouble");
+}
+
+GDP_RETCODE atomicPropagateWithMeasureDouble(const int, const int, const int, const int *, const int *,
+                                             const double *, const double *, const double *, double *,
+                                             double *, const int *) {
+    return not_implemented("atomicPropagateWithMeasureDouble");
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

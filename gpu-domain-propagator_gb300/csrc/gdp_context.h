@@ -1,0 +1,51 @@
+// gdp_context.h -- host-side propagation context (device layout + drivers).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gdp_ext.h"
+#include "gdp_internal.h"
+
+namespace gdp {
+
+void set_error(const std::string &msg);
+const char *last_error();
+
+// Owns device allocations; frees them on destruction.
+struct Arena {
+    std::vector<void *> ptrs;
+    ~Arena();
+    void *alloc_bytes(size_t bytes);
+};
+
+GDP_RETCODE validate_csr(int m, int n, int nnz, const int *col, const int *row_ptr,
+                         const double *val, const int *vartype);
+
+class Context {
+public:
+    ~Context();
+    GDP_RETCODE init(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
+                     const double *lhs, const double *rhs, const int *vartype, const gdp_options *o);
+    GDP_RETCODE propagate_host(double *lbs, double *ubs, gdp_stats *st);
+    GDP_RETCODE propagate_device(double *d_lbs, double *d_ubs, cudaStream_t s, gdp_stats *st);
+    GDP_RETCODE run_rounds(cudaStream_t s, gdp_stats *st);
+
+    int m = 0, n = 0, nnz = 0;
+    gdp_options opts{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    RoundFlags *h_flags = nullptr;  // pinned
+    Arena arena;
+    DevProblem P{};
+    double *d_lb = nullptr, *d_ub = nullptr, *d_lb_nxt = nullptr, *d_ub_nxt = nullptr;
+    RoundFlags *d_flags = nullptr;
+    unsigned *d_barrier = nullptr;
+    int n_sms = 0, finalize_blocks = 1, mega_grid = 1;
+    int n_srows = 0, n_slices = 0, n_lrows = 0, n_tiles = 0;
+    long long sell_elems = 0, rows_nonempty = 0, nnz_rows = 0;
+};
+
+}  // namespace gdp

@@ -1,0 +1,290 @@
+"""Python host interface of the GB300 domain propagator (ctypes over libgdp_gb300.so).
+
+Two layers:
+
+* ``propagateGPUAtomic`` / ``propagateGPUReduction`` mirror the reference's
+  Python driver (fileReader/GPUDomPropInterface.py:35-145): same names, same
+  argument order ``(n_vars, n_cons, nnz, csr_col_indices, csr_row_ptrs,
+  csr_vals, lhss, rhss, lbs, ubs, vartypes, ...)``, same return value
+  ``(lbs, ubs)`` as lists. They call the reference-named C symbols.
+* ``Context`` / ``propagate`` use the extended C API (gdp_ext.h) with numpy
+  arrays, options and statistics (rounds, infeasibility, device time).
+
+The library must be built (``build.build()``); there is no fallback: loading
+fails loudly when libgdp_gb300.so is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libgdp_gb300.so"
+
+GDP_OKAY, GDP_ERROR, GDP_NOTIMPLEMENTED = 1, 0, -18
+CPU_LOOP, GPU_LOOP, MEGAKERNEL = 0, 1, 2
+GDP_BINARY, GDP_INTEGER, GDP_CONTINUOUS = 0, 1, 3
+GDP_INF = 1e20
+
+
+class GDPError(RuntimeError):
+    pass
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("max_rounds", C.c_int),
+        ("sync_type", C.c_int),
+        ("thread_row_max", C.c_int),
+        ("split_tile", C.c_int),
+        ("device", C.c_int),
+        ("reserved", C.c_int * 8),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("rounds", C.c_int),
+        ("converged", C.c_int),
+        ("infeasible", C.c_int),
+        ("infeasible_var", C.c_int),
+        ("device_error", C.c_int),
+        ("kernel_launches", C.c_int),
+        ("changed_vars", C.c_longlong),
+        ("rows_processed", C.c_longlong),
+        ("nnz_processed", C.c_longlong),
+        ("bytes_algorithmic", C.c_double),
+        ("device_ms", C.c_double),
+        ("total_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib: Optional[C.CDLL] = None
+
+_P_INT = C.POINTER(C.c_int)
+_P_DBL = C.POINTER(C.c_double)
+_LEGACY_ARGS = [C.c_int, C.c_int, C.c_int, _P_INT, _P_INT, _P_DBL, _P_DBL, _P_DBL, _P_DBL, _P_DBL, _P_INT]
+
+
+def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
+    """Loads libgdp_gb300.so (once) and declares the C signatures."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise GDPError(f"{p} is missing: build it with gpu-domain-propagator_gb300/build.py "
+                       "(the CUDA library is required; there is no CPU fallback)")
+    lib = C.CDLL(str(p))
+    lib.gdp_last_error.restype = C.c_char_p
+    lib.gdp_default_options.argtypes = [C.POINTER(Options)]
+    lib.gdp_context_create.argtypes = [C.c_int, C.c_int, C.c_int, _P_INT, _P_INT, _P_DBL, _P_DBL, _P_DBL,
+                                       _P_INT, C.POINTER(Options), C.POINTER(C.c_void_p)]
+    lib.gdp_context_destroy.argtypes = [C.c_void_p]
+    lib.gdp_propagate.argtypes = [C.c_void_p, _P_DBL, _P_DBL, C.POINTER(Stats)]
+    lib.gdp_propagate_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
+    lib.gdp_context_set_options.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.gdp_context_layout.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+    lib.gdp_propagate_once.argtypes = _LEGACY_ARGS + [C.POINTER(Options), C.POINTER(Stats)]
+    lib.propagateConstraintsGPUAtomicDouble.argtypes = _LEGACY_ARGS + [C.c_int]
+    lib.propagateConstraintsGPUReductionDouble.argtypes = _LEGACY_ARGS
+    for name in ("gdp_default_options", "gdp_context_create", "gdp_context_destroy", "gdp_propagate",
+                 "gdp_propagate_device", "gdp_context_set_options", "gdp_context_layout",
+                 "gdp_propagate_once", "propagateConstraintsGPUAtomicDouble",
+                 "propagateConstraintsGPUReductionDouble"):
+        getattr(lib, name).restype = C.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load_library().gdp_last_error().decode(errors="replace")
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != GDP_OKAY:
+        raise GDPError(f"{what} returned {rc}: {last_error()}")
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    load_library().gdp_default_options(C.byref(o))
+    for k, v in kw.items():
+        if v is not None:
+            setattr(o, k, int(v))
+    return o
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _pi(a: np.ndarray):
+    return a.ctypes.data_as(_P_INT)
+
+
+def _pd(a: np.ndarray):
+    return a.ctypes.data_as(_P_DBL)
+
+
+@dataclass
+class MIP:
+    """A MIP in the reference's CSR argument convention."""
+    row_ptr: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+    lhs: np.ndarray
+    rhs: np.ndarray
+    lb: np.ndarray
+    ub: np.ndarray
+    vartype: np.ndarray
+
+    @property
+    def m(self) -> int:
+        return len(self.row_ptr) - 1
+
+    @property
+    def n(self) -> int:
+        return len(self.lb)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.row_ptr[-1]) if len(self.row_ptr) else 0
+
+    def normalized(self) -> "MIP":
+        return MIP(_i32(self.row_ptr), _i32(self.col), _f64(self.val), _f64(self.lhs), _f64(self.rhs),
+                   _f64(self.lb), _f64(self.ub), _i32(self.vartype))
+
+
+def propagate(mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
+              split_tile: int = 0, lb=None, ub=None) -> Tuple[np.ndarray, np.ndarray, dict]:
+    """One-shot propagation (upload, propagate, download) with statistics."""
+    lib = load_library()
+    p = mip.normalized()
+    lbo = _f64(p.lb if lb is None else lb).copy()
+    ubo = _f64(p.ub if ub is None else ub).copy()
+    o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
+                        split_tile=split_tile)
+    st = Stats()
+    rc = lib.gdp_propagate_once(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val), _pd(p.lhs),
+                                _pd(p.rhs), _pd(lbo), _pd(ubo), _pi(p.vartype), C.byref(o), C.byref(st))
+    _check(rc, "gdp_propagate_once")
+    return lbo, ubo, st.as_dict()
+
+
+class Context:
+    """Persistent device context: upload once, propagate many bound vectors."""
+
+    def __init__(self, mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
+                 split_tile: int = 0):
+        self._lib = load_library()
+        self.mip = mip.normalized()
+        p = self.mip
+        o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
+                            split_tile=split_tile)
+        h = C.c_void_p()
+        rc = self._lib.gdp_context_create(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val),
+                                          _pd(p.lhs), _pd(p.rhs), _pi(p.vartype), C.byref(o), C.byref(h))
+        _check(rc, "gdp_context_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gdp_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_options(self, max_rounds: int = 0, sync_type: int = CPU_LOOP) -> None:
+        _check(self._lib.gdp_context_set_options(self._h, int(max_rounds), int(sync_type)),
+               "gdp_context_set_options")
+
+    def layout(self) -> dict:
+        out = (C.c_longlong * 6)()
+        _check(self._lib.gdp_context_layout(self._h, out), "gdp_context_layout")
+        keys = ("thread_rows", "slices", "split_rows", "split_tiles", "sell_elements", "mega_grid")
+        return dict(zip(keys, [int(v) for v in out]))
+
+    def propagate(self, lb=None, ub=None) -> Tuple[np.ndarray, np.ndarray, dict]:
+        lbo = _f64(self.mip.lb if lb is None else lb).copy()
+        ubo = _f64(self.mip.ub if ub is None else ub).copy()
+        st = Stats()
+        _check(self._lib.gdp_propagate(self._h, _pd(lbo), _pd(ubo), C.byref(st)), "gdp_propagate")
+        return lbo, ubo, st.as_dict()
+
+    def propagate_device(self, d_lb_ptr: int, d_ub_ptr: int, stream_ptr: int = 0) -> dict:
+        """Propagates device-resident bounds (raw device pointers, e.g. torch data_ptr())."""
+        st = Stats()
+        _check(self._lib.gdp_propagate_device(self._h, C.c_void_p(d_lb_ptr), C.c_void_p(d_ub_ptr),
+                                              C.c_void_p(stream_ptr or None), C.byref(st)),
+               "gdp_propagate_device")
+        return st.as_dict()
+
+
+# ---- mirror of the reference's Python driver (fileReader/GPUDomPropInterface.py) ----
+
+def _legacy_arrays(n_vars, n_cons, nnz, csr_col_indices, csr_row_ptrs, csr_vals, lhss, rhss, lbs, ubs,
+                   vartypes):
+    # same length checks as the reference's check_input (GPUDomPropInterface.py:12-32)
+    assert len(csr_col_indices) == nnz
+    assert len(csr_row_ptrs) == n_cons + 1
+    assert len(csr_vals) == nnz
+    assert len(lhss) == n_cons
+    assert len(rhss) == n_cons
+    assert len(lbs) == n_vars
+    assert len(ubs) == n_vars
+    assert len(vartypes) == n_vars
+    return (_i32(csr_col_indices), _i32(csr_row_ptrs), _f64(csr_vals), _f64(lhss), _f64(rhss),
+            _f64(lbs).copy(), _f64(ubs).copy(), _i32(vartypes))
+
+
+def propagateGPUAtomic(n_vars: int, n_cons: int, nnz: int, csr_col_indices, csr_row_ptrs, csr_vals, lhss,
+                       rhss, lbs, ubs, vartypes, synctype: int = 0,
+                       datatype=C.c_double) -> Tuple[List[float], List[float]]:
+    """Reference fileReader/GPUDomPropInterface.py:90-145, on this library."""
+    if datatype is not C.c_double:
+        raise GDPError("only c_double is supported (FP64 propagation)")
+    lib = load_library()
+    col, rp, val, lhs, rhs, lbo, ubo, vt = _legacy_arrays(n_vars, n_cons, nnz, csr_col_indices, csr_row_ptrs,
+                                                          csr_vals, lhss, rhss, lbs, ubs, vartypes)
+    rc = lib.propagateConstraintsGPUAtomicDouble(n_cons, n_vars, nnz, _pi(col), _pi(rp), _pd(val), _pd(lhs),
+                                                 _pd(rhs), _pd(lbo), _pd(ubo), _pi(vt), int(synctype))
+    _check(rc, "propagateConstraintsGPUAtomicDouble")
+    return list(lbo), list(ubo)
+
+
+def propagateGPUReduction(n_vars: int, n_cons: int, nnz: int, csr_col_indices, csr_row_ptrs, csr_vals, lhss,
+                          rhss, lbs, ubs, vartypes, datatype=C.c_double) -> Tuple[List[float], List[float]]:
+    """Reference fileReader/GPUDomPropInterface.py:35-87, on this library."""
+    if datatype is not C.c_double:
+        raise GDPError("only c_double is supported (FP64 propagation)")
+    lib = load_library()
+    col, rp, val, lhs, rhs, lbo, ubo, vt = _legacy_arrays(n_vars, n_cons, nnz, csr_col_indices, csr_row_ptrs,
+                                                          csr_vals, lhss, rhss, lbs, ubs, vartypes)
+    rc = lib.propagateConstraintsGPUReductionDouble(n_cons, n_vars, nnz, _pi(col), _pi(rp), _pd(val),
+                                                    _pd(lhs), _pd(rhs), _pd(lbo), _pd(ubo), _pi(vt))
+    _check(rc, "propagateConstraintsGPUReductionDouble")
+    return list(lbo), list(ubo)

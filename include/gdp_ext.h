@@ -1,0 +1,99 @@
+/*
+ * gdp_ext.h -- extended C API of the GB300 domain propagator (libgdp_gb300.so).
+ *
+ * The reference's C API (interface.h) uploads the problem, propagates and
+ * frees everything in every call, and returns no round count or
+ * infeasibility status. This header adds, with no counterpart in the
+ * reference (so no reference citation applies to its entry points):
+ *   - a persistent device context: upload a MIP once, propagate many bound
+ *     vectors (branch-and-bound nodes) against it;
+ *   - a stats struct (rounds, convergence, infeasibility, device time, bytes);
+ *   - runtime options (round cap, loop driver, row-length thresholds) that the
+ *     reference fixed at compile time (src/params.h).
+ * Semantics of a propagation are those of interface.h: FP64 iterated
+ * activity-based bound tightening to a fixpoint (reference
+ * src/propagation_methods.cuh), run in deterministic Jacobi rounds.
+ */
+#ifndef GDP_GB300_EXT_H
+#define GDP_GB300_EXT_H
+
+#include <stddef.h>
+#include "gdp_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gdp_context gdp_context; /* opaque */
+
+typedef struct {
+    int max_rounds;       /* round cap; <= 0 selects GDP_MAX_NUM_ROUNDS (100) */
+    int sync_type;        /* GDP_SYNCTYPE: CPU_LOOP, GPU_LOOP or MEGAKERNEL */
+    int thread_row_max;   /* rows up to this length run one lane per row (bit-exact
+                             left-to-right sums); longer rows are split across CTAs.
+                             0 selects the default (1024). */
+    int split_tile;       /* non-zeros per split-row tile; 0 selects the default (4096) */
+    int device;           /* CUDA device ordinal (default 0) */
+    int reserved[8];      /* must be zero */
+} gdp_options;
+
+typedef struct {
+    int rounds;             /* rounds executed (the reference's prop_round - 1) */
+    int converged;          /* 1: the last round changed nothing (or infeasible) */
+    int infeasible;         /* 1: some variable has lb - ub > GDP_FEASTOL*max(1,|lb|,|ub|) */
+    int infeasible_var;     /* smallest violating variable, -1 if feasible */
+    int device_error;       /* device-side error code, 0 if none */
+    int kernel_launches;    /* kernels launched by the propagation */
+    long long changed_vars; /* variable bound changes committed, summed over rounds */
+    long long rows_processed;  /* rows swept, summed over rounds */
+    long long nnz_processed;   /* their non-zeros */
+    double bytes_algorithmic;  /* sum over rounds of 12*nnz + 20*rows + 36*n
+                                  (CSR col+val, row_ptr+lhs+rhs, lb/ub read+write and vartype) */
+    double device_ms;       /* device time of the round loop (CUDA events) */
+    double total_ms;        /* host wall time of the call */
+} gdp_stats;
+
+/* Fills *opts with the defaults. */
+GDP_RETCODE gdp_default_options(gdp_options *opts);
+
+/* Last error message of the calling thread ("" if none). */
+const char *gdp_last_error(void);
+
+/* Uploads a MIP (host CSR arrays, reference argument meaning) and builds the
+ * device layout. opts may be NULL. The context owns its device memory and a
+ * CUDA stream; it is not thread-safe (use one context per thread). */
+GDP_RETCODE gdp_context_create(int n_cons, int n_vars, int nnz, const int *csr_col_indices,
+                               const int *csr_row_ptrs, const double *csr_vals,
+                               const double *lhss, const double *rhss, const int *vartypes,
+                               const gdp_options *opts, gdp_context **out);
+
+GDP_RETCODE gdp_context_destroy(gdp_context *ctx);
+
+/* Propagates host bounds lbs/ubs (n_vars each, in/out) to a fixpoint.
+ * stats may be NULL. */
+GDP_RETCODE gdp_propagate(gdp_context *ctx, double *lbs, double *ubs, gdp_stats *stats);
+
+/* Same on device-resident bounds (d_lbs/d_ubs: n_vars doubles each in device
+ * memory, in/out) on the given CUDA stream (NULL: the context's stream). The
+ * call returns after the propagation has finished. */
+GDP_RETCODE gdp_propagate_device(gdp_context *ctx, double *d_lbs, double *d_ubs, void *stream,
+                                 gdp_stats *stats);
+
+/* Changes the round cap / driver of an existing context. */
+GDP_RETCODE gdp_context_set_options(gdp_context *ctx, int max_rounds, int sync_type);
+
+/* Layout facts of a context: number of thread rows, slices, split rows and
+ * split tiles, padded SELL elements (for tests and tuning). */
+GDP_RETCODE gdp_context_layout(const gdp_context *ctx, long long out[6]);
+
+/* The C API call of interface.h with options and stats. */
+GDP_RETCODE gdp_propagate_once(int n_cons, int n_vars, int nnz, const int *csr_col_indices,
+                               const int *csr_row_ptrs, const double *csr_vals,
+                               const double *lhss, const double *rhss, double *lbs, double *ubs,
+                               const int *vartypes, const gdp_options *opts, gdp_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GDP_GB300_EXT_H */

@@ -1,0 +1,424 @@
+/*
+ * gdp_oracle.c -- TEST INFRASTRUCTURE ONLY (the oracle).
+ *
+ * Plain-C restatement of the reference's CPU propagation, used as the checker
+ * of the GPU path by tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg. Nothing in the product library links, loads or calls it.
+ *
+ * Each function names the reference file:line it restates. Compile with
+ * -ffp-contract=off: the reference's x86 build never fuses a*b+c, and every
+ * expression here must round exactly like the reference's.
+ */
+#include "gdp_oracle.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define O_INF 1e20
+#define O_EPS 1e-9
+#define O_FEASTOL 1e-6
+#define O_MAX_ROUNDS 100
+
+/* EPS comparisons: reference src/def.h:68-79 */
+static inline int eps_le(double x, double y) { return (x - y) <= O_EPS; }
+static inline int eps_lt(double x, double y) { return (x - y) < -O_EPS; }
+static inline int eps_ge(double x, double y) { return (x - y) >= -O_EPS; }
+static inline int eps_gt(double x, double y) { return (x - y) > O_EPS; }
+static inline double eps_floor(double x) { return floor(x + O_EPS); }
+static inline double eps_ceil(double x) { return ceil(x - O_EPS); }
+static inline int is_posinf(double x) { return eps_ge(x, O_INF); }
+static inline int is_neginf(double x) { return eps_le(x, -O_INF); }
+/* std::min(a, b) as the reference's canConsBeTightened uses it */
+static inline double std_min(double a, double b) { return (b < a) ? b : a; }
+
+/* reference src/propagation_methods.cuh:40-47 */
+double gdpo_adjust_upper(int is_cont, double ub) { return is_cont ? ub : eps_floor(ub); }
+/* reference src/propagation_methods.cuh:49-52 */
+double gdpo_adjust_lower(int is_cont, double lb) { return is_cont ? lb : eps_ceil(lb); }
+/* reference src/propagation_methods.cuh:54-58 (the assert is a debug check only) */
+int gdpo_is_lb_better(double lb, double ub, double newlb) { (void)ub; return eps_gt(newlb, lb); }
+/* reference src/propagation_methods.cuh:60-64 */
+int gdpo_is_ub_better(double lb, double ub, double newub) { (void)lb; return eps_lt(newub, ub); }
+
+/* reference src/propagation_methods.cuh:136-154 */
+int gdpo_can_cons_be_tightened(double minact, double maxact, int minact_inf, int maxact_inf,
+                               double lhs, double rhs, double maxactdelta) {
+    if (minact_inf > 1 && maxact_inf > 1) return 0;
+    if (eps_lt(maxactdelta, O_INF)) return !eps_le(maxactdelta, std_min(rhs - minact, maxact - lhs));
+    return 1;
+}
+
+/* reference src/propagation_methods.cuh:156-159 */
+int gdpo_is_cons_infeasible(double minact, double maxact, double rhs, double lhs) {
+    return (minact > rhs || maxact < lhs);
+}
+
+/* reference src/propagation_methods.cuh:78-106 */
+int gdpo_tighten_var_upper(double coeff, double slack, double surplus, int num_inf,
+                           double lb, double ub, int is_cont, double *newb_out) {
+    double newb;
+    *newb_out = ub;
+    if (num_inf == 0) {
+        newb = coeff > 0 ? slack / coeff : surplus / coeff;
+        newb += lb;
+    } else if (num_inf == 1 && is_neginf(lb)) {
+        newb = coeff > 0 ? slack / coeff : surplus / coeff;
+    } else {
+        return 0;
+    }
+    newb = gdpo_adjust_upper(is_cont, newb);
+    if (gdpo_is_ub_better(lb, ub, newb)) {
+        *newb_out = newb;
+        return 1;
+    }
+    return 0;
+}
+
+/* reference src/propagation_methods.cuh:108-134 */
+int gdpo_tighten_var_lower(double coeff, double slack, double surplus, int num_inf,
+                           double lb, double ub, int is_cont, double *newb_out) {
+    double newb;
+    *newb_out = lb;
+    if (num_inf == 0) {
+        newb = coeff > 0 ? surplus / coeff : slack / coeff;
+        newb += ub;
+    } else if (num_inf == 1 && is_posinf(ub)) {
+        newb = coeff > 0 ? surplus / coeff : slack / coeff;
+    } else {
+        return 0;
+    }
+    newb = gdpo_adjust_lower(is_cont, newb);
+    if (gdpo_is_lb_better(lb, ub, newb)) {
+        *newb_out = newb;
+        return 1;
+    }
+    return 0;
+}
+
+/* reference src/propagation_methods.cuh:223-276 */
+void gdpo_tighten_variable(double coeff, double lhs, double rhs, double minact, double maxact,
+                           int minact_inf, int maxact_inf, int is_cont, double lb, double ub,
+                           int *lb_t, double *newlb, int *ub_t, double *newub) {
+    const double slack = rhs - minact;
+    const double surplus = lhs - maxact;
+    *lb_t = 0; *newlb = lb;
+    *ub_t = 0; *newub = ub;
+    if (coeff > 0.0) {
+        if (eps_gt(coeff * (ub - lb), rhs - minact) && !is_posinf(rhs) && !is_neginf(minact))
+            *ub_t = gdpo_tighten_var_upper(coeff, slack, surplus, minact_inf, lb, ub, is_cont, newub);
+        if (eps_gt(coeff * (ub - lb), maxact - lhs) && !is_neginf(lhs) && !is_posinf(maxact))
+            *lb_t = gdpo_tighten_var_lower(coeff, slack, surplus, maxact_inf, lb, ub, is_cont, newlb);
+    } else {
+        if (eps_gt(coeff * (lb - ub), rhs - minact) && !is_posinf(rhs) && !is_neginf(minact))
+            *lb_t = gdpo_tighten_var_lower(coeff, slack, surplus, minact_inf, lb, ub, is_cont, newlb);
+        if (eps_gt(coeff * (lb - ub), maxact - lhs) && !is_neginf(lhs) && !is_posinf(maxact))
+            *ub_t = gdpo_tighten_var_upper(coeff, slack, surplus, maxact_inf, lb, ub, is_cont, newub);
+    }
+}
+
+/* reference src/propagation_methods.cuh:161-221 (left-to-right summation) */
+gdpo_acts gdpo_activities(int row, const int *col, const int *row_ptr, const double *val,
+                          const double *lb, const double *ub) {
+    gdpo_acts a;
+    double minact = 0.0, maxact = 0.0;
+    int minact_inf = 0, maxact_inf = 0;
+    a.maxactdelta = 0.0;
+    for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
+        const int j = col[k];
+        const double coeff = val[k];
+        const double l = lb[j], u = ub[j];
+        const double delta = fabs(coeff) * (u - l);
+        if (eps_gt(delta, a.maxactdelta)) a.maxactdelta = delta;
+        const int is_min_inf = eps_gt(coeff, 0) ? is_neginf(l) : is_posinf(u);
+        const int is_max_inf = eps_gt(coeff, 0) ? is_posinf(u) : is_neginf(l);
+        minact_inf += is_min_inf;
+        maxact_inf += is_max_inf;
+        if (is_min_inf == 0) minact += coeff > 0 ? coeff * l : coeff * u;
+        if (is_max_inf == 0) maxact += coeff > 0 ? coeff * u : coeff * l;
+    }
+    a.minact = minact; a.maxact = maxact;
+    a.minact_inf = minact_inf; a.maxact_inf = maxact_inf;
+    return a;
+}
+
+/* ---- the GPU path's summation order for split rows ----
+ * Rows longer than split_len are reduced by the GPU in tiles of split_tile
+ * non-zeros: thread t of a 256-thread CTA sums elements t, t+256, ... of the
+ * tile in order, a warp shuffle tree (offsets 16, 8, 4, 2, 1) combines the 32
+ * lanes, the 8 warp partials are combined in warp order and the tile partials
+ * in tile order; |a|(ub-lb) is reduced with an exact max. This emulation lets
+ * the tests compare the GPU bit for bit on every row. With split_len = 0 the
+ * oracle sums every row left to right, the reference's order. */
+static inline void acts_combine(gdpo_acts *a, const gdpo_acts *b) {
+    a->minact = a->minact + b->minact;
+    a->maxact = a->maxact + b->maxact;
+    a->maxactdelta = fmax(a->maxactdelta, b->maxactdelta);
+    a->minact_inf += b->minact_inf;
+    a->maxact_inf += b->maxact_inf;
+}
+
+static gdpo_acts acts_tile(int b, int e, const int *col, const double *val, const double *lb,
+                           const double *ub) {
+    gdpo_acts th[256];
+    for (int t = 0; t < 256; t++) {
+        gdpo_acts a = {0.0, 0.0, 0.0, 0, 0};
+        for (int k = b + t; k < e; k += 256) {
+            const int j = col[k];
+            const double coeff = val[k];
+            const double l = lb[j], u = ub[j];
+            const double delta = fabs(coeff) * (u - l);
+            a.maxactdelta = fmax(a.maxactdelta, delta);
+            const int is_min_inf = eps_gt(coeff, 0) ? is_neginf(l) : is_posinf(u);
+            const int is_max_inf = eps_gt(coeff, 0) ? is_posinf(u) : is_neginf(l);
+            a.minact_inf += is_min_inf;
+            a.maxact_inf += is_max_inf;
+            if (!is_min_inf) a.minact = a.minact + (coeff > 0 ? coeff * l : coeff * u);
+            if (!is_max_inf) a.maxact = a.maxact + (coeff > 0 ? coeff * u : coeff * l);
+        }
+        th[t] = a;
+    }
+    gdpo_acts warp[8];
+    for (int w = 0; w < 8; w++) {
+        gdpo_acts *lane = &th[32 * w];
+        for (int off = 16; off > 0; off >>= 1)
+            for (int i = 0; i < off; i++) acts_combine(&lane[i], &lane[i + off]);
+        warp[w] = lane[0];
+    }
+    gdpo_acts s = warp[0];
+    for (int w = 1; w < 8; w++) acts_combine(&s, &warp[w]);
+    return s;
+}
+
+gdpo_acts gdpo_activities_split(int row, const int *col, const int *row_ptr, const double *val,
+                                const double *lb, const double *ub, int tile) {
+    const int b0 = row_ptr[row], e0 = row_ptr[row + 1];
+    gdpo_acts a = acts_tile(b0, b0 + tile < e0 ? b0 + tile : e0, col, val, lb, ub);
+    for (int b = b0 + tile; b < e0; b += tile) {
+        const gdpo_acts t = acts_tile(b, b + tile < e0 ? b + tile : e0, col, val, lb, ub);
+        acts_combine(&a, &t);
+    }
+    return a;
+}
+
+static inline gdpo_acts row_acts(int row, const int *col, const int *row_ptr, const double *val,
+                                 const double *lb, const double *ub, int split_len, int split_tile) {
+    if (split_len > 0 && row_ptr[row + 1] - row_ptr[row] > split_len)
+        return gdpo_activities_split(row, col, row_ptr, val, lb, ub, split_tile);
+    return gdpo_activities(row, col, row_ptr, val, lb, ub);
+}
+
+/* Infeasibility rule of this project (the reference detects none): bounds
+ * crossing by more than a relative feasibility tolerance. */
+int gdpo_var_infeasible(double lb, double ub) {
+    double s = fabs(lb) > fabs(ub) ? fabs(lb) : fabs(ub);
+    if (s < 1.0) s = 1.0;
+    return (lb - ub) > O_FEASTOL * s;
+}
+
+/* --- order-independent candidate application (max for lb, min for ub) --- */
+static inline void atomic_max_d(double *addr, double v) {
+    uint64_t *p = (uint64_t *)addr;
+    uint64_t old = __atomic_load_n(p, __ATOMIC_RELAXED);
+    for (;;) {
+        double od;
+        memcpy(&od, &old, 8);
+        if (!(v > od)) return;
+        uint64_t nv;
+        memcpy(&nv, &v, 8);
+        if (__atomic_compare_exchange_n(p, &old, nv, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return;
+    }
+}
+static inline void atomic_min_d(double *addr, double v) {
+    uint64_t *p = (uint64_t *)addr;
+    uint64_t old = __atomic_load_n(p, __ATOMIC_RELAXED);
+    for (;;) {
+        double od;
+        memcpy(&od, &old, 8);
+        if (!(v < od)) return;
+        uint64_t nv;
+        memcpy(&nv, &v, 8);
+        if (__atomic_compare_exchange_n(p, &old, nv, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return;
+    }
+}
+
+/* One Jacobi row: reference src/propagators/OMP_propagator.h:58-131, with the
+ * locked "apply if better" replaced by max/min of the gated candidates. */
+static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
+                      const double *lhs, const double *rhs, const double *lb, const double *ub,
+                      const int *vartype, double *lb_out, double *ub_out,
+                      unsigned char *var_changed, int split_len, int split_tile) {
+    const gdpo_acts a = row_acts(row, col, row_ptr, val, lb, ub, split_len, split_tile);
+    int any = 0;
+    if (!gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[row],
+                                    rhs[row], a.maxactdelta))
+        return 0;
+    for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
+        const int j = col[k];
+        int lt, ut;
+        double nl, nu;
+        gdpo_tighten_variable(val[k], lhs[row], rhs[row], a.minact, a.maxact, a.minact_inf,
+                              a.maxact_inf, vartype[j] == 3, lb[j], ub[j], &lt, &nl, &ut, &nu);
+        if (lt) atomic_max_d(&lb_out[j], nl);
+        if (ut) atomic_min_d(&ub_out[j], nu);
+        if (lt || ut) {
+            any = 1;
+            if (var_changed) __atomic_store_n(&var_changed[j], (unsigned char)1, __ATOMIC_RELAXED);
+        }
+    }
+    return any;
+}
+
+int gdpo_jacobi_round(int m, int n, const int *col, const int *row_ptr, const double *val,
+                      const double *lhs, const double *rhs, const double *lb, const double *ub,
+                      const int *vartype, const unsigned char *mark, double *lb_out,
+                      double *ub_out, unsigned char *tight_row, int nthreads) {
+    int change = 0;
+    (void)n;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads > 0 ? nthreads : 1) reduction(| : change)
+#endif
+    for (int i = 0; i < m; i++) {
+        if (mark && !mark[i]) continue;
+        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL, 0, 0);
+        if (t && tight_row) tight_row[i] = 1;
+        change |= t;
+    }
+    return change;
+}
+
+/* CSC of the sparsity pattern (row indices per column), used for marking:
+ * the reference builds it with cuSPARSE (src/kernels/util_kernels.cuh:92-152). */
+static void build_csc(int m, int n, int nnz, const int *col, const int *row_ptr, int *col_ptr,
+                      int *row_idx) {
+    memset(col_ptr, 0, sizeof(int) * (size_t)(n + 1));
+    for (int k = 0; k < nnz; k++) col_ptr[col[k] + 1]++;
+    for (int j = 0; j < n; j++) col_ptr[j + 1] += col_ptr[j];
+    int *fill = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    memcpy(fill, col_ptr, sizeof(int) * (size_t)n);
+    for (int i = 0; i < m; i++)
+        for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) row_idx[fill[col[k]]++] = i;
+    free(fill);
+}
+
+static int check_input(int m, int n, int nnz, const int *col, const int *row_ptr) {
+    if (m < 0 || n < 0 || nnz < 0) return -1;
+    if (row_ptr[0] != 0 || row_ptr[m] != nnz) return -2;
+    for (int i = 0; i < m; i++)
+        if (row_ptr[i + 1] < row_ptr[i]) return -3;
+    for (int k = 0; k < nnz; k++)
+        if (col[k] < 0 || col[k] >= n) return -4;
+    return 0;
+}
+
+/* Fixpoint loop: reference src/propagators/sequential_propagator.h:241-278
+ * (SEQUENTIAL) and src/propagators/OMP_propagator.h:168-211 (JACOBI), with a
+ * configurable round cap and the infeasibility rule checked after each round. */
+int gdpo_propagate(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
+                   const double *lhs, const double *rhs, double *lb, double *ub,
+                   const int *vartype, int schedule, int max_rounds, int nthreads,
+                   gdpo_result *res) {
+    return gdpo_propagate_ex(m, n, nnz, col, row_ptr, val, lhs, rhs, lb, ub, vartype, schedule,
+                             max_rounds, nthreads, 0, 0, res);
+}
+
+int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
+                      const double *lhs, const double *rhs, double *lb, double *ub,
+                      const int *vartype, int schedule, int max_rounds, int nthreads,
+                      int split_len, int split_tile, gdpo_result *res) {
+    gdpo_result r;
+    if (split_tile <= 0) split_len = 0;
+    memset(&r, 0, sizeof(r));
+    r.infeasible_var = -1;
+    if (max_rounds <= 0) max_rounds = O_MAX_ROUNDS;
+    if (m == 0 || n == 0 || nnz == 0) {
+        r.converged = 1;
+        if (res) *res = r;
+        return 0;
+    }
+    const int rc = check_input(m, n, nnz, col, row_ptr);
+    if (rc) return rc;
+
+    for (int j = 0; j < n; j++)
+        if (gdpo_var_infeasible(lb[j], ub[j])) {
+            r.infeasible = 1;
+            r.infeasible_var = j;
+            r.converged = 1;
+            if (res) *res = r;
+            return 0;
+        }
+
+    int *col_ptr = (int *)malloc(sizeof(int) * (size_t)(n + 1));
+    int *row_idx = (int *)malloc(sizeof(int) * (size_t)nnz);
+    build_csc(m, n, nnz, col, row_ptr, col_ptr, row_idx);
+    unsigned char *mark = (unsigned char *)malloc((size_t)m);
+    unsigned char *var_changed = (unsigned char *)calloc((size_t)n, 1);
+    double *lb_snap = (double *)malloc(sizeof(double) * (size_t)n);
+    double *ub_snap = (double *)malloc(sizeof(double) * (size_t)n);
+    memset(mark, 1, (size_t)m); /* every row is marked in round 1 */
+
+    int change = 1;
+    while (r.rounds < max_rounds && change && !r.infeasible) {
+        r.rounds++;
+        change = 0;
+        long long rows = 0, nz = 0, cands = 0;
+        for (int i = 0; i < m; i++)
+            if (mark[i]) { rows++; nz += row_ptr[i + 1] - row_ptr[i]; }
+        if (schedule == GDPO_SCHED_SEQUENTIAL) {
+            /* reference src/propagators/sequential_propagator.h:46-121 */
+            for (int i = 0; i < m; i++) {
+                if (!mark[i]) continue;
+                const gdpo_acts a = gdpo_activities(i, col, row_ptr, val, lb, ub);
+                if (!gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf,
+                                                lhs[i], rhs[i], a.maxactdelta))
+                    continue;
+                for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+                    const int j = col[k];
+                    int lt, ut;
+                    double nl, nu;
+                    gdpo_tighten_variable(val[k], lhs[i], rhs[i], a.minact, a.maxact,
+                                          a.minact_inf, a.maxact_inf, vartype[j] == 3, lb[j],
+                                          ub[j], &lt, &nl, &ut, &nu);
+                    if (lt) lb[j] = nl;
+                    if (ut) ub[j] = nu;
+                    if (lt || ut) { change = 1; var_changed[j] = 1; cands += lt + ut; }
+                }
+            }
+        } else {
+            memcpy(lb_snap, lb, sizeof(double) * (size_t)n);
+            memcpy(ub_snap, ub, sizeof(double) * (size_t)n);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads > 0 ? nthreads : 1) reduction(| : change)
+#endif
+            for (int i = 0; i < m; i++) {
+                if (!mark[i]) continue;
+                change |= jacobi_row(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
+                                     ub, var_changed, split_len, split_tile);
+            }
+        }
+        /* marking for the next round: reference src/propagation_methods.cu:3-13 */
+        memset(mark, 0, (size_t)m);
+        for (int j = 0; j < n; j++) {
+            if (!var_changed[j]) continue;
+            var_changed[j] = 0;
+            if (schedule != GDPO_SCHED_SEQUENTIAL) cands++;
+            for (int k = col_ptr[j]; k < col_ptr[j + 1]; k++) mark[row_idx[k]] = 1;
+            if (!r.infeasible && gdpo_var_infeasible(lb[j], ub[j])) {
+                r.infeasible = 1;
+                r.infeasible_var = j;
+            }
+        }
+        r.rows_processed += rows;
+        r.nnz_processed += nz;
+        r.candidates += cands;
+    }
+    r.converged = !change || r.infeasible;
+
+    free(col_ptr); free(row_idx); free(mark); free(var_changed); free(lb_snap); free(ub_snap);
+    if (res) *res = r;
+    return 0;
+}

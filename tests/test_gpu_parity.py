@@ -1,0 +1,233 @@
+"""GPU parity: the CUDA path through the C-ABI against the oracle and the
+reference's golden outputs.
+
+The GPU runs the deterministic Jacobi schedule. Rows up to thread_row_max
+non-zeros are summed left to right by one lane (the reference's order), longer
+rows in a fixed tile tree that the oracle reproduces (split_len/split_tile),
+so every comparison against the oracle with the same split parameters is bit
+for bit; comparisons against the reference's own outputs are bit for bit where
+no row is split.
+"""
+import numpy as np
+import pytest
+
+import gdp
+import gdpgen
+import oracle
+from gdp_testutil import (GOLDEN_CASES, REF_TEST_EPS, assert_bitexact, assert_bounds_close, clamp_inf,
+                          load_golden, permute)
+
+pytestmark = pytest.mark.gpu
+
+SYNCS = [gdp.CPU_LOOP, gdp.GPU_LOOP, gdp.MEGAKERNEL]
+TRM, TILE = 1024, 4096  # library defaults
+
+
+def gpu(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=0, tile=0, lb=None, ub=None):
+    return gdp.propagate(mip, sync_type=sync, max_rounds=max_rounds, thread_row_max=trm, split_tile=tile, lb=lb,
+                         ub=ub)
+
+
+def check_vs_oracle(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=TRM, tile=TILE):
+    lb, ub, st = gpu(mip, sync, max_rounds, trm, tile)
+    ref = oracle.propagate(mip, oracle.JACOBI, max_rounds=max_rounds, split_len=trm, split_tile=tile, nthreads=8)
+    assert st["rounds"] == ref.rounds
+    assert bool(st["infeasible"]) == ref.infeasible
+    if ref.infeasible:
+        assert st["infeasible_var"] == ref.infeasible_var
+    assert_bitexact(lb, ub, ref.lb, ref.ub, what=f"sync={sync} trm={trm} tile={tile}")
+    return st
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("sync", SYNCS)
+def test_golden_vs_reference_cpu_omp(name, sync):
+    """Bit-exact against the reference's own cpu_omp round function (rows unsplit)."""
+    mip, g = load_golden(name)
+    lb, ub, st = gpu(mip, sync)
+    assert st["rounds"] == int(g["rounds_omp"])
+    assert st["infeasible"] == int(g["infeasible_omp"])
+    assert_bitexact(lb, ub, g["lb_omp"], g["ub_omp"], what=name)
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES])
+def test_golden_vs_reference_cpu_seq(name):
+    """Final bounds against the reference's cpu_seq: exact for integer
+    variables and within 1e-9 rel / 1e-12 abs for continuous ones, except the
+    two fixtures whose fixpoint is only reached in the limit (TwoLines,
+    ATMSynthetic): there both schedules stop where the last improvement falls
+    below GDP_EPS, and the reference's own tolerance (1e-4) applies."""
+    mip, g = load_golden(name)
+    lb, ub, st = gpu(mip)
+    assert st["infeasible"] == int(g["infeasible_seq"])
+    if int(g["infeasible_seq"]):
+        return
+    if name in ("two_lines", "atm_synthetic_2000"):
+        np.testing.assert_allclose(clamp_inf(lb), clamp_inf(g["lb_seq"]), atol=REF_TEST_EPS)
+        np.testing.assert_allclose(clamp_inf(ub), clamp_inf(g["ub_seq"]), atol=REF_TEST_EPS)
+    else:
+        assert_bounds_close(lb, ub, g["lb_seq"], g["ub_seq"], mip.vartype)
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if "analytical" in np.load(
+    __import__("gdp_testutil").GOLDEN / f"{c}.npz").files])
+def test_golden_analytical(name):
+    mip, g = load_golden(name)
+    lb, ub, _ = gpu(mip, gdp.MEGAKERNEL)
+    np.testing.assert_allclose(clamp_inf(ub), clamp_inf(g["ub_analytical"]), atol=REF_TEST_EPS)
+    np.testing.assert_allclose(clamp_inf(lb), clamp_inf(g["lb_analytical"]), atol=REF_TEST_EPS)
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("sync", SYNCS)
+def test_random_small_mip(seed, sync):
+    check_vs_oracle(gdpgen.random_mip(0, seed=100 + seed), sync)
+
+
+@pytest.mark.parametrize("trm,tile", [(4, 3), (8, 5), (16, 1), (2, 256)])
+def test_split_rows_bitexact(trm, tile):
+    """Force rows through the split (multi-CTA) path; the oracle emulates its tree."""
+    mip = gdpgen.random_mip(0, seed=7)
+    for sync in SYNCS:
+        check_vs_oracle(mip, sync, trm=trm, tile=tile)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_power_law_scaled(seed):
+    mip = gdpgen.random_mip(1, seed=seed, m=100_000, n=75_000, len_max=5000, dense_len=20_000, n_dense_rows=4)
+    for sync in (gdp.CPU_LOOP, gdp.MEGAKERNEL):
+        st = check_vs_oracle(mip, sync, trm=1024, tile=4096)
+        assert st["rounds"] >= 2
+
+
+def test_power_law_small_tiles_and_threshold():
+    mip = gdpgen.random_mip(1, seed=5, m=30_000, n=20_000, len_max=3000, dense_len=8000, n_dense_rows=3)
+    check_vs_oracle(mip, gdp.MEGAKERNEL, trm=64, tile=512)
+    check_vs_oracle(mip, gdp.CPU_LOOP, trm=256, tile=1024)
+
+
+def test_chains_many_rounds():
+    mip = gdpgen.chains(6000, chain_max=400, seed=2)
+    st = check_vs_oracle(mip, gdp.MEGAKERNEL, max_rounds=5000)
+    assert st["rounds"] > 100
+
+
+def test_chains_infeasible():
+    mip = gdpgen.chains(6000, chain_max=400, infeasible=True, seed=3)
+    for sync in SYNCS:
+        st = check_vs_oracle(mip, sync, max_rounds=5000)
+        assert st["infeasible"] == 1
+
+
+def test_cover_knapsack():
+    mip = gdpgen.cover_knapsack(20_000, 2_000, 16_000, 2_000, seed=1)
+    for sync in SYNCS:
+        check_vs_oracle(mip, sync)
+
+
+def test_round_cap_and_not_converged():
+    mip, _ = load_golden("two_lines")
+    for sync in SYNCS:
+        lb, ub, st = gpu(mip, sync, max_rounds=5)
+        ref = oracle.propagate(mip, oracle.JACOBI, max_rounds=5)
+        assert st["rounds"] == 5 and not st["converged"]
+        assert_bitexact(lb, ub, ref.lb, ref.ub)
+
+
+def test_initially_infeasible_bounds():
+    mip, _ = load_golden("savelsbergh1")
+    lb = mip.lb.copy()
+    lb[0] = 2.0
+    for sync in SYNCS:
+        _, _, st = gpu(mip, sync, lb=lb)
+        assert st["infeasible"] == 1 and st["rounds"] == 0 and st["infeasible_var"] == 0
+
+
+def test_row_permutation_bitexact():
+    mip = gdpgen.random_mip(0, seed=21)
+    perm = np.random.default_rng(1).permutation(mip.m)
+    a = gpu(mip)
+    b = gpu(permute(mip, row_perm=perm))
+    assert a[2]["rounds"] == b[2]["rounds"]
+    assert_bitexact(a[0], a[1], b[0], b[1])
+
+
+def test_column_permutation():
+    """Metamorphic check as in the reference's permute_mip: a column
+    permutation reorders the sums, so bounds agree within tolerance."""
+    mip = gdpgen.random_mip(0, seed=22)
+    cp = np.random.default_rng(2).permutation(mip.n)
+    a = gpu(mip)
+    b = gpu(permute(mip, col_perm=cp))
+    assert_bounds_close(a[0][cp], a[1][cp], b[0], b[1], mip.vartype[cp], rel=1e-9, abs_=1e-9)
+
+
+def test_context_reuse_branch_and_bound_nodes():
+    """One upload, many node bound vectors (fixings), each equal to a fresh run."""
+    mip = gdpgen.random_mip(0, seed=23)
+    rng = np.random.default_rng(3)
+    ints = np.flatnonzero(mip.vartype != 3)
+    with gdp.Context(mip, sync_type=gdp.MEGAKERNEL) as ctx:
+        for _ in range(5):
+            lb, ub = mip.lb.copy(), mip.ub.copy()
+            fix = rng.choice(ints, size=10, replace=False)
+            v = np.floor(rng.uniform(lb[fix], ub[fix] + 1))
+            lb[fix] = np.minimum(v, ub[fix])
+            ub[fix] = lb[fix]
+            glb, gub, st = ctx.propagate(lb, ub)
+            ref = oracle.propagate(mip, oracle.JACOBI, lb=lb, ub=ub)
+            assert st["rounds"] == ref.rounds and bool(st["infeasible"]) == ref.infeasible
+            assert_bitexact(glb, gub, ref.lb, ref.ub)
+
+
+def test_device_pointer_entry_point():
+    torch = pytest.importorskip("torch")
+    mip = gdpgen.random_mip(0, seed=24)
+    dlb = torch.tensor(mip.lb, dtype=torch.float64, device="cuda")
+    dub = torch.tensor(mip.ub, dtype=torch.float64, device="cuda")
+    with gdp.Context(mip) as ctx:
+        st = ctx.propagate_device(dlb.data_ptr(), dub.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    ref = oracle.propagate(mip, oracle.JACOBI)
+    assert st["rounds"] == ref.rounds
+    assert_bitexact(dlb.cpu().numpy(), dub.cpu().numpy(), ref.lb, ref.ub)
+
+
+def test_reference_python_driver_mirror():
+    """Same call shape as the reference's fileReader/GPUDomPropInterface.py."""
+    mip, g = load_golden("achterberg")
+    for synctype in (0, 1, 2):
+        lbs, ubs = gdp.propagateGPUAtomic(mip.n, mip.m, mip.nnz, list(mip.col), list(mip.row_ptr), list(mip.val),
+                                          list(mip.lhs), list(mip.rhs), list(mip.lb), list(mip.ub),
+                                          list(mip.vartype), synctype=synctype)
+        assert_bitexact(np.array(lbs), np.array(ubs), g["lb_omp"], g["ub_omp"])
+    lbs, ubs = gdp.propagateGPUReduction(mip.n, mip.m, mip.nnz, mip.col, mip.row_ptr, mip.val, mip.lhs, mip.rhs,
+                                         mip.lb, mip.ub, mip.vartype)
+    assert_bitexact(np.array(lbs), np.array(ubs), g["lb_omp"], g["ub_omp"])
+
+
+def test_infinite_bound_forms():
+    """ex1 mixes 1e100 / DBL_MAX / 1e20 infinities (reference test_setups.cuh:614-660)."""
+    mip, g = load_golden("ex1")
+    for sync in SYNCS:
+        lb, ub, st = gpu(mip, sync)
+        assert_bitexact(lb, ub, g["lb_omp"], g["ub_omp"])
+
+
+def test_single_row_and_empty_rows():
+    mip = gdp.MIP(np.array([0, 0, 3, 3], np.int32), np.array([0, 1, 2], np.int32), np.array([1.0, 2.0, -1.5]),
+                  np.array([-1e20, 1.0, -1e20]), np.array([1e20, 4.0, 1e20]), np.zeros(3), np.array([5.0, 5.0, 2.0]),
+                  np.array([1, 3, 3], np.int32))
+    for sync in SYNCS:
+        lb, ub, st = gpu(mip, sync)
+        ref = oracle.propagate(mip, oracle.JACOBI)
+        assert st["rounds"] == ref.rounds
+        assert_bitexact(lb, ub, ref.lb, ref.ub)
+
+
+def test_stats_accounting():
+    mip = gdpgen.random_mip(0, seed=25)
+    _, _, st = gpu(mip, gdp.MEGAKERNEL)
+    assert st["rows_processed"] == st["rounds"] * mip.m
+    assert st["nnz_processed"] == st["rounds"] * mip.nnz
+    assert st["bytes_algorithmic"] == st["rounds"] * (12.0 * mip.nnz + 20.0 * mip.m + 36.0 * mip.n)
+    assert st["device_ms"] > 0 and st["kernel_launches"] >= 2
