@@ -96,6 +96,9 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     lib.gdp_propagate_once.argtypes = _LEGACY_ARGS + [C.POINTER(Options), C.POINTER(Stats)]
     lib.propagateConstraintsGPUAtomicDouble.argtypes = _LEGACY_ARGS + [C.c_int]
     lib.propagateConstraintsGPUReductionDouble.argtypes = _LEGACY_ARGS
+    lib.gdp_propagate_noalloc.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8 + \
+        [C.c_int, C.c_void_p, C.POINTER(Stats)]
+    lib.gdp_propagate_noalloc.restype = C.c_int
     for name in ("gdp_default_options", "gdp_context_create", "gdp_context_destroy", "gdp_propagate",
                  "gdp_propagate_device", "gdp_context_set_options", "gdp_context_layout",
                  "gdp_propagate_once", "propagateConstraintsGPUAtomicDouble",
@@ -242,6 +245,22 @@ class Context:
                                               C.c_void_p(stream_ptr or None), C.byref(st)),
                "gdp_propagate_device")
         return st.as_dict()
+
+
+NOALLOC_MAX_VARS = 1 << 20
+
+
+def propagate_noalloc(n_cons: int, n_vars: int, nnz: int, d_col: int, d_row_ptr: int, d_val: int, d_lhs: int,
+                      d_rhs: int, d_lb: int, d_ub: int, d_vartype: int, max_rounds: int = 0,
+                      stream: int = 0) -> dict:
+    """gdp_propagate_noalloc on device pointers (ints, e.g. torch data_ptr()):
+    the library allocates nothing; bounds d_lb/d_ub are updated in place."""
+    st = Stats()
+    rc = load_library().gdp_propagate_noalloc(int(n_cons), int(n_vars), int(nnz), *(C.c_void_p(p) for p in (
+        d_col, d_row_ptr, d_val, d_lhs, d_rhs, d_lb, d_ub, d_vartype)), int(max_rounds),
+        C.c_void_p(stream or None), C.byref(st))
+    _check(rc, "gdp_propagate_noalloc")
+    return st.as_dict()
 
 
 # ---- mirror of the reference's Python driver (fileReader/GPUDomPropInterface.py) ----

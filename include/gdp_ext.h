@@ -92,6 +92,33 @@ GDP_RETCODE gdp_propagate_once(int n_cons, int n_vars, int nnz, const int *csr_c
                                const double *lhss, const double *rhss, double *lbs, double *ubs,
                                const int *vartypes, const gdp_options *opts, gdp_stats *stats);
 
+/* Propagation that allocates no memory, for callers that cannot call
+ * cudaMalloc (e.g. a solver or framework whose device memory belongs to its
+ * own pool and that propagates many nodes in a loop, where cudaMalloc/cudaFree
+ * would synchronize the device and fragment that pool). No counterpart in the
+ * reference.
+ *   - Every array argument is DEVICE memory (CSR with the reference's meaning,
+ *     bounds in/out); nothing is copied to or from the host except the round
+ *     flags.
+ *   - Working memory is one fixed device array inside the library, sized for
+ *     GDP_NOALLOC_MAX_VARS variables (about 16 MiB); every GPU that loads the
+ *     library holds it until the process exits. n_vars above the limit returns
+ *     GDP_ERROR.
+ *   - The first call on a device looks up that array's device address (once per
+ *     device); make that first call before any stream capture.
+ *   - Calls share the array: calls that overlap on the GPU race and must be
+ *     serialized by the caller. Each call re-initializes it.
+ *   - Rows are summed left to right by one thread each: results equal the
+ *     context path's for rows up to 1024 non-zeros.
+ * stream: CUDA stream (NULL = legacy default stream); the call returns when the
+ * propagation has finished. stats may be NULL (device_ms is not measured). */
+#define GDP_NOALLOC_MAX_VARS (1 << 20)
+GDP_RETCODE gdp_propagate_noalloc(int n_cons, int n_vars, int nnz, const int *d_csr_col_indices,
+                                  const int *d_csr_row_ptrs, const double *d_csr_vals,
+                                  const double *d_lhss, const double *d_rhss, double *d_lbs,
+                                  double *d_ubs, const int *d_vartypes, int max_rounds, void *stream,
+                                  gdp_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif
