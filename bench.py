@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0)
     ap.add_argument("--max-rounds", type=int, default=0)
+    ap.add_argument("--marking", type=int, default=1, help="1: process only rows with a changed variable")
+    ap.add_argument("--trm", type=int, default=0, help="thread_row_max (0: library default)")
+    ap.add_argument("--tile", type=int, default=0, help="split_tile (0: library default)")
     return ap.parse_args()
 
 
@@ -211,7 +214,8 @@ def main():
     sync = {"megakernel": gdp.MEGAKERNEL, "cpu_loop": gdp.CPU_LOOP, "gpu_loop": gdp.GPU_LOOP}[args.sync]
     mip, gen_s = make_instance(args, rank)
     t0 = time.perf_counter()
-    ctx = gdp.Context(mip, sync_type=sync, max_rounds=args.max_rounds)
+    ctx = gdp.Context(mip, sync_type=sync, max_rounds=args.max_rounds, thread_row_max=args.trm,
+                      split_tile=args.tile, use_marking=args.marking)
     ctx_s = time.perf_counter() - t0
     layout = ctx.layout()
     stream = torch.cuda.current_stream()
@@ -271,7 +275,8 @@ def main():
     for _ in range(max(1, args.e2e_steps)):
         lb, ub = list(), list()
         t1 = time.perf_counter()
-        lbs, ubs, _ = gdp.propagate(mip, sync_type=sync, max_rounds=args.max_rounds)
+        lbs, ubs, _ = gdp.propagate(mip, sync_type=sync, max_rounds=args.max_rounds, thread_row_max=args.trm,
+                                    split_tile=args.tile, use_marking=args.marking)
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
     h2d = (mip.nnz * 12 + (mip.m + 1) * 4 + mip.m * 16 + mip.n * 20)
     d2h = mip.n * 16
@@ -281,7 +286,8 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": rounds,
                        "converged": bool(stats[-1]["converged"]), "infeasible": bool(stats[-1]["infeasible"]),
-                       "sync": args.sync, "layout": layout, "parallelism": "replicas" if ws > 1 else "single",
+                       "sync": args.sync, "layout": layout, "marking": args.marking,
+                       "rows_processed": stats[-1]["rows_processed"], "nnz_processed": stats[-1]["nnz_processed"], "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (CSR %.0f MB vs 129 MB L2)" % (mip.nnz * 12 / 1e6),
                        "scale": args.scale},
             "hbm_gbs": achieved, "nnz_per_s": mip.nnz * rounds / (ms_step * 1e-3),

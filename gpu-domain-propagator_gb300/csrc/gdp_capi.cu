@@ -67,9 +67,10 @@ GDP_RETCODE gdp_default_options(gdp_options *o) {
     *o = gdp_options{};
     o->max_rounds = GDP_MAX_NUM_ROUNDS;
     o->sync_type = CPU_LOOP;
-    o->thread_row_max = 1024;
-    o->split_tile = 4096;
+    o->thread_row_max = 32;
+    o->split_tile = 1024;
     o->device = 0;
+    o->use_marking = 1;
     return GDP_OKAY;
 }
 
@@ -133,6 +134,9 @@ GDP_RETCODE gdp_context_set_options(gdp_context *ctx, int max_rounds, int sync_t
     ctx->impl.opts.max_rounds = max_rounds > 0 ? max_rounds : GDP_MAX_NUM_ROUNDS;
     ctx->impl.opts.sync_type = sync_type;
     ctx->impl.P.max_rounds = ctx->impl.opts.max_rounds;
+    // the GPU_LOOP graph holds the round cap in its captured kernel arguments
+    if (ctx->impl.graph_exec) { cudaGraphExecDestroy(ctx->impl.graph_exec); ctx->impl.graph_exec = nullptr; }
+    if (ctx->impl.graph) { cudaGraphDestroy(ctx->impl.graph); ctx->impl.graph = nullptr; }
     return GDP_OKAY;
 }
 

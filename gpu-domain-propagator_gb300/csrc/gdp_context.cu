@@ -1,19 +1,19 @@
 // gdp_context.cu -- host side of the propagator: input validation, device
-// layout (SELL slices of thread rows, tiles of split rows), device buffers and
-// the round-loop drivers.
+// layout (SELL slices of thread rows, warp tiles of split rows, work items,
+// marking index), device buffers and the three round-loop drivers.
 //
 // Replaces the reference's per-call host driver propagateConstraintsGPUAtomic
 // (src/propagators/GPU_propagator.cuh:98-268): uploads, row binning
-// (fill_row_blocks, src/kernels/util_kernels.cu:12-62) and the three round
-// loops. CUDA errors return GDP_ERROR with a message instead of exit()
-// (reference src/cuda_def.cuh:10-15).
+// (fill_row_blocks, src/kernels/util_kernels.cu:12-62) and the round loops
+// (CPU_LOOP :160-204, GPU_LOOP :146-159, MEGAKERNEL :205-255). CUDA errors
+// return GDP_ERROR with a message instead of exit() (src/cuda_def.cuh:10-15).
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -63,16 +63,20 @@ GDP_RETCODE validate_csr(int m, int n, int nnz, const int *col, const int *row_p
     }
     for (int i = 0; i < m; i++)
         if (row_ptr[i + 1] < row_ptr[i]) { set_error("csr_row_ptrs is not monotone"); return GDP_ERROR; }
-    for (int k = 0; k < nnz; k++)
-        if ((unsigned)col[k] >= (unsigned)n) {
-            set_error("column index out of range at non-zero " + std::to_string(k));
-            return GDP_ERROR;
-        }
-    for (int k = 0; k < nnz; k++)
-        if (!std::isfinite(val[k])) {
-            set_error("non-finite coefficient at non-zero " + std::to_string(k));
-            return GDP_ERROR;
-        }
+    long long bad_col = -1, bad_val = -1;
+#pragma omp parallel for reduction(max : bad_col, bad_val) schedule(static)
+    for (int k = 0; k < nnz; k++) {
+        if ((unsigned)col[k] >= (unsigned)n) bad_col = std::max(bad_col, (long long)k);
+        if (!std::isfinite(val[k])) bad_val = std::max(bad_val, (long long)k);
+    }
+    if (bad_col >= 0) {
+        set_error("column index out of range at non-zero " + std::to_string(bad_col));
+        return GDP_ERROR;
+    }
+    if (bad_val >= 0) {
+        set_error("non-finite coefficient at non-zero " + std::to_string(bad_val));
+        return GDP_ERROR;
+    }
     for (int j = 0; j < n; j++)
         if (vartype[j] != 0 && vartype[j] != 1 && vartype[j] != 3) {
             set_error("vartype must be 0, 1 or 3 (variable " + std::to_string(j) + ")");
@@ -89,8 +93,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     gdp_default_options(&opts);
     if (o) opts = *o;
     if (opts.max_rounds <= 0) opts.max_rounds = GDP_MAX_NUM_ROUNDS;
-    if (opts.thread_row_max <= 0) opts.thread_row_max = 1024;
-    if (opts.split_tile <= 0) opts.split_tile = 4096;
+    if (opts.thread_row_max <= 0) opts.thread_row_max = 32;
+    if (opts.split_tile <= 0) opts.split_tile = 1024;
+    if (opts.use_marking < 0) opts.use_marking = 1;
+    if (opts.thread_row_max > (1 << 20)) opts.thread_row_max = 1 << 20;
+    if (opts.split_tile > (1 << 24)) opts.split_tile = 1 << 24;
     if (opts.sync_type < CPU_LOOP || opts.sync_type > MEGAKERNEL) {
         set_error("Unknown sync type");
         return GDP_ERROR;
@@ -107,60 +114,75 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opts.device));
     n_sms = sms;
 
-    // ---- row binning (host) ----
-    const int Lt = opts.thread_row_max;
+    // ---- row binning (SELL-g) ----
+    // g = 1 for rows up to thread_row_max; g = smallest power of two >= len/32
+    // (2..32) up to split_tile; longer rows are split into warp tiles.
+    const int Lt = opts.thread_row_max, Ls = std::max(opts.split_tile, Lt);
+    auto lanes_of = [&](int L) {
+        if (L <= Lt) return 1;
+        int g = 2;
+        while (g < 32 && g * 32 < L) g <<= 1;
+        return g;
+    };
     std::vector<int> len(m);
-    int max_len = 0;
-    for (int i = 0; i < m; i++) {
-        len[i] = row_ptr[i + 1] - row_ptr[i];
-        max_len = std::max(max_len, len[i]);
-    }
-    // counting sort of thread rows by length, longest first, stable by row index
-    std::vector<int> cnt(Lt + 2, 0);
-    std::vector<int> split_rows;
+    for (int i = 0; i < m; i++) len[i] = row_ptr[i + 1] - row_ptr[i];
+    std::vector<int> sell_rows, split_rows;
     for (int i = 0; i < m; i++) {
         if (len[i] == 0) continue;
-        if (len[i] <= Lt) cnt[len[i]]++;
+        if (len[i] <= Ls) sell_rows.push_back(i);
         else split_rows.push_back(i);
     }
-    std::vector<int> start(Lt + 2, 0);
-    int acc = 0;
-    for (int L = Lt; L >= 1; L--) { start[L] = acc; acc += cnt[L]; }
-    const int ns = acc;
-    std::vector<int> order(ns);
-    for (int i = 0; i < m; i++)
-        if (len[i] >= 1 && len[i] <= Lt) order[start[len[i]]++] = i;
-    std::stable_sort(split_rows.begin(), split_rows.end(),
-                     [&](int a, int b) { return len[a] > len[b]; });
+    // by lanes per row (widest first), then length (longest first), stable
+    std::stable_sort(sell_rows.begin(), sell_rows.end(), [&](int a, int b) {
+        const int ga = lanes_of(len[a]), gb = lanes_of(len[b]);
+        return ga != gb ? ga > gb : len[a] > len[b];
+    });
+    std::stable_sort(split_rows.begin(), split_rows.end(), [&](int a, int b) { return len[a] > len[b]; });
+    const int ns = (int)sell_rows.size();
+    const std::vector<int> &order = sell_rows;  // row position -> original row
 
     n_srows = ns;
-    n_slices = (ns + 31) / 32;
-    std::vector<long long> slice_ptr(n_slices + 1, 0);
-    for (int s = 0; s < n_slices; s++) slice_ptr[s + 1] = slice_ptr[s] + 32LL * len[order[32 * s]];
+    std::vector<long long> slice_ptr(1, 0);
+    std::vector<int> slice_row0(1, 0), slice_lg;
+    for (int p = 0; p < ns;) {
+        const int g = lanes_of(len[order[p]]);
+        int lg = 0;
+        while ((1 << lg) < g) lg++;
+        int q = p;
+        const int per = 32 / g;
+        while (q < ns && q - p < per && lanes_of(len[order[q]]) == g) q++;
+        const long long width = (len[order[p]] + g - 1) / g;
+        slice_ptr.push_back(slice_ptr.back() + 32LL * width);
+        slice_row0.push_back(q);
+        slice_lg.push_back(lg);
+        p = q;
+    }
+    n_slices = (int)slice_lg.size();
+    if (slice_lg.empty()) slice_lg.push_back(0);
     sell_elems = slice_ptr[n_slices];
     std::vector<int> sell_col((size_t)std::max<long long>(sell_elems, 1), 0);
     std::vector<double> sell_val((size_t)std::max<long long>(sell_elems, 1), 0.0);
     std::vector<int> srow_len(std::max(ns, 1));
     std::vector<double> srow_lhs(std::max(ns, 1)), srow_rhs(std::max(ns, 1));
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(dynamic, 64)
     for (int s = 0; s < n_slices; s++) {
-        for (int l = 0; l < 32; l++) {
-            const int r = 32 * s + l;
-            if (r >= ns) break;
-            const int i = order[r];
-            srow_len[r] = len[i];
-            srow_lhs[r] = lhs[i];
-            srow_rhs[r] = rhs[i];
+        const int lg = slice_lg[s], g = 1 << lg;
+        for (int p = slice_row0[s]; p < slice_row0[s + 1]; p++) {
+            const int i = order[p], rl = p - slice_row0[s];
+            srow_len[p] = len[i];
+            srow_lhs[p] = lhs[i];
+            srow_rhs[p] = rhs[i];
             for (int k = 0; k < len[i]; k++) {
-                const long long e = slice_ptr[s] + 32LL * k + l;
+                const long long e = slice_ptr[s] + 32LL * (k >> lg) + (rl << lg) + (k & (g - 1));
                 sell_col[e] = col[row_ptr[i] + k];
                 sell_val[e] = val[row_ptr[i] + k];
             }
         }
     }
-    // split rows: CSR-contiguous, tiles of split_tile non-zeros
+    // split rows: CSR-contiguous, warp tiles of split_tile non-zeros
     n_lrows = (int)split_rows.size();
-    std::vector<int> lrow_ptr(n_lrows + 1, 0), lrow_tile0(n_lrows + 1, 0);
+    std::vector<long long> lrow_ptr(n_lrows + 1, 0);
+    std::vector<int> lrow_tile0(n_lrows + 1, 0);
     std::vector<double> lrow_lhs(std::max(n_lrows, 1)), lrow_rhs(std::max(n_lrows, 1));
     std::vector<int> tile_row, tile_begin, tile_end;
     for (int r = 0; r < n_lrows; r++) {
@@ -169,10 +191,10 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         lrow_lhs[r] = lhs[i];
         lrow_rhs[r] = rhs[i];
         lrow_tile0[r] = (int)tile_row.size();
-        for (int b = lrow_ptr[r]; b < lrow_ptr[r + 1]; b += opts.split_tile) {
+        for (long long b = lrow_ptr[r]; b < lrow_ptr[r + 1]; b += opts.split_tile) {
             tile_row.push_back(r);
-            tile_begin.push_back(b);
-            tile_end.push_back(std::min(b + opts.split_tile, lrow_ptr[r + 1]));
+            tile_begin.push_back((int)b);
+            tile_end.push_back((int)std::min(b + opts.split_tile, lrow_ptr[r + 1]));
         }
     }
     lrow_tile0[n_lrows] = (int)tile_row.size();
@@ -186,9 +208,20 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         std::memcpy(&lcol[lrow_ptr[r]], &col[row_ptr[i]], sizeof(int) * (size_t)len[i]);
         std::memcpy(&lval[lrow_ptr[r]], &val[row_ptr[i]], sizeof(double) * (size_t)len[i]);
     }
-    rows_nonempty = (long long)ns + n_lrows;
-    nnz_rows = nnz;
-
+    // work items of the activity phase, heaviest first (slices: 32 x width non-zeros)
+    std::vector<int> items;
+    items.reserve((size_t)n_slices + n_tiles);
+    {
+        std::vector<std::pair<long long, int>> cost;
+        cost.reserve((size_t)n_slices + n_tiles);
+        for (int s = 0; s < n_slices; s++) cost.emplace_back(slice_ptr[s + 1] - slice_ptr[s], s);
+        for (int t = 0; t < n_tiles; t++) cost.emplace_back((long long)(tile_end[t] - tile_begin[t]), -t - 1);
+        std::stable_sort(cost.begin(), cost.end(),
+                         [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
+                             return a.first > b.first;
+                         });
+        for (auto &c : cost) items.push_back(c.second);
+    }
     // ---- upload ----
     auto up = [&](const void *src, size_t bytes) -> void * {
         void *d = arena.alloc_bytes(bytes);
@@ -197,117 +230,211 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             return nullptr;
         return d;
     };
-#define GDP_UP(dst, T, vec, cnt_)                                                        \
-    do {                                                                               \
-        dst = (T *)up((vec).data(), sizeof(T) * (size_t)(cnt_));                       \
-        if (!dst) { set_error("device allocation/upload failed for " #vec); return GDP_ERROR; } \
+#define GDP_UP(dst, T, vec)                                                                         \
+    do {                                                                                           \
+        dst = (T *)up((vec).data(), sizeof((vec)[0]) * (vec).size());                              \
+        if (!dst) { set_error("device allocation/upload failed for " #vec); return GDP_ERROR; }     \
     } while (0)
-    const long long *d_slice_ptr; const int *d_sell_col; const double *d_sell_val;
-    const int *d_srow_len; const double *d_srow_lhs, *d_srow_rhs;
-    GDP_UP(d_slice_ptr, const long long, slice_ptr, n_slices + 1);
-    GDP_UP(d_sell_col, const int, sell_col, sell_col.size());
-    GDP_UP(d_sell_val, const double, sell_val, sell_val.size());
-    GDP_UP(d_srow_len, const int, srow_len, srow_len.size());
-    GDP_UP(d_srow_lhs, const double, srow_lhs, srow_lhs.size());
-    GDP_UP(d_srow_rhs, const double, srow_rhs, srow_rhs.size());
-    const int *d_lcol, *d_lrow_tile0, *d_tile_row, *d_tile_begin, *d_tile_end;
-    const double *d_lval, *d_lrow_lhs, *d_lrow_rhs;
-    GDP_UP(d_lcol, const int, lcol, lcol.size());
-    GDP_UP(d_lval, const double, lval, lval.size());
-    GDP_UP(d_lrow_lhs, const double, lrow_lhs, lrow_lhs.size());
-    GDP_UP(d_lrow_rhs, const double, lrow_rhs, lrow_rhs.size());
-    GDP_UP(d_lrow_tile0, const int, lrow_tile0, lrow_tile0.size());
+    std::memset(&P, 0, sizeof(P));
+    P.n = n;
+    P.n_srows = n_srows;
+    P.n_slices = n_slices;
+    GDP_UP(P.slice_ptr, const long long, slice_ptr);
+    GDP_UP(P.slice_row0, const int, slice_row0);
+    GDP_UP(P.slice_lg, const int, slice_lg);
+    GDP_UP(P.sell_col, const int, sell_col);
+    GDP_UP(P.sell_val, const double, sell_val);
+    GDP_UP(P.srow_len, const int, srow_len);
+    GDP_UP(P.srow_lhs, const double, srow_lhs);
+    GDP_UP(P.srow_rhs, const double, srow_rhs);
+    P.n_lrows = n_lrows;
+    P.n_tiles = n_tiles;
+    GDP_UP(P.lcol, const int, lcol);
+    GDP_UP(P.lval, const double, lval);
+    GDP_UP(P.lrow_lhs, const double, lrow_lhs);
+    GDP_UP(P.lrow_rhs, const double, lrow_rhs);
+    GDP_UP(P.lrow_tile0, const int, lrow_tile0);
     if (tile_row.empty()) { tile_row.push_back(0); tile_begin.push_back(0); tile_end.push_back(0); }
-    GDP_UP(d_tile_row, const int, tile_row, tile_row.size());
-    GDP_UP(d_tile_begin, const int, tile_begin, tile_begin.size());
-    GDP_UP(d_tile_end, const int, tile_end, tile_end.size());
+    GDP_UP(P.tile_row, const int, tile_row);
+    GDP_UP(P.tile_begin, const int, tile_begin);
+    GDP_UP(P.tile_end, const int, tile_end);
+    std::vector<int> mtiles;
+    for (int r = 0; r < n_lrows; r++)
+        if (lrow_tile0[r + 1] - lrow_tile0[r] > 1)
+            for (int t = lrow_tile0[r]; t < lrow_tile0[r + 1]; t++) mtiles.push_back(t);
+    P.n_mtiles = (int)mtiles.size();
+    if (mtiles.empty()) mtiles.push_back(0);
+    GDP_UP(P.mtiles, const int, mtiles);
+    P.n_items = (int)items.size();
+    if (items.empty()) items.push_back(0);
+    GDP_UP(P.items, const int, items);
+    P.use_marking = opts.use_marking < 0 ? 1 : (opts.use_marking > 2 ? 2 : opts.use_marking);
+    // adaptive marking: mark when a round tightened fewer bounds than 1/16 of the variables
+    P.mark_threshold = (unsigned)std::max(1, n / 16);
     std::vector<unsigned char> is_cont(std::max(n, 1), 0);
     for (int j = 0; j < n; j++) is_cont[j] = vartype[j] == GDP_CONTINUOUS ? 1 : 0;
-    const unsigned char *d_is_cont;
-    GDP_UP(d_is_cont, const unsigned char, is_cont, is_cont.size());
+    GDP_UP(P.is_cont, const unsigned char, is_cont);
 #undef GDP_UP
-
-    RowActsPOD *d_tile_part = (RowActsPOD *)arena.alloc_bytes(sizeof(RowActsPOD) * (size_t)std::max(n_tiles, 1));
+    const int npos = std::max(ns + n_lrows, 1);
+    const int n_words = (n + 31) / 32;
+    P.tile_part = (TilePart *)arena.alloc_bytes(sizeof(TilePart) * (size_t)std::max(n_tiles, 1));
+    P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);
+    P.bnd = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
+    P.bnd_nxt = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
+    P.chg = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * (size_t)std::max(n_words, 1));
+    P.n_chg_words = n_words;
+    P.flags = (RoundFlags *)arena.alloc_bytes(sizeof(RoundFlags) * 3);
+    P.barrier = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 2);
+    P.queue = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 4);
+    P.max_rounds = opts.max_rounds;
     d_lb = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     d_ub = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    d_lb_nxt = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    d_ub_nxt = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    const int n_words = (n + 31) / 32;
-    unsigned *d_chg = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * (size_t)std::max(n_words, 1));
-    d_flags = (RoundFlags *)arena.alloc_bytes(sizeof(RoundFlags) * 3);
-    d_barrier = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 2);
-    if (!d_tile_part || !d_lb || !d_ub || !d_lb_nxt || !d_ub_nxt || !d_chg || !d_flags || !d_barrier) {
+    if (!P.tile_part || !P.mark || !P.bnd || !P.bnd_nxt || !P.chg || !P.flags || !P.barrier || !P.queue ||
+        !d_lb || !d_ub) {
         set_error("device allocation failed");
         return GDP_ERROR;
     }
-    GDP_CUDA(cudaMemsetAsync(d_chg, 0, sizeof(unsigned) * (size_t)std::max(n_words, 1), stream));
 
-    std::memset(&P, 0, sizeof(P));
-    P.n = n;
-    P.n_srows = n_srows; P.n_slices = n_slices;
-    P.slice_ptr = d_slice_ptr; P.sell_col = d_sell_col; P.sell_val = d_sell_val;
-    P.srow_len = d_srow_len; P.srow_lhs = d_srow_lhs; P.srow_rhs = d_srow_rhs;
-    P.n_lrows = n_lrows; P.n_tiles = n_tiles;
-    P.lcol = d_lcol; P.lval = d_lval; P.lrow_lhs = d_lrow_lhs; P.lrow_rhs = d_lrow_rhs;
-    P.lrow_tile0 = d_lrow_tile0; P.tile_row = d_tile_row; P.tile_begin = d_tile_begin;
-    P.tile_end = d_tile_end; P.tile_part = d_tile_part;
-    P.lb = d_lb; P.ub = d_ub; P.lb_nxt = d_lb_nxt; P.ub_nxt = d_ub_nxt;
-    P.is_cont = d_is_cont; P.chg = d_chg; P.n_chg_words = n_words;
-    P.flags = d_flags; P.barrier = d_barrier;
-    P.max_rounds = opts.max_rounds;
-
-    finalize_blocks = std::max(1, std::min((n_words + kFinalizeThreads - 1) / kFinalizeThreads, 4 * n_sms));
-    int bps = 0;
-    GDP_CUDA(megakernel_occupancy(kMegaThreads, &bps));
-    mega_grid = std::max(1, bps) * n_sms;
+    vec_blocks = std::max(1, std::min((std::max(n, npos) + 255) / 256, 8 * n_sms));
+    // marking index (variable -> row positions), built on the device from the layout
+    if (P.use_marking) {
+        int *vp = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1));
+        int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
+        int *scratch = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1 + (n + 1 + 1023) / 1024 + 1));
+        if (!vp || !vpos || !scratch) { set_error("device allocation failed (marking index)"); return GDP_ERROR; }
+        GDP_CUDA(build_marking_index(P, vp, vpos, scratch, 8 * n_sms, stream));
+        P.var_ptr = vp;
+        P.var_pos = vpos;
+    }
+    int act_bps = 0, cand_bps = 0, mega_bps = 0;
+    GDP_CUDA(phase_occupancy(&act_bps, &cand_bps, &mega_bps));
+    act_blocks = std::max(1, std::min(act_bps * n_sms, (P.n_items + kWarpsPerCta - 1) / kWarpsPerCta));
+    cand_blocks = std::max(1, std::min(cand_bps * n_sms, (P.n_mtiles + kWarpsPerCta - 1) / kWarpsPerCta));
+    mega_grid = std::max(1, mega_bps) * n_sms;
     GDP_CUDA(cudaStreamSynchronize(stream));
     return GDP_OKAY;
 }
 
 Context::~Context() {
     if (stream) cudaStreamSynchronize(stream);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (h_flags) cudaFreeHost(h_flags);
     if (stream) cudaStreamDestroy(stream);
 }
 
-// Runs the round loop on P.lb/P.ub (already holding the input bounds; nxt
-// holding a copy). Fills the round statistics.
-GDP_RETCODE Context::run_rounds(cudaStream_t s, gdp_stats *st) {
+// ---- drivers ---------------------------------------------------------------
+// CPU_LOOP: the host launches each round's phases and reads the flags.
+GDP_RETCODE Context::rounds_cpu_loop(cudaStream_t s, int *launches) {
+    GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
+    GDP_CUDA(cudaStreamSynchronize(s));
+    bool go = !h_flags[0].infeasible;
+    for (int r = 1; go && r <= opts.max_rounds; r++) {
+        GDP_CUDA(launch_round_begin(P, s));
+        GDP_CUDA(launch_activity_phase(P, act_blocks, s));
+        GDP_CUDA(launch_candidate_phase(P, cand_blocks, s));
+        GDP_CUDA(launch_finalize(P, vec_blocks, s));
+        *launches += 2 + (P.n_items > 0) + (P.n_mtiles > 0);
+        GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
+        GDP_CUDA(cudaStreamSynchronize(s));
+        go = h_flags[0].change && !h_flags[0].infeasible;
+    }
+    return GDP_OKAY;
+}
+
+// GPU_LOOP: one CUDA graph whose conditional WHILE node repeats the round's
+// phase kernels until the condition kernel clears it -- the device-driven loop
+// the reference built with dynamic parallelism (src/kernels/atomic_kernel.cuh:452-503).
+GDP_RETCODE Context::build_graph(cudaStream_t s) {
+    cudaGraph_t g = nullptr;
+    GDP_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    GDP_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
+    // cudaGraphNodeParams has no usable default constructor in C++: zero a raw buffer
+    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+    std::memset(cp_buf, 0, sizeof(cp_buf));
+    cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    GDP_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t cs;
+    GDP_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    GDP_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    int rc = launch_round_begin(P, cs);
+    if (!rc) rc = launch_activity_phase(P, act_blocks, cs);
+    if (!rc) rc = launch_candidate_phase(P, cand_blocks, cs);
+    if (!rc) rc = launch_finalize(P, vec_blocks, cs);
+    if (!rc) rc = launch_condition(P, (unsigned long long)h, cs);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cs, &captured);
+    cudaStreamDestroy(cs);
+    (void)s;
+    if (rc || ec != cudaSuccess) {
+        cudaGraphDestroy(g);
+        set_error(std::string("GPU_LOOP graph capture failed: ") +
+                  cudaGetErrorString(rc ? (cudaError_t)rc : ec));
+        return GDP_ERROR;
+    }
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&ge, g, 0);
+    if (ei != cudaSuccess) {
+        cudaGraphDestroy(g);
+        set_error(std::string("GPU_LOOP graph instantiation failed: ") + cudaGetErrorString(ei));
+        return GDP_ERROR;
+    }
+    graph = g;
+    graph_exec = ge;
+    return GDP_OKAY;
+}
+
+GDP_RETCODE Context::rounds_gpu_loop(cudaStream_t s, int *launches) {
+    if (!graph_exec && build_graph(s) != GDP_OKAY) return GDP_ERROR;
+    GDP_CUDA(cudaGraphLaunch(graph_exec, s));
+    GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
+    GDP_CUDA(cudaStreamSynchronize(s));
+    *launches += h_flags[0].rounds * (3 + (P.n_items > 0) + (P.n_mtiles > 0)) + 1;
+    return GDP_OKAY;
+}
+
+// MEGAKERNEL: every round in one persistent cooperative launch.
+GDP_RETCODE Context::rounds_megakernel(cudaStream_t s, int *launches) {
+    GDP_CUDA(launch_megakernel(P, mega_grid, s));
+    *launches += 1;
+    GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
+    GDP_CUDA(cudaStreamSynchronize(s));
+    return GDP_OKAY;
+}
+
+GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_out, double *ub_out,
+                         cudaStream_t s, gdp_stats *st) {
+    P.max_rounds = opts.max_rounds;
     RoundFlags init[3];
     std::memset(init, 0, sizeof(init));
     init[0].infeasible_var = INT_MAX;
     GDP_CUDA(cudaMemcpyAsync(P.flags, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    int launches = 0;
-    GDP_CUDA(launch_check_bounds(P, finalize_blocks, s));
-    launches++;
+    GDP_CUDA(cudaMemsetAsync(P.queue, 0, sizeof(unsigned) * 4, s));
+    GDP_CUDA(cudaMemsetAsync(P.barrier, 0, sizeof(unsigned) * 2, s));
+    GDP_CUDA(cudaMemsetAsync(P.chg, 0, sizeof(unsigned) * (size_t)std::max(P.n_chg_words, 1), s));
+    GDP_CUDA(launch_interleave(P, lb_in, ub_in, vec_blocks, s));
+    GDP_CUDA(launch_mark_all(P, vec_blocks, s));  // clear round stamps of earlier propagations
+    GDP_CUDA(launch_check_bounds(P, vec_blocks, s));
+    int launches = 3;
     GDP_CUDA(cudaEventRecord(ev0, s));
-    if (opts.sync_type == MEGAKERNEL) {
-        GDP_CUDA(cudaMemsetAsync(P.barrier, 0, sizeof(unsigned) * 2, s));
-        GDP_CUDA(launch_megakernel(P, mega_grid, kMegaThreads, s));
-        launches++;
-        GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
-        GDP_CUDA(cudaEventRecord(ev1, s));
-        GDP_CUDA(cudaStreamSynchronize(s));
-    } else {
-        GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
-        GDP_CUDA(cudaStreamSynchronize(s));
-        bool go = !h_flags[0].infeasible;
-        for (int r = 1; go && r <= opts.max_rounds; r++) {
-            GDP_CUDA(launch_round_begin(P, s));
-            GDP_CUDA(launch_split_partial(P, s));
-            GDP_CUDA(launch_sell_round(P, s));
-            GDP_CUDA(launch_split_cand(P, s));
-            GDP_CUDA(launch_finalize(P, finalize_blocks, s));
-            launches += 2 + (n_slices > 0) + 2 * (n_tiles > 0);
-            GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
-            GDP_CUDA(cudaStreamSynchronize(s));
-            go = h_flags[0].change && !h_flags[0].infeasible;
-        }
-        GDP_CUDA(cudaEventRecord(ev1, s));
-        GDP_CUDA(cudaStreamSynchronize(s));
-    }
+    GDP_RETCODE rc;
+    if (opts.sync_type == MEGAKERNEL) rc = rounds_megakernel(s, &launches);
+    else if (opts.sync_type == GPU_LOOP) rc = rounds_gpu_loop(s, &launches);
+    else rc = rounds_cpu_loop(s, &launches);
+    if (rc != GDP_OKAY) return rc;
+    GDP_CUDA(cudaEventRecord(ev1, s));
+    GDP_CUDA(launch_deinterleave(P, lb_out, ub_out, vec_blocks, s));
+    launches++;
+    GDP_CUDA(cudaStreamSynchronize(s));
     const RoundFlags &f = h_flags[0];
     if (f.error != kErrNone) {
         set_error("device error " + std::to_string(f.error) + " (grid barrier wait exceeded its limit)");
@@ -320,14 +447,13 @@ GDP_RETCODE Context::run_rounds(cudaStream_t s, gdp_stats *st) {
         st->rounds = f.rounds;
         st->infeasible = f.infeasible;
         st->infeasible_var = f.infeasible ? f.infeasible_var : -1;
-        // converged: the last executed round changed nothing, or infeasible
         st->converged = (f.infeasible || !f.change) ? 1 : 0;
         st->device_error = f.error;
         st->kernel_launches = launches;
-        st->changed_vars = f.changed_vars;
-        st->rows_processed = (long long)f.rounds * rows_nonempty;
-        st->nnz_processed = (long long)f.rounds * nnz_rows;
-        st->bytes_algorithmic = (double)f.rounds * (12.0 * nnz_rows + 20.0 * rows_nonempty + 36.0 * n);
+        st->changed_vars = (long long)f.changed_vars;
+        st->rows_processed = (long long)f.rows_proc;
+        st->nnz_processed = (long long)f.nnz_proc;
+        st->bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc + 36.0 * n * (double)f.rounds;
         st->device_ms = ms;
     }
     return GDP_OKAY;
@@ -337,10 +463,7 @@ GDP_RETCODE Context::propagate_host(double *lbs, double *ubs, gdp_stats *st) {
     const size_t bytes = sizeof(double) * (size_t)n;
     GDP_CUDA(cudaMemcpyAsync(d_lb, lbs, bytes, cudaMemcpyHostToDevice, stream));
     GDP_CUDA(cudaMemcpyAsync(d_ub, ubs, bytes, cudaMemcpyHostToDevice, stream));
-    P.lb = d_lb; P.ub = d_ub;
-    GDP_CUDA(cudaMemcpyAsync(d_lb_nxt, d_lb, bytes, cudaMemcpyDeviceToDevice, stream));
-    GDP_CUDA(cudaMemcpyAsync(d_ub_nxt, d_ub, bytes, cudaMemcpyDeviceToDevice, stream));
-    if (run_rounds(stream, st) != GDP_OKAY) return GDP_ERROR;
+    if (run(d_lb, d_ub, d_lb, d_ub, stream, st) != GDP_OKAY) return GDP_ERROR;
     GDP_CUDA(cudaMemcpyAsync(lbs, d_lb, bytes, cudaMemcpyDeviceToHost, stream));
     GDP_CUDA(cudaMemcpyAsync(ubs, d_ub, bytes, cudaMemcpyDeviceToHost, stream));
     GDP_CUDA(cudaStreamSynchronize(stream));
@@ -349,13 +472,7 @@ GDP_RETCODE Context::propagate_host(double *lbs, double *ubs, gdp_stats *st) {
 
 GDP_RETCODE Context::propagate_device(double *d_lbs, double *d_ubs, cudaStream_t s, gdp_stats *st) {
     if (!s) s = stream;
-    const size_t bytes = sizeof(double) * (size_t)n;
-    P.lb = d_lbs; P.ub = d_ubs;
-    GDP_CUDA(cudaMemcpyAsync(d_lb_nxt, d_lbs, bytes, cudaMemcpyDeviceToDevice, s));
-    GDP_CUDA(cudaMemcpyAsync(d_ub_nxt, d_ubs, bytes, cudaMemcpyDeviceToDevice, s));
-    const GDP_RETCODE rc = run_rounds(s, st);
-    P.lb = d_lb; P.ub = d_ub;
-    return rc;
+    return run(d_lbs, d_ubs, d_lbs, d_ubs, s, st);
 }
 
 }  // namespace gdp

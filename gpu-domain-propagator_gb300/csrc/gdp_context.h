@@ -31,7 +31,6 @@ public:
                      const double *lhs, const double *rhs, const int *vartype, const gdp_options *o);
     GDP_RETCODE propagate_host(double *lbs, double *ubs, gdp_stats *st);
     GDP_RETCODE propagate_device(double *d_lbs, double *d_ubs, cudaStream_t s, gdp_stats *st);
-    GDP_RETCODE run_rounds(cudaStream_t s, gdp_stats *st);
 
     int m = 0, n = 0, nnz = 0;
     gdp_options opts{};
@@ -40,12 +39,21 @@ public:
     RoundFlags *h_flags = nullptr;  // pinned
     Arena arena;
     DevProblem P{};
-    double *d_lb = nullptr, *d_ub = nullptr, *d_lb_nxt = nullptr, *d_ub_nxt = nullptr;
-    RoundFlags *d_flags = nullptr;
-    unsigned *d_barrier = nullptr;
-    int n_sms = 0, finalize_blocks = 1, mega_grid = 1;
+    double *d_lb = nullptr, *d_ub = nullptr;  // staging for host bounds
+    int n_sms = 0, vec_blocks = 1, act_blocks = 1, cand_blocks = 1, mega_grid = 1;
     int n_srows = 0, n_slices = 0, n_lrows = 0, n_tiles = 0;
-    long long sell_elems = 0, rows_nonempty = 0, nnz_rows = 0;
+    long long sell_elems = 0;
+    // GPU_LOOP graph (built on first use, reused while the context lives)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+private:
+    GDP_RETCODE run(const double *lb_in, const double *ub_in, double *lb_out, double *ub_out,
+                    cudaStream_t s, gdp_stats *st);
+    GDP_RETCODE build_graph(cudaStream_t s);
+    GDP_RETCODE rounds_cpu_loop(cudaStream_t s, int *launches);
+    GDP_RETCODE rounds_gpu_loop(cudaStream_t s, int *launches);
+    GDP_RETCODE rounds_megakernel(cudaStream_t s, int *launches);
 };
 
 }  // namespace gdp

@@ -144,6 +144,149 @@ __device__ __forceinline__ void atomic_min_f64(double *addr, double v) {
     else atomicMax(reinterpret_cast<unsigned long long *>(addr), static_cast<unsigned long long>(b));
 }
 
+// ---- integer-domain forms (no FP64 pipe) ----------------------------------
+// Exact for every non-NaN double: a double's bit pattern orders like a signed
+// integer when the sign bit is 0, and in reverse as an unsigned integer when
+// it is 1.
+constexpr long long kBitsEps = 0x3E112E0BE826D695LL;          // 1e-9
+constexpr long long kBitsPosInf = 0x4415AF1D78B58C40LL;       // 1e20
+constexpr unsigned long long kBitsNegInf = 0xC415AF1D78B58C40ULL;  // -1e20
+
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+// x > 1e-9 (the reference's EPSGT(x, 0))
+__device__ __forceinline__ bool gt_eps_bits(long long b) { return b > kBitsEps; }
+// x > 0
+__device__ __forceinline__ bool gt0_bits(long long b) { return b > 0; }
+// x <= -1e20 (ISNEGINF)
+__device__ __forceinline__ bool neginf_bits(long long b) { return (unsigned long long)b >= kBitsNegInf; }
+// x >= 1e20 (ISPOSINF)
+__device__ __forceinline__ bool posinf_bits(long long b) { return b >= kBitsPosInf; }
+// key(x) < key(y) iff x < y for non-NaN doubles (NaN keys sort above +inf)
+__device__ __forceinline__ long long order_key(long long b) {
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+// EPSGT(x, y) with the FP64 subtraction only when x > y.
+__device__ __forceinline__ bool eps_gt_fast(double x, double y) {
+    return order_key(dbits(x)) > order_key(dbits(y)) && eps_gt(x, y);
+}
+
+// Outward rounding of a double to float by integer arithmetic.
+__device__ __forceinline__ float f32_mag(unsigned long long mag, bool up) {
+    const int e = (int)(mag >> 52);
+    if (e == 2047) return (mag & 0xFFFFFFFFFFFFFULL) ? __uint_as_float(0x7FC00000u) : __uint_as_float(0x7F800000u);
+    const int fe = e - 1023 + 127;
+    if (fe >= 255) return up ? __uint_as_float(0x7F800000u) : __uint_as_float(0x7F7FFFFFu);
+    if (fe <= 0) return (up && mag) ? __uint_as_float(0x00800000u) : 0.0f;
+    const unsigned long long man = mag & 0xFFFFFFFFFFFFFULL;
+    unsigned fb = ((unsigned)fe << 23) | (unsigned)(man >> 29);
+    if (up && (man & 0x1FFFFFFFULL)) fb += 1u;
+    return __uint_as_float(fb);
+}
+__device__ __forceinline__ float f32_up(long long b) {
+    const unsigned long long mag = (unsigned long long)b & 0x7FFFFFFFFFFFFFFFULL;
+    return b < 0 ? -f32_mag(mag, false) : f32_mag(mag, true);
+}
+__device__ __forceinline__ float f32_dn(long long b) {
+    const unsigned long long mag = (unsigned long long)b & 0x7FFFFFFFFFFFFFFFULL;
+    return b < 0 ? -f32_mag(mag, true) : f32_mag(mag, false);
+}
+// FP32 upper bound of |a| (ub - lb) up to two round-to-nearest float errors
+// (covered by the row test's 1 + 2^-20 margin).
+__device__ __forceinline__ float delta_up(long long ab, long long lbb, long long ubb) {
+    const float au = f32_mag((unsigned long long)ab & 0x7FFFFFFFFFFFFFFFULL, true);
+    const float d = __fsub_rn(f32_up(ubb), f32_dn(lbb));
+    return __fmul_rn(au, d);
+}
+constexpr float kUMargin = 1.00000095367431640625f;  // 1 + 2^-20
+
+// Sign-aware FP32 enclosure lo <= |a| (ub - lb) <= hi of one element, each end
+// widened by a relative 2^-20 (covers the round-to-nearest float operations).
+// NaN (e.g. inf - inf) makes every comparison inconclusive, which sends the
+// element to the exact FP64 path.
+struct DeltaBox {
+    float lo, hi;
+};
+__device__ __forceinline__ float widen_up(float x) { return __fadd_rn(x, fabsf(x) * 9.5367431640625e-7f); }
+__device__ __forceinline__ float widen_dn(float x) { return __fsub_rn(x, fabsf(x) * 9.5367431640625e-7f); }
+__device__ __forceinline__ DeltaBox delta_box(long long ab, long long lbb, long long ubb) {
+    const unsigned long long am = (unsigned long long)ab & 0x7FFFFFFFFFFFFFFFULL;
+    const float a_up = f32_mag(am, true), a_dn = f32_mag(am, false);
+    const float dh = __fsub_rn(f32_up(ubb), f32_dn(lbb));  // >= ub - lb (up to rounding)
+    const float dl = __fsub_rn(f32_dn(ubb), f32_up(lbb));  // <= ub - lb (up to rounding)
+    DeltaBox b;
+    b.hi = widen_up(__fmul_rn(dh >= 0.0f ? a_up : a_dn, dh));
+    b.lo = widen_dn(__fmul_rn(dl >= 0.0f ? a_dn : a_up, dl));
+    return b;
+}
+
+// Activity accumulator: the reference's computeActivities terms with integer
+// classification (no FP64 compares) and an FP32 enclosure [L, U] of the
+// maximum of |a| (ub - lb) (the reference's maxactdelta, before its EPS rule).
+struct Acc {
+    double minact, maxact;
+    int minf, maxf;
+    float U, L;
+};
+__device__ __forceinline__ void acc_init(Acc &s) {
+    s.minact = 0.0; s.maxact = 0.0; s.minf = 0; s.maxf = 0; s.U = 0.0f; s.L = 0.0f;
+}
+template <bool kLower>
+__device__ __forceinline__ void acc_add(Acc &s, double a, double lb, double ub) {
+    const long long ab = dbits(a), lbb = dbits(lb), ubb = dbits(ub);
+    const bool pos = gt_eps_bits(ab);
+    const bool lneg = neginf_bits(lbb), upos = posinf_bits(ubb);
+    const bool min_inf = pos ? lneg : upos;
+    const bool max_inf = pos ? upos : lneg;
+    s.minf += min_inf;
+    s.maxf += max_inf;
+    const bool gt0 = gt0_bits(ab);
+    if (!min_inf) s.minact = dadd(s.minact, dmul(a, gt0 ? lb : ub));
+    if (!max_inf) s.maxact = dadd(s.maxact, dmul(a, gt0 ? ub : lb));
+    s.U = fmaxf(s.U, delta_up(ab, lbb, ubb));
+    if (kLower) s.L = fmaxf(s.L, delta_box(ab, lbb, ubb).lo);
+}
+__device__ __forceinline__ void acc_combine(Acc &a, const Acc &b) {
+    a.minact = dadd(a.minact, b.minact);
+    a.maxact = dadd(a.maxact, b.maxact);
+    a.minf += b.minf;
+    a.maxf += b.maxf;
+    a.U = fmaxf(a.U, b.U);
+    a.L = fmaxf(a.L, b.L);
+}
+
+// Exact decision from the enclosure where possible. The reference's
+// sequential maxactdelta m satisfies M - 1e-9 <= m <= M for the true maximum
+// M >= 0 of |a|(ub-lb) (an element below the running value by at most 1e-9 is
+// skipped, so the running value never trails the maximum by more), and
+// L <= M <= U. Returns 0: skip, 1: process, 2: undecided (needs the exact
+// sequential pass). mn is min(rhs - minact, maxact - lhs).
+__device__ __forceinline__ int row_decision(int minf, int maxf, float U, float L, double mn) {
+    if (minf > 1 && maxf > 1) return 0;
+    if (mn < kInf && (double)__fmul_rn(U, kUMargin) <= mn) return 0;  // m <= M <= U <= mn
+    // m - mn >= L - 1e-9 - mn > 3e-9 - 1e-9: then fl(m - mn) > 1e-9 (see eps_gt_sure)
+    const double mn_hi = dadd(mn, 4e-9);
+    if ((double)widen_dn(L) > mn_hi) return 1;
+    return 2;
+}
+
+// min(rhs - minact, maxact - lhs) as std::min(s, t) in canConsBeTightened.
+__device__ __forceinline__ double row_min_slack(double minact, double maxact, double lhs, double rhs) {
+    const double s = dsub(rhs, minact), t = dsub(maxact, lhs);
+    return (t < s) ? t : s;
+}
+// The FP32 row filter: true if no variable of the row can be tightened
+// (U bounds the reference's maxactdelta from above).
+__device__ __forceinline__ bool u_filter_skips(int minf, int maxf, float U, double mn) {
+    if (minf > 1 && maxf > 1) return true;
+    return mn < kInf && (double)__fmul_rn(U, kUMargin) <= mn;
+}
+// The reference's decision from its sequential maxactdelta (canConsBeTightened).
+__device__ __forceinline__ bool reference_row_go(int minf, int maxf, double maxactdelta, double mn) {
+    if (minf > 1 && maxf > 1) return false;
+    if (maxactdelta < kInf) return !eps_le(maxactdelta, mn);
+    return true;
+}
+
 // The project's infeasibility rule (the reference detects none).
 __device__ __forceinline__ bool var_infeasible(double lb, double ub) {
     double s = fmax(fabs(lb), fabs(ub));

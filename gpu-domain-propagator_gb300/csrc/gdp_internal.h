@@ -1,38 +1,51 @@
 // gdp_internal.h -- device data layout shared by the host driver and kernels.
 //
 // HBM layout of one problem (built once per context, resident across rounds):
-//  * thread rows (1 <= len <= thread_row_max): sorted by length, longest first,
-//    grouped 32 to a slice; a slice stores its elements column-major
-//    (element k of lane l at slice_ptr[s] + 32*k + l), so a warp streams a
-//    slice with coalesced 128 B (col) / 256 B (val) loads while each lane sums
-//    its own row left to right -- the reference's summation order.
-//  * split rows (len > thread_row_max): CSR-contiguous, cut into tiles of
-//    split_tile non-zeros; one CTA reduces a tile, partials combine per row in
-//    tile order.
-//  * bounds: cur (read-only during a round) and nxt (receives the FP64
-//    min/max atomics); a bitmap records the variables changed in the round.
+//  * SELL-g slices (rows up to split_tile non-zeros): rows sorted by lanes per
+//    row g and length; a slice holds 32/g rows with g lanes each and stores
+//    its elements column-major (step i of lane l at slice_ptr[s] + 32*i + l),
+//    so a warp streams a slice with coalesced 128 B (col) / 256 B (val) loads.
+//    Rows up to thread_row_max have g = 1: one lane sums the row left to
+//    right -- the reference's summation order. Longer rows get g = 2..32 lanes
+//    (about 32 elements per lane) and a shuffle-tree combine.
+//  * split rows (len > split_tile): CSR-contiguous, cut into warp tiles of
+//    split_tile non-zeros; tile partials combine per row in tile order.
+//  * bounds: interleaved (lb, ub) pairs, current (read-only during a round) and
+//    next (receives the FP64 min/max atomics); a bitmap records the variables
+//    changed in the round.
+//  * marking: per row position the round in which it must be processed next,
+//    and the positions of every variable's rows (CSC of positions).
 #pragma once
 
 #include <cstdint>
+#include <cuda_runtime.h>
 
 namespace gdp {
 
-struct RowActsPOD {
-    double minact, maxact, maxactdelta;
-    int minact_inf, maxact_inf;
+// Partial activities of a split-row tile (and of a whole split row).
+struct TilePart {
+    double minact, maxact;
+    int minf, maxf;
+    float U;  // FP32 upper bound of max |a|(ub - lb)
+    int pad;
 };
 
-// Device-written round status. Read by the host (CPU_LOOP), by the graph's
-// conditional node (GPU_LOOP) and by every CTA of the megakernel.
+// Device-written round status. [0] is read by the host (CPU_LOOP), by the
+// graph's condition kernel (GPU_LOOP) and by every CTA of the megakernel;
+// [1], [2] are the megakernel's double-buffered per-round change flags.
 struct RoundFlags {
     int change;          // a candidate tightened some bound in the (last) round
     int infeasible;      // the infeasibility rule fired
     int infeasible_var;  // smallest violating variable index (INT_MAX if none)
     int rounds;          // rounds executed
-    int changed_vars;    // variables changed in the last round
     int error;           // device-side error code (0 = none)
     int done;            // loop finished (GPU_LOOP / MEGAKERNEL)
-    int pad;
+    int mark_cur;        // this round processes only marked rows (else every row)
+    unsigned tight;      // tightenings found in this round (decides the next round's mode)
+    unsigned long long changed_vars;  // committed variable changes, all rounds
+    unsigned long long rows_proc;     // rows processed, all rounds
+    unsigned long long nnz_proc;      // their non-zeros
+    unsigned long long pad2;
 };
 
 enum DeviceError : int {
@@ -41,10 +54,12 @@ enum DeviceError : int {
 };
 
 struct DevProblem {
-    int n;                 // variables
+    int n;  // variables
     // thread rows
     int n_srows, n_slices;
     const long long *slice_ptr;  // n_slices + 1
+    const int *slice_row0;       // n_slices + 1: first row position of each slice
+    const int *slice_lg;         // n_slices: log2 of the lanes per row (SELL-g)
     const int *sell_col;
     const double *sell_val;
     const int *srow_len;         // n_srows
@@ -54,35 +69,55 @@ struct DevProblem {
     const int *lcol;
     const double *lval;
     const double *lrow_lhs, *lrow_rhs;
-    const int *lrow_tile0;       // n_lrows + 1: tiles of long row r are [lrow_tile0[r], lrow_tile0[r+1])
-    const int *tile_row;         // n_tiles
-    const int *tile_begin;       // n_tiles + 1 (element offsets; tile t = [tile_begin[t], tile_end[t]))
+    const int *lrow_tile0;  // n_lrows + 1: tiles of split row r are [lrow_tile0[r], lrow_tile0[r+1])
+    const int *tile_row;    // n_tiles
+    const int *tile_begin;  // n_tiles (element offsets into lcol/lval)
     const int *tile_end;
-    RowActsPOD *tile_part;       // n_tiles
+    TilePart *tile_part;    // n_tiles
+    int n_mtiles;           // tiles of rows with more than one tile (candidate phase)
+    const int *mtiles;
+    // warp work items of the activity phase, heaviest first: s >= 0 is slice s,
+    // s < 0 is split tile -s-1
+    int n_items;
+    const int *items;
+    // marking (row positions: thread rows 0..n_srows-1, split rows n_srows + r).
+    // use_marking: 0 never, 1 adaptive (a round runs on marked rows only when
+    // the previous round found fewer than mark_threshold tightenings; pushing
+    // marks costs about one write per non-zero of every changed variable), 2
+    // always (tests).
+    int use_marking;
+    unsigned mark_threshold;
+    int *mark;             // round in which the position is processed next (0: none)
+    const int *var_ptr;    // n + 1
+    const int *var_pos;    // positions of each variable's rows
     // bounds
-    double *lb, *ub;             // current (read-only while a round runs)
-    double *lb_nxt, *ub_nxt;     // next (atomic min/max targets)
+    double2 *bnd;          // current (lb, ub); read-only while a round runs
+    double2 *bnd_nxt;      // next: FP64 min/max atomics
     const unsigned char *is_cont;
-    unsigned *chg;               // changed-variable bitmap, n_chg_words words
+    unsigned *chg;         // changed-variable bitmap, n_chg_words words
     int n_chg_words;
-    RoundFlags *flags;          // [0]: sticky state; [1], [2]: megakernel per-round change slots
-    unsigned *barrier;          // megakernel grid barrier {count, generation}
+    RoundFlags *flags;
+    unsigned *barrier;     // megakernel grid barrier {count, generation}
+    unsigned *queue;       // work counters: [parity * 2 + phase]
     int max_rounds;
 };
 
-// Launch helpers (gdp_round.cu). All return the cudaError_t of the launch.
-int launch_sell_round(const DevProblem &P, void *stream);
-int launch_split_partial(const DevProblem &P, void *stream);
-int launch_split_cand(const DevProblem &P, void *stream);
-int launch_finalize(const DevProblem &P, int finalize_blocks, void *stream);
-int launch_round_begin(const DevProblem &P, void *stream);
-int launch_check_bounds(const DevProblem &P, int blocks, void *stream);
-int launch_megakernel(const DevProblem &P, int grid, int block, void *stream);
-int megakernel_occupancy(int block, int *blocks_per_sm);
+constexpr int kWarpsPerCta = 8;
+constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
-constexpr int kSellWarpsPerCta = 8;
-constexpr int kSplitThreads = 256;
-constexpr int kFinalizeThreads = 256;
-constexpr int kMegaThreads = 256;
+// Launch helpers (gdp_round.cu). All return the cudaError_t of the launch.
+int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s);
+int launch_interleave(const DevProblem &P, const double *lb, const double *ub, int blocks, cudaStream_t s);
+int launch_deinterleave(const DevProblem &P, double *lb, double *ub, int blocks, cudaStream_t s);
+int launch_mark_all(const DevProblem &P, int blocks, cudaStream_t s);
+int launch_round_begin(const DevProblem &P, cudaStream_t s);
+int launch_activity_phase(const DevProblem &P, int blocks, cudaStream_t s);
+int launch_candidate_phase(const DevProblem &P, int blocks, cudaStream_t s);
+int launch_finalize(const DevProblem &P, int blocks, cudaStream_t s);
+int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_t s);
+int launch_megakernel(const DevProblem &P, int grid, cudaStream_t s);
+int phase_occupancy(int *act_blocks_per_sm, int *cand_blocks_per_sm, int *mega_blocks_per_sm);
+// gdp_layout.cu: variable -> row-position index for marking (scratch: n + 2 + (n+1)/1024 ints)
+int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s);
 
 }  // namespace gdp

@@ -1,0 +1,117 @@
+// gdp_layout.cu -- device-side construction of the marking index: for every
+// variable, the row positions (SELL slot or split-row slot) of the rows it
+// appears in. This is the transpose (CSR -> CSC pattern) that the reference
+// computes with cuSPARSE csr2csc on every call (src/kernels/util_kernels.cuh:92-229)
+// and uses to mark constraints (src/propagation_methods.cu:3-13).
+//
+// Three steps over the context's own layout: count the non-zeros of every
+// column (warp per slice / per split tile), exclusive scan of the counts,
+// scatter the positions. The order of positions inside a column is not
+// defined (it does not matter for marking).
+#include <cuda_runtime.h>
+
+#include "gdp_internal.h"
+
+namespace gdp {
+namespace {
+
+constexpr int kScanBlock = 1024;
+
+// For every element of the layout, calls f(col, position). Warp per slice
+// (lane = row) or per split tile; items are visited through the grid stride.
+template <class F>
+__device__ __forceinline__ void for_each_element(const DevProblem &P, F &&f) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int s = warp; s < P.n_slices; s += nwarps) {
+        const int lg = P.slice_lg[s], g = 1 << lg;
+        const int row0 = P.slice_row0[s], nrows = P.slice_row0[s + 1] - row0;
+        const int rl = lane >> lg, sub = lane & (g - 1);
+        const int len = rl < nrows ? P.srow_len[row0 + rl] : 0;
+        const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
+        const long long base = P.slice_ptr[s] + lane;
+        for (int i = 0; i < cnt; i++) f(P.sell_col[base + 32LL * i], row0 + rl);
+    }
+    for (int t = warp; t < P.n_tiles; t += nwarps) {
+        const int pos = P.n_srows + P.tile_row[t];
+        for (int k = P.tile_begin[t] + lane; k < P.tile_end[t]; k += 32) f(P.lcol[k], pos);
+    }
+}
+
+__global__ void k_count_cols(DevProblem P, int *cnt) {
+    for_each_element(P, [&](int j, int) { atomicAdd(cnt + j, 1); });
+}
+
+__global__ void k_fill_cols(DevProblem P, const int *col_ptr, int *fill, int *pos_out) {
+    for_each_element(P, [&](int j, int pos) { pos_out[col_ptr[j] + atomicAdd(fill + j, 1)] = pos; });
+}
+
+// Block-level exclusive scan (Hillis-Steele in shared memory; counts fit int).
+__global__ void k_scan_blocks(const int *in, int *out, int *block_sums, int n) {
+    __shared__ int s[kScanBlock];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = i < n ? in[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        const int t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = s[threadIdx.x] - v;
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
+}
+
+// Exclusive scan of the block sums by one block (sequential chunks).
+__global__ void k_scan_sums(int *sums, int nb) {
+    __shared__ int s[kScanBlock];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < nb; c0 += kScanBlock) {
+        const int i = c0 + threadIdx.x;
+        const int v = i < nb ? sums[i] : 0;
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < kScanBlock; off <<= 1) {
+            const int t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+            __syncthreads();
+            s[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < nb) sums[i] = carry + s[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == kScanBlock - 1) carry += s[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+__global__ void k_add_offsets(int *out, const int *block_sums, int n) {
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += block_sums[blockIdx.x];
+}
+
+}  // namespace
+
+// Builds var_ptr (n + 1) and var_pos (nnz) on the device. scratch: n + 1 +
+// ceil((n + 1) / 1024) ints. Returns the cudaError_t of the launches.
+int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s) {
+    const int n1 = P.n + 1;
+    const int nb = (n1 + kScanBlock - 1) / kScanBlock;
+    int *cnt = scratch;        // n + 1 counts, reused as fill cursors
+    int *sums = scratch + n1;  // nb block sums
+    cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n1, s);
+    if (e != cudaSuccess) return (int)e;
+    k_count_cols<<<blocks, 256, 0, s>>>(P, cnt);
+    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(cnt, var_ptr, sums, n1);
+    k_scan_sums<<<1, kScanBlock, 0, s>>>(sums, nb);
+    k_add_offsets<<<nb, kScanBlock, 0, s>>>(var_ptr, sums, n1);
+    e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n1, s);
+    if (e != cudaSuccess) return (int)e;
+    k_fill_cols<<<blocks, 256, 0, s>>>(P, var_ptr, cnt, var_pos);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace gdp

@@ -17,8 +17,8 @@
 // race on it and must be serialized by the caller.
 //
 // Rows are summed left to right by one thread each (the reference's order),
-// so results equal those of the context path for every row up to its
-// thread_row_max (1024 non-zeros); longer rows serialize on one thread here.
+// so results equal those of the context path for every row up to the
+// context's thread_row_max; longer rows serialize on one thread here.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -127,7 +127,7 @@ __global__ void k_noalloc_finalize(Csr A, NoallocView S, int words) {
             }
         }
     }
-    if (changed) atomicAdd(&S.flags->changed_vars, changed);
+    if (changed) atomicAdd(&S.flags->changed_vars, (unsigned long long)changed);
 }
 
 __global__ void k_noalloc_round_begin(NoallocView S) {

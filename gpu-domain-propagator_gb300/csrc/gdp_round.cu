@@ -1,16 +1,27 @@
-// gdp_round.cu -- one Jacobi propagation round on sm_103a, as standalone
-// kernels (CPU_LOOP / GPU_LOOP drivers) and as a persistent cooperative
-// megakernel that runs every round in one launch (MEGAKERNEL driver).
+// gdp_round.cu -- one Jacobi propagation round on sm_103a, as phase kernels
+// (CPU_LOOP and GPU_LOOP drivers) and as a persistent cooperative megakernel
+// that runs every round in one launch (MEGAKERNEL driver).
 //
 // A round reads the round-start bounds (cur), writes every tightening into nxt
 // with an FP64 min/max atomic and flags the variable in a bitmap; the finalize
-// phase copies the flagged variables nxt -> cur and applies the
-// infeasibility rule. The result is independent of scheduling: each row's sums
-// are computed in a fixed order from the snapshot and min/max commute.
+// phase copies flagged variables nxt -> cur, applies the infeasibility rule
+// and marks the rows of changed variables for the next round. The result does
+// not depend on scheduling: each row's sums run in a fixed order from the
+// snapshot and min/max commute.
+//
+// GB300's FP64 pipe (about 1.75 lane-ops per clock per SM) is the scarce
+// resource, so the kernels spend it only on the reference's arithmetic: 2 DMUL
+// + 2 DADD per non-zero for the activities. Classification against the
+// +-1e20 infinity thresholds is integer work on the bit patterns, the
+// reference's row test (canConsBeTightened) is pre-filtered with an FP32 upper
+// bound of max |a|(ub - lb) and decided exactly only for rows that survive,
+// and the candidate divisions of a warp are gathered into a queue and run 32
+// at a time instead of diverging.
+//
 // Reference: the round body of GPUAtomicDomainPropagation
 // (src/kernels/atomic_kernel.cuh:9-450) and of the megakernel
 // (src/kernels/atomic_megakernel.cuh:14-490), re-planned for a snapshot
-// (deterministic) schedule.
+// schedule; math from src/propagation_methods.cuh:78-276.
 #include <climits>
 #include <cuda_runtime.h>
 
@@ -22,199 +33,525 @@ namespace gdp {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kQueueCap = 128;  // >= 31 pending + 64 pushed per step
 
 __device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
     atomicOr(P.chg + (j >> 5), 1u << (j & 31));
 }
 
-__device__ __forceinline__ void to_acts(RowActs &a, const RowActsPOD &p) {
-    a.minact = p.minact; a.maxact = p.maxact; a.maxactdelta = p.maxactdelta;
-    a.minact_inf = p.minact_inf; a.maxact_inf = p.maxact_inf;
+// Bounds are written by the finalize phase of the same megakernel launch, so
+// they are read with coherent loads (never the read-only path).
+__device__ __forceinline__ double2 load_bnd(const DevProblem &P, int j) { return P.bnd[j]; }
+
+// Row constants of tightenVariable (src/propagation_methods.cuh:223-276), with
+// float thresholds that decide most per-element EPS tests without FP64:
+// d <= x if d_hi <= f32_dn(x); fl(d - x) > 1e-9 if d_lo > f32_up(fl(x + 4e-9))
+// (then d - x > 3e-9 for |x| < 2^24, and d > x with ulp(x) > 3.7e-9 above).
+struct RowC {
+    double slack, surplus;  // rhs - minact, lhs - maxact
+    double neg_surplus;     // maxact - lhs
+    int minf, maxf;
+    int ok;                 // bit 0: rhs side usable, bit 1: lhs side usable
+    float slack_dn, slack_hi, nsur_dn, nsur_hi;
+};
+
+__device__ __forceinline__ RowC make_rowc(double minact, double maxact, int minf, int maxf, double lhs,
+                                          double rhs) {
+    RowC c;
+    c.slack = dsub(rhs, minact);
+    c.surplus = dsub(lhs, maxact);
+    c.neg_surplus = dsub(maxact, lhs);
+    c.minf = minf;
+    c.maxf = maxf;
+    const bool rhs_ok = !posinf_bits(dbits(rhs)) && !neginf_bits(dbits(minact));
+    const bool lhs_ok = !neginf_bits(dbits(lhs)) && !posinf_bits(dbits(maxact));
+    c.ok = (rhs_ok ? 1 : 0) | (lhs_ok ? 2 : 0);
+    c.slack_dn = f32_dn(dbits(c.slack));
+    c.slack_hi = f32_up(dbits(dadd(c.slack, 4e-9)));
+    c.nsur_dn = f32_dn(dbits(c.neg_surplus));
+    c.nsur_hi = f32_up(dbits(dadd(c.neg_surplus, 4e-9)));
+    return c;
 }
 
-// Apply one element's candidates; returns true if it tightened something.
-__device__ __forceinline__ bool apply_candidates(const DevProblem &P, const RowCand &rc, int j,
-                                                 double coeff) {
-    const double lb = __ldg(P.lb + j), ub = __ldg(P.ub + j);
-    bool lt, ut;
-    double nl, nu;
-    tighten_variable(coeff, rc, __ldg(P.is_cont + j) != 0, lb, ub, lt, nl, ut, nu);
-    if (lt) atomic_max_f64(P.lb_nxt + j, nl);
-    if (ut) atomic_min_f64(P.ub_nxt + j, nu);
-    if (lt || ut) {
-        mark_changed(P, j);
-        return true;
+// 0: EPSGT(d, x) is false, 1: true, 2: undecided from the enclosure.
+__device__ __forceinline__ int side_test(const DeltaBox &b, float x_dn, float x_hi) {
+    if (b.hi <= x_dn) return 0;
+    if (b.lo > x_hi) return 1;
+    return 2;
+}
+
+// Which candidate sides of element (a, lb, ub) need a division. Bit 0: upper
+// bound (tightenVarUpperBound), bit 1: lower bound (tightenVarLowerBound).
+// The FP64 product |a|(ub-lb) -- equal bit for bit to the reference's
+// coeff*(ub-lb) / coeff*(lb-ub) -- is formed only when the enclosure leaves a
+// test undecided.
+__device__ __forceinline__ int candidate_sides(const RowC &c, double a, double lb, double ub) {
+    const long long ab = dbits(a), lbb = dbits(lb), ubb = dbits(ub);
+    const DeltaBox box = delta_box(ab, lbb, ubb);
+    int rs = (c.ok & 1) ? side_test(box, c.slack_dn, c.slack_hi) : 0;
+    int ls = (c.ok & 2) ? side_test(box, c.nsur_dn, c.nsur_hi) : 0;
+    if (rs == 2 || ls == 2) {
+        const double d = dmul(fabs(a), dsub(ub, lb));
+        if (rs == 2) rs = eps_gt_fast(d, c.slack) ? 1 : 0;
+        if (ls == 2) ls = eps_gt_fast(d, c.neg_surplus) ? 1 : 0;
+    }
+    const bool pos = gt0_bits(ab);
+    const bool u_side = pos ? rs : ls;
+    const bool l_side = pos ? ls : rs;
+    const int nu = pos ? c.minf : c.maxf;
+    const int nl = pos ? c.maxf : c.minf;
+    const bool u_ok = u_side && (nu == 0 || (nu == 1 && neginf_bits(lbb)));
+    const bool l_ok = l_side && (nl == 0 || (nl == 1 && posinf_bits(ubb)));
+    return (u_ok ? 1 : 0) | (l_ok ? 2 : 0);
+}
+
+// One candidate (side 0: upper, 1: lower) of variable j; applies it with an
+// FP64 atomic if EPS-better than the snapshot. Returns true if it tightened.
+__device__ __forceinline__ bool apply_side(const DevProblem &P, const RowC &c, int j, double a, int side) {
+    const double2 b = load_bnd(P, j);
+    const bool pos = gt0_bits(dbits(a));
+    const bool cont = __ldg(P.is_cont + j) != 0;
+    if (side == 0) {
+        const int ninf = pos ? c.minf : c.maxf;
+        double nb = ddiv(pos ? c.slack : c.surplus, a);
+        if (ninf == 0) nb = dadd(nb, b.x);
+        if (!cont) nb = eps_floor(nb);
+        if (eps_lt(nb, b.y)) {
+            atomic_min_f64(&P.bnd_nxt[j].y, nb);
+            mark_changed(P, j);
+            return true;
+        }
+    } else {
+        const int ninf = pos ? c.maxf : c.minf;
+        double nb = ddiv(pos ? c.surplus : c.slack, a);
+        if (ninf == 0) nb = dadd(nb, b.y);
+        if (!cont) nb = eps_ceil(nb);
+        if (eps_gt(nb, b.x)) {
+            atomic_max_f64(&P.bnd_nxt[j].x, nb);
+            mark_changed(P, j);
+            return true;
+        }
     }
     return false;
 }
 
-// ---- thread rows: one warp per slice, one lane per row ---------------------
-__device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int lane, int change_slot) {
-    const int r = slice * 32 + lane;
-    const bool valid = r < P.n_srows;
-    const int len = valid ? __ldg(P.srow_len + r) : 0;
-    const long long base = __ldg(P.slice_ptr + slice) + lane;
-    const int *__restrict__ col = P.sell_col + base;
-    const double *__restrict__ val = P.sell_val + base;
+// ---- warp division queue --------------------------------------------------
+// Items are 32-bit codes; the caller decodes them. push() appends each lane's
+// items (ballot + prefix), drain() runs full batches of 32.
+struct WarpQueue {
+    unsigned *q;
+    int cnt;  // warp-uniform
+};
 
-    RowActs a;
-    acts_init(a);
-#pragma unroll 4
-    for (int k = 0; k < len; k++) {
-        const int j = __ldg(col + 32 * (long long)k);
-        const double c = __ldg(val + 32 * (long long)k);
-        acts_add(a, c, __ldg(P.lb + j), __ldg(P.ub + j));
+template <class Run>
+__device__ __forceinline__ void queue_drain(WarpQueue &Q, int lane, bool all, Run &&run) {
+    while (Q.cnt >= 32 || (all && Q.cnt > 0)) {
+        const int take = Q.cnt < 32 ? Q.cnt : 32;
+        if (lane < take) run(Q.q[lane]);
+        __syncwarp();
+        const int rest = Q.cnt - take;
+        for (int i = lane; i < rest; i += 32) Q.q[i] = Q.q[take + i];
+        __syncwarp();
+        Q.cnt = rest;
     }
-    bool tight = false;
-    if (valid) {
-        const double lhs = __ldg(P.srow_lhs + r), rhs = __ldg(P.srow_rhs + r);
-        if (can_cons_be_tightened(a, lhs, rhs)) {
-            const RowCand rc = row_cand(a, lhs, rhs);
-            for (int k = 0; k < len; k++)
-                tight |= apply_candidates(P, rc, __ldg(col + 32 * (long long)k), __ldg(val + 32 * (long long)k));
-        }
-    }
-    if (__any_sync(kFull, tight) && lane == 0) P.flags[change_slot].change = 1;
 }
 
-// ---- split rows: one CTA per tile -----------------------------------------
-__device__ __forceinline__ void combine(RowActs &a, const RowActs &b) {
-    a.minact = dadd(a.minact, b.minact);
-    a.maxact = dadd(a.maxact, b.maxact);
-    a.maxactdelta = fmax(a.maxactdelta, b.maxactdelta);
-    a.minact_inf += b.minact_inf;
-    a.maxact_inf += b.maxact_inf;
+__device__ __forceinline__ void queue_push(WarpQueue &Q, int lane, int sides, unsigned code_base) {
+    const unsigned bu = __ballot_sync(kFull, sides & 1);
+    const unsigned bl = __ballot_sync(kFull, sides & 2);
+    const unsigned lt = (1u << lane) - 1u;
+    if (sides & 1) Q.q[Q.cnt + __popc(bu & lt)] = code_base | 0u;
+    if (sides & 2) Q.q[Q.cnt + __popc(bu) + __popc(bl & lt)] = code_base | 1u;
+    __syncwarp();
+    Q.cnt += __popc(bu) + __popc(bl);
 }
 
-__device__ __forceinline__ RowActs shfl_down(const RowActs &a, int off) {
-    RowActs b;
-    b.minact = __shfl_down_sync(kFull, a.minact, off);
-    b.maxact = __shfl_down_sync(kFull, a.maxact, off);
-    b.maxactdelta = __shfl_down_sync(kFull, a.maxactdelta, off);
-    b.minact_inf = __shfl_down_sync(kFull, a.minact_inf, off);
-    b.maxact_inf = __shfl_down_sync(kFull, a.maxact_inf, off);
-    return b;
-}
-
-// Partial activities of tile t. Thread i sums elements i, i+256, ... in order;
-// the warp tree and the warp-order combine are fixed, so the partial is
-// deterministic. Split rows keep the exact max of |a|(ub-lb) (a sequential
-// EPS-max is not defined for a tree).
-__device__ void split_partial(const DevProblem &P, int t, RowActsPOD *smem) {
-    const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
-    RowActs a;
-    acts_init(a);
-    for (int k = b + (int)threadIdx.x; k < e; k += kSplitThreads) {
-        const int j = __ldg(P.lcol + k);
-        const double c = __ldg(P.lval + k);
-        const double lb = __ldg(P.lb + j), ub = __ldg(P.ub + j);
-        const double delta = dmul(fabs(c), dsub(ub, lb));
-        a.maxactdelta = fmax(a.maxactdelta, delta);
-        const bool pos = c > kEps;
-        const bool min_inf = pos ? is_neginf(lb) : is_posinf(ub);
-        const bool max_inf = pos ? is_posinf(ub) : is_neginf(lb);
-        a.minact_inf += min_inf;
-        a.maxact_inf += max_inf;
-        const bool gt0 = c > 0.0;
-        if (!min_inf) a.minact = dadd(a.minact, dmul(c, gt0 ? lb : ub));
-        if (!max_inf) a.maxact = dadd(a.maxact, dmul(c, gt0 ? ub : lb));
-    }
+// Warp-aggregated round bookkeeping: change flag and tightening count.
+__device__ __forceinline__ void report_tight(int tight, int lane, int *change, unsigned *tight_ctr) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) combine(a, shfl_down(a, off));
-    const int warp = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        smem[warp].minact = a.minact; smem[warp].maxact = a.maxact;
-        smem[warp].maxactdelta = a.maxactdelta;
-        smem[warp].minact_inf = a.minact_inf; smem[warp].maxact_inf = a.maxact_inf;
+    for (int off = 16; off > 0; off >>= 1) tight += __shfl_down_sync(kFull, tight, off);
+    if (lane == 0 && tight) {
+        *change = 1;
+        atomicAdd(tight_ctr, (unsigned)tight);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        RowActs s;
-        to_acts(s, smem[0]);
-        for (int w = 1; w < kSplitThreads / 32; w++) {
-            RowActs o;
-            to_acts(o, smem[w]);
-            combine(s, o);
+}
+
+// ---- SELL-g rows: one warp per slice, g lanes per row ----------------------
+struct WarpSmem {
+    RowC rc[32];
+    unsigned q[kQueueCap];
+};
+
+// Combines the partial accumulators of a group of g lanes (g a power of two,
+// warp-uniform) into its first lane: shuffle tree with offsets g/2, ..., 1.
+__device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
+    for (int off = g >> 1; off > 0; off >>= 1) {
+        Acc o;
+        o.minact = __shfl_down_sync(kFull, s.minact, off);
+        o.maxact = __shfl_down_sync(kFull, s.maxact, off);
+        o.minf = __shfl_down_sync(kFull, s.minf, off);
+        o.maxf = __shfl_down_sync(kFull, s.maxf, off);
+        o.U = __shfl_down_sync(kFull, s.U, off);
+        o.L = __shfl_down_sync(kFull, s.L, off);
+        acc_combine(s, o);
+    }
+}
+
+// One SELL-g slice per warp: 32/g rows, g lanes per row. Lane l serves row
+// l >> lg and its elements sub, sub+g, ... (sub = l & (g-1)), stored
+// column-major (step i of lane l at slice_ptr[slice] + 32 i + l). g == 1 rows
+// are summed left to right and take the reference's exact row decision;
+// g > 1 rows are combined by a shuffle tree and use the FP32 bound rule.
+__device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int lane, int round, bool marked,
+                                           int *change, unsigned *tight_ctr, WarpSmem &ws) {
+    const int lg = __ldg(P.slice_lg + slice);
+    const int g = 1 << lg;
+    const int row0 = __ldg(P.slice_row0 + slice);
+    const int nrows = __ldg(P.slice_row0 + slice + 1) - row0;
+    const int rl = lane >> lg, sub = lane & (g - 1);
+    const int r = row0 + rl;
+    bool act = rl < nrows;
+    if (act && marked) act = P.mark[r] == round;
+    if (!__any_sync(kFull, act)) return;
+    const int len = act ? __ldg(P.srow_len + r) : 0;
+    const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;  // my elements
+    const long long base = __ldg(P.slice_ptr + slice) + lane;
+    const int *col = P.sell_col + base;
+    const double *val = P.sell_val + base;
+    const bool leader = act && sub == 0;
+
+    // pass 1: activities + FP32 enclosure, each lane in order, then the group tree
+    Acc s;
+    acc_init(s);
+#pragma unroll 4
+    for (int i = 0; i < cnt; i++) {
+        const int j = __ldcs(col + 32 * i);
+        const double a = __ldcs(val + 32 * i);
+        const double2 b = load_bnd(P, j);
+        acc_add<true>(s, a, b.x, b.y);
+    }
+    if (g > 1) acc_group_reduce(s, g);
+    {
+        int lsum = leader ? len : 0, rows = leader ? 1 : 0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            lsum += __shfl_down_sync(kFull, lsum, off);
+            rows += __shfl_down_sync(kFull, rows, off);
         }
-        RowActsPOD out;
-        out.minact = s.minact; out.maxact = s.maxact; out.maxactdelta = s.maxactdelta;
-        out.minact_inf = s.minact_inf; out.maxact_inf = s.maxact_inf;
-        P.tile_part[t] = out;
+        if (lane == 0) {
+            atomicAdd(&P.flags[0].rows_proc, (unsigned long long)rows);
+            atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)lsum);
+        }
     }
-    __syncthreads();
+    double lhs = 0.0, rhs = 0.0, mn = 0.0;
+    int dec = 0;
+    if (leader) {
+        lhs = __ldg(P.srow_lhs + r);
+        rhs = __ldg(P.srow_rhs + r);
+        mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
+        if (g == 1) dec = row_decision(s.minf, s.maxf, s.U, s.L, mn);
+        else dec = u_filter_skips(s.minf, s.maxf, s.U, mn) ? 0 : 1;
+    }
+    // pass 2 (g == 1 only): the reference's sequential EPS-max, where the
+    // enclosure leaves the row test undecided
+    if (__any_sync(kFull, dec == 2)) {
+        double m = 0.0;
+        const int len2 = dec == 2 ? len : 0;
+        for (int k = 0; k < len2; k++) {
+            const int j = __ldg(col + 32 * k);
+            const double a = __ldg(val + 32 * k);
+            const double2 b = load_bnd(P, j);
+            const double d = dmul(fabs(a), dsub(b.y, b.x));
+            if (eps_gt_fast(d, m)) m = d;
+        }
+        if (dec == 2) dec = reference_row_go(s.minf, s.maxf, m, mn) ? 1 : 0;
+    }
+    // pass 3: candidates through the warp division queue
+    int tight = 0;
+    const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && act;
+    if (__any_sync(kFull, go)) {
+        if (leader && dec == 1) ws.rc[rl] = make_rowc(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs);
+        __syncwarp();
+        WarpQueue Q{ws.q, 0};
+        const long long sbase = base - lane;
+        auto run = [&](unsigned code) {
+            const int owner = (code >> 1) & 31;
+            const int i = (int)(code >> 6);
+            const long long e = sbase + 32LL * i + owner;
+            const int j = __ldg(P.sell_col + e);
+            const double a = __ldg(P.sell_val + e);
+            tight += apply_side(P, ws.rc[owner >> lg], j, a, (int)(code & 1u)) ? 1 : 0;
+        };
+        int maxcnt = go ? cnt : 0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) maxcnt = max(maxcnt, __shfl_xor_sync(kFull, maxcnt, off));
+        for (int i = 0; i < maxcnt; i++) {
+            int sides = 0;
+            if (go && i < cnt) {
+                const int j = __ldg(col + 32 * i);
+                const double a = __ldg(val + 32 * i);
+                const double2 b = load_bnd(P, j);
+                sides = candidate_sides(ws.rc[rl], a, b.x, b.y);
+            }
+            queue_push(Q, lane, sides, ((unsigned)i << 6) | ((unsigned)lane << 1));
+            queue_drain(Q, lane, false, run);
+        }
+        queue_drain(Q, lane, true, run);
+    }
+    report_tight(tight, lane, change, tight_ctr);
 }
 
-// Candidates of tile t from its row's combined activities (tiles combined in
-// tile order by every thread: identical values, no extra barrier).
-__device__ void split_cand(const DevProblem &P, int t, int change_slot) {
-    const int r = __ldg(P.tile_row + t);
-    const int t0 = __ldg(P.lrow_tile0 + r), t1 = __ldg(P.lrow_tile0 + r + 1);
-    RowActs a;
-    to_acts(a, P.tile_part[t0]);
-    for (int u = t0 + 1; u < t1; u++) {
-        RowActs o;
-        to_acts(o, P.tile_part[u]);
-        combine(a, o);
+// ---- split rows: one warp per tile ----------------------------------------
+__device__ __forceinline__ void acc_shfl_reduce(Acc &s) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Acc o;
+        o.minact = __shfl_down_sync(kFull, s.minact, off);
+        o.maxact = __shfl_down_sync(kFull, s.maxact, off);
+        o.minf = __shfl_down_sync(kFull, s.minf, off);
+        o.maxf = __shfl_down_sync(kFull, s.maxf, off);
+        o.U = __shfl_down_sync(kFull, s.U, off);
+        acc_combine(s, o);
     }
-    const double lhs = __ldg(P.lrow_lhs + r), rhs = __ldg(P.lrow_rhs + r);
-    if (!can_cons_be_tightened(a, lhs, rhs)) return;
-    const RowCand rc = row_cand(a, lhs, rhs);
+}
+
+// Decision (the FP32 bound rule) and candidates of split row `row` over the
+// element range [b, e) of one tile, from the row's complete activities held by
+// lane 0; the warp queues the divisions.
+__device__ __forceinline__ void split_row_candidates(const DevProblem &P, int row, int b, int e, const Acc &s0,
+                                                     int lane, int *change, unsigned *tight_ctr, unsigned *qbuf) {
+    RowC c;
+    int go = 0;
+    if (lane == 0) {
+        const double lhs = __ldg(P.lrow_lhs + row), rhs = __ldg(P.lrow_rhs + row);
+        const double mn = row_min_slack(s0.minact, s0.maxact, lhs, rhs);
+        go = !u_filter_skips(s0.minf, s0.maxf, s0.U, mn);
+        c = make_rowc(s0.minact, s0.maxact, s0.minf, s0.maxf, lhs, rhs);
+    }
+    go = __shfl_sync(kFull, go, 0);
+    if (!go) return;
+    c.slack = __shfl_sync(kFull, c.slack, 0);
+    c.surplus = __shfl_sync(kFull, c.surplus, 0);
+    c.neg_surplus = __shfl_sync(kFull, c.neg_surplus, 0);
+    c.minf = __shfl_sync(kFull, c.minf, 0);
+    c.maxf = __shfl_sync(kFull, c.maxf, 0);
+    c.ok = __shfl_sync(kFull, c.ok, 0);
+    c.slack_dn = __shfl_sync(kFull, c.slack_dn, 0);
+    c.slack_hi = __shfl_sync(kFull, c.slack_hi, 0);
+    c.nsur_dn = __shfl_sync(kFull, c.nsur_dn, 0);
+    c.nsur_hi = __shfl_sync(kFull, c.nsur_hi, 0);
+    int tight = 0;
+    WarpQueue Q{qbuf, 0};
+    auto run = [&](unsigned code) {
+        const int k = b + (int)(code >> 1);
+        tight += apply_side(P, c, __ldg(P.lcol + k), __ldg(P.lval + k), (int)(code & 1u)) ? 1 : 0;
+    };
+    for (int k0 = b; k0 < e; k0 += 32) {
+        const int k = k0 + lane;
+        int sides = 0;
+        if (k < e) {
+            const int j = __ldg(P.lcol + k);
+            const double a = __ldg(P.lval + k);
+            const double2 bb = load_bnd(P, j);
+            sides = candidate_sides(c, a, bb.x, bb.y);
+        }
+        queue_push(Q, lane, sides, (unsigned)(k - b) << 1);
+        queue_drain(Q, lane, false, run);
+    }
+    queue_drain(Q, lane, true, run);
+    report_tight(tight, lane, change, tight_ctr);
+}
+
+// Activities of split-row tile t (lane l sums elements l, l+32, ... in order,
+// shuffle tree across lanes). A row that fits in one tile is finished here
+// (decision and candidates); tiles of longer rows store a partial for the
+// candidate phase.
+__device__ __forceinline__ void split_partial(const DevProblem &P, int t, int lane, int round, bool marked,
+                                              int *change, unsigned *tight_ctr, unsigned *qbuf) {
+    const int row = __ldg(P.tile_row + t);
+    if (marked && P.mark[P.n_srows + row] != round) return;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
-    bool tight = false;
-    for (int k = b + (int)threadIdx.x; k < e; k += blockDim.x)
-        tight |= apply_candidates(P, rc, __ldg(P.lcol + k), __ldg(P.lval + k));
-    if (__any_sync(kFull, tight) && (threadIdx.x & 31) == 0) P.flags[change_slot].change = 1;
+    Acc s;
+    acc_init(s);
+#pragma unroll 4
+    for (int k = b + lane; k < e; k += 32) {
+        const int j = __ldg(P.lcol + k);
+        const double a = __ldg(P.lval + k);
+        const double2 bb = load_bnd(P, j);
+        acc_add<false>(s, a, bb.x, bb.y);
+    }
+    acc_shfl_reduce(s);
+    const int t0 = __ldg(P.lrow_tile0 + row);
+    const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
+    if (lane == 0) {
+        atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)(e - b));
+        if (t == t0) atomicAdd(&P.flags[0].rows_proc, 1ULL);
+        if (!single) {
+            TilePart tp;
+            tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf; tp.U = s.U; tp.pad = 0;
+            P.tile_part[t] = tp;
+        }
+    }
+    if (single) split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, qbuf);
 }
 
-// Copy changed variables nxt -> cur, apply the infeasibility rule, clear the
-// bitmap. Grid-stride over bitmap words.
-__device__ void finalize_words(const DevProblem &P, int tid, int nthreads) {
-    int changed = 0;
+// Candidate phase for tile t of a multi-tile row: lane 0 combines the row's
+// tile partials in tile order.
+__device__ __forceinline__ void split_cand(const DevProblem &P, int t, int lane, int round, bool marked,
+                                           int *change, unsigned *tight_ctr, unsigned *qbuf) {
+    const int row = __ldg(P.tile_row + t);
+    if (marked && P.mark[P.n_srows + row] != round) return;
+    Acc s;
+    acc_init(s);
+    if (lane == 0) {
+        const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
+        {
+            const TilePart p = P.tile_part[t0];
+            s.minact = p.minact; s.maxact = p.maxact; s.minf = p.minf; s.maxf = p.maxf; s.U = p.U;
+        }
+        for (int u = t0 + 1; u < t1; u++) {
+            const TilePart p = P.tile_part[u];
+            Acc o;
+            o.minact = p.minact; o.maxact = p.maxact; o.minf = p.minf; o.maxf = p.maxf; o.U = p.U;
+            acc_combine(s, o);
+        }
+    }
+    split_row_candidates(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, qbuf);
+}
+
+// Commit changed variables nxt -> cur, apply the infeasibility rule, mark the
+// rows of changed variables for the next round, clear the bitmap.
+__device__ __forceinline__ void finalize_words(const DevProblem &P, int round, bool push_marks, int tid,
+                                               int nthreads) {
+    unsigned long long changed = 0;
     for (int w = tid; w < P.n_chg_words; w += nthreads) {
         unsigned bits = P.chg[w];
         if (!bits) continue;
         P.chg[w] = 0u;
         changed += __popc(bits);
         while (bits) {
-            const int bit = __ffs(bits) - 1;
+            const int j = w * 32 + __ffs(bits) - 1;
             bits &= bits - 1;
-            const int j = w * 32 + bit;
-            const double l = P.lb_nxt[j], u = P.ub_nxt[j];
-            P.lb[j] = l;
-            P.ub[j] = u;
-            if (var_infeasible(l, u)) {
+            const double2 b = P.bnd_nxt[j];
+            P.bnd[j] = b;
+            if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);
             }
+            if (push_marks)
+                for (int p = __ldg(P.var_ptr + j); p < __ldg(P.var_ptr + j + 1); p++)
+                    P.mark[__ldg(P.var_pos + p)] = round + 1;
         }
     }
     if (changed) atomicAdd(&P.flags[0].changed_vars, changed);
 }
 
-// ---- standalone kernels ---------------------------------------------------
-__global__ void __launch_bounds__(32 * kSellWarpsPerCta) k_sell_round(DevProblem P) {
-    const int slice = blockIdx.x * kSellWarpsPerCta + (threadIdx.x >> 5);
-    if (slice >= P.n_slices) return;
-    sell_slice(P, slice, threadIdx.x & 31, 0);
+// ---- work distribution ----------------------------------------------------
+// Warp-level dynamic queue over items sorted heaviest first.
+__device__ __forceinline__ int warp_next(unsigned *ctr, int lane) {
+    unsigned v = 0;
+    if (lane == 0) v = atomicAdd(ctr, 1u);
+    return (int)__shfl_sync(kFull, v, 0);
 }
 
-__global__ void __launch_bounds__(kSplitThreads) k_split_partial(DevProblem P) {
-    __shared__ RowActsPOD smem[kSplitThreads / 32];
-    split_partial(P, blockIdx.x, smem);
+__device__ __forceinline__ void activity_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
+                                               int *change, unsigned *tight_ctr, WarpSmem &ws, int lane) {
+    for (;;) {
+        const int i = warp_next(ctr, lane);
+        if (i >= P.n_items) break;
+        const int it = __ldg(P.items + i);
+        if (it >= 0) sell_slice(P, it, lane, round, marked, change, tight_ctr, ws);
+        else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws.q);
+    }
 }
 
-__global__ void __launch_bounds__(kSplitThreads) k_split_cand(DevProblem P) {
-    split_cand(P, blockIdx.x, 0);
+__device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
+                                                int *change, unsigned *tight_ctr, WarpSmem &ws, int lane) {
+    for (;;) {
+        const int i = warp_next(ctr, lane);
+        if (i >= P.n_mtiles) break;
+        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, change, tight_ctr, ws.q);
+    }
 }
 
-__global__ void __launch_bounds__(kFinalizeThreads) k_finalize(DevProblem P) {
-    finalize_words(P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+// Whether the round after one with `tight` tightenings runs on marked rows.
+__device__ __forceinline__ bool next_round_marked(const DevProblem &P, unsigned tight) {
+    return P.use_marking == 2 || (P.use_marking == 1 && tight < P.mark_threshold);
 }
 
-// Zero the round's change flag and count the round.
+// ---- phase kernels (CPU_LOOP / GPU_LOOP) -----------------------------------
+__global__ void __launch_bounds__(kCtaThreads, 4) k_activity(DevProblem P) {
+    __shared__ WarpSmem ws[kWarpsPerCta];
+    const int round = P.flags[0].rounds;
+    if (P.flags[0].infeasible) return;
+    activity_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 0, &P.flags[0].change, &P.flags[0].tight,
+                   ws[threadIdx.x >> 5], threadIdx.x & 31);
+}
+
+__global__ void __launch_bounds__(kCtaThreads, 4) k_candidates(DevProblem P) {
+    __shared__ WarpSmem ws[kWarpsPerCta];
+    const int round = P.flags[0].rounds;
+    if (P.flags[0].infeasible) return;
+    candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].change, &P.flags[0].tight,
+                    ws[threadIdx.x >> 5], threadIdx.x & 31);
+}
+
+// Every thread derives the same next-round mode from the final tightening count.
+__global__ void __launch_bounds__(256) k_finalize(DevProblem P) {
+    const bool push = next_round_marked(P, P.flags[0].tight);
+    finalize_words(P, P.flags[0].rounds, push, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// Starts a round: counts it, takes the mode the previous finalize chose,
+// clears the change flag, tightening count and work counters (unless the
+// propagation is already infeasible).
 __global__ void k_round_begin(DevProblem P) {
+    if (P.flags[0].infeasible) return;
+    const int r = P.flags[0].rounds;
+    P.flags[0].mark_cur = r > 0 && next_round_marked(P, P.flags[0].tight);
     P.flags[0].change = 0;
-    P.flags[0].rounds += 1;
+    P.flags[0].tight = 0u;
+    P.flags[0].rounds = r + 1;
+    P.queue[0] = 0u;
+    P.queue[1] = 0u;
+}
+
+// GPU_LOOP: decides whether the graph's WHILE node runs another round.
+__global__ void k_condition(DevProblem P, cudaGraphConditionalHandle h) {
+    const RoundFlags &f = P.flags[0];
+    const bool more = f.change && !f.infeasible && f.rounds < P.max_rounds;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(256) k_check_bounds(DevProblem P) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < P.n; j += gridDim.x * blockDim.x) {
+        const double2 b = P.bnd[j];
+        if (var_infeasible(b.x, b.y)) {
+            P.flags[0].infeasible = 1;
+            atomicMin(&P.flags[0].infeasible_var, j);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_interleave(DevProblem P, const double *lb, const double *ub) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < P.n; j += gridDim.x * blockDim.x) {
+        const double2 b = make_double2(lb[j], ub[j]);
+        P.bnd[j] = b;
+        P.bnd_nxt[j] = b;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_deinterleave(DevProblem P, double *lb, double *ub) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < P.n; j += gridDim.x * blockDim.x) {
+        const double2 b = P.bnd[j];
+        lb[j] = b.x;
+        ub[j] = b.y;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_mark_all(DevProblem P) {
+    const int npos = P.n_srows + P.n_lrows;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npos; p += gridDim.x * blockDim.x) P.mark[p] = 0;
 }
 
 // ---- megakernel -----------------------------------------------------------
@@ -254,40 +591,39 @@ __device__ bool grid_barrier(unsigned *bar, int *error) {
     return __syncthreads_and(ok) != 0;
 }
 
-// Round loop on the device. flags[0] holds the sticky state (rounds,
-// infeasibility, error, last change); flags[1 + (round & 1)].change is the
-// per-round change flag, double-buffered so that no CTA can clear a flag
-// another CTA has not read yet (the slot of round r+1 is cleared after round
-// r's first barrier, which every CTA passes only after reading round r-1's).
-__global__ void __launch_bounds__(kMegaThreads) k_megakernel(DevProblem P) {
-    __shared__ RowActsPOD smem[kMegaThreads / 32];
-    const int n_groups = (P.n_slices + kSellWarpsPerCta - 1) / kSellWarpsPerCta;
-    const int n_items = P.n_tiles + n_groups;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// Round loop on the device. flags[0] holds the sticky state; flags[1 + (round
+// & 1)].change is the per-round change flag and queue[2 * (round & 1) + phase]
+// the per-round work counters, double-buffered so that nothing a CTA may
+// still read is cleared: the next round's slots are cleared after the current
+// round's first barrier, which every CTA passes only after finishing the
+// previous round.
+__global__ void __launch_bounds__(kCtaThreads, 4) k_megakernel(DevProblem P) {
+    __shared__ WarpSmem ws[kWarpsPerCta];
+    const int lane = threadIdx.x & 31;
+    WarpSmem &mine = ws[threadIdx.x >> 5];
     int *err = &P.flags[0].error;
     int last_change = 0;
+    bool marked = false;  // round 1 processes every row
     if (*((volatile int *)&P.flags[0].infeasible) == 0) {
         for (int round = 1; round <= P.max_rounds; round++) {
-            const int slot = 1 + (round & 1);
-            // phase A: split-row partials, then thread-row slices
-            for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
-                if (item < P.n_tiles) {
-                    split_partial(P, item, smem);
-                } else {
-                    const int slice = (item - P.n_tiles) * kSellWarpsPerCta + warp;
-                    if (slice < P.n_slices) sell_slice(P, slice, lane, slot);
-                }
+            const int par = round & 1;
+            int *change = &P.flags[1 + par].change;
+            unsigned *tight = &P.flags[1 + par].tight;
+            activity_phase(P, round, marked, P.queue + 2 * par, change, tight, mine, lane);
+            if (!grid_barrier(P.barrier, err)) return;
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                P.flags[1 + (par ^ 1)].change = 0;
+                P.flags[1 + (par ^ 1)].tight = 0u;
+                P.queue[2 * (par ^ 1)] = 0u;
+                P.queue[2 * (par ^ 1) + 1] = 0u;
             }
+            candidate_phase(P, round, marked, P.queue + 2 * par + 1, change, tight, mine, lane);
             if (!grid_barrier(P.barrier, err)) return;
-            if (blockIdx.x == 0 && threadIdx.x == 0) P.flags[1 + ((round + 1) & 1)].change = 0;
-            // phase B: split-row candidates
-            for (int t = blockIdx.x; t < P.n_tiles; t += gridDim.x) split_cand(P, t, slot);
-            if (!grid_barrier(P.barrier, err)) return;
-            // phase C: commit changed variables, infeasibility rule
-            finalize_words(P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+            marked = next_round_marked(P, *((volatile unsigned *)tight));
+            finalize_words(P, round, marked, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
             if (blockIdx.x == 0 && threadIdx.x == 0) P.flags[0].rounds = round;
             if (!grid_barrier(P.barrier, err)) return;
-            last_change = *((volatile int *)&P.flags[slot].change);
+            last_change = *((volatile int *)change);
             const int infeasible = *((volatile int *)&P.flags[0].infeasible);
             if (!last_change || infeasible) break;
         }
@@ -298,64 +634,71 @@ __global__ void __launch_bounds__(kMegaThreads) k_megakernel(DevProblem P) {
     }
 }
 
-// Initial infeasibility check over every variable (before round 1).
-__global__ void __launch_bounds__(kFinalizeThreads) k_check_bounds(DevProblem P) {
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < P.n; j += gridDim.x * blockDim.x) {
-        if (var_infeasible(P.lb[j], P.ub[j])) {
-            P.flags[0].infeasible = 1;
-            atomicMin(&P.flags[0].infeasible_var, j);
-        }
-    }
-}
-
 }  // namespace
 
 // ---- launchers ------------------------------------------------------------
-int launch_round_begin(const DevProblem &P, void *stream) {
-    k_round_begin<<<1, 1, 0, (cudaStream_t)stream>>>(P);
-    return (int)cudaGetLastError();
-}
-
-int launch_check_bounds(const DevProblem &P, int blocks, void *stream) {
+int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s) {
     if (P.n == 0) return 0;
-    k_check_bounds<<<blocks, kFinalizeThreads, 0, (cudaStream_t)stream>>>(P);
+    k_check_bounds<<<blocks, 256, 0, s>>>(P);
     return (int)cudaGetLastError();
 }
 
-int launch_sell_round(const DevProblem &P, void *stream) {
-    if (P.n_slices == 0) return 0;
-    const int grid = (P.n_slices + kSellWarpsPerCta - 1) / kSellWarpsPerCta;
-    k_sell_round<<<grid, 32 * kSellWarpsPerCta, 0, (cudaStream_t)stream>>>(P);
+int launch_interleave(const DevProblem &P, const double *lb, const double *ub, int blocks, cudaStream_t s) {
+    k_interleave<<<blocks, 256, 0, s>>>(P, lb, ub);
     return (int)cudaGetLastError();
 }
 
-int launch_split_partial(const DevProblem &P, void *stream) {
-    if (P.n_tiles == 0) return 0;
-    k_split_partial<<<P.n_tiles, kSplitThreads, 0, (cudaStream_t)stream>>>(P);
+int launch_deinterleave(const DevProblem &P, double *lb, double *ub, int blocks, cudaStream_t s) {
+    k_deinterleave<<<blocks, 256, 0, s>>>(P, lb, ub);
     return (int)cudaGetLastError();
 }
 
-int launch_split_cand(const DevProblem &P, void *stream) {
-    if (P.n_tiles == 0) return 0;
-    k_split_cand<<<P.n_tiles, kSplitThreads, 0, (cudaStream_t)stream>>>(P);
+int launch_mark_all(const DevProblem &P, int blocks, cudaStream_t s) {
+    if (!P.use_marking || P.n_srows + P.n_lrows == 0) return 0;
+    k_mark_all<<<blocks, 256, 0, s>>>(P);
     return (int)cudaGetLastError();
 }
 
-int launch_finalize(const DevProblem &P, int finalize_blocks, void *stream) {
+int launch_round_begin(const DevProblem &P, cudaStream_t s) {
+    k_round_begin<<<1, 1, 0, s>>>(P);
+    return (int)cudaGetLastError();
+}
+
+int launch_activity_phase(const DevProblem &P, int blocks, cudaStream_t s) {
+    if (P.n_items == 0) return 0;
+    k_activity<<<blocks, kCtaThreads, 0, s>>>(P);
+    return (int)cudaGetLastError();
+}
+
+int launch_candidate_phase(const DevProblem &P, int blocks, cudaStream_t s) {
+    if (P.n_mtiles == 0) return 0;
+    k_candidates<<<blocks, kCtaThreads, 0, s>>>(P);
+    return (int)cudaGetLastError();
+}
+
+int launch_finalize(const DevProblem &P, int blocks, cudaStream_t s) {
     if (P.n_chg_words == 0) return 0;
-    k_finalize<<<finalize_blocks, kFinalizeThreads, 0, (cudaStream_t)stream>>>(P);
+    k_finalize<<<blocks, 256, 0, s>>>(P);
     return (int)cudaGetLastError();
 }
 
-int megakernel_occupancy(int block, int *blocks_per_sm) {
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_megakernel, block, 0);
+int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_t s) {
+    k_condition<<<1, 1, 0, s>>>(P, (cudaGraphConditionalHandle)handle);
+    return (int)cudaGetLastError();
 }
 
-int launch_megakernel(const DevProblem &P, int grid, int block, void *stream) {
+int phase_occupancy(int *act, int *cand, int *mega) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(act, k_activity, kCtaThreads, 0);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(cand, k_candidates, kCtaThreads, 0);
+    if (e != cudaSuccess) return (int)e;
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(mega, k_megakernel, kCtaThreads, 0);
+}
+
+int launch_megakernel(const DevProblem &P, int grid, cudaStream_t s) {
     DevProblem Pc = P;
     void *args[] = {&Pc};
-    return (int)cudaLaunchCooperativeKernel((const void *)k_megakernel, dim3(grid), dim3(block), args, 0,
-                                            (cudaStream_t)stream);
+    return (int)cudaLaunchCooperativeKernel((const void *)k_megakernel, dim3(grid), dim3(kCtaThreads), args, 0, s);
 }
 
 }  // namespace gdp

@@ -43,7 +43,8 @@ class Options(C.Structure):
         ("thread_row_max", C.c_int),
         ("split_tile", C.c_int),
         ("device", C.c_int),
-        ("reserved", C.c_int * 8),
+        ("use_marking", C.c_int),
+        ("reserved", C.c_int * 7),
     ]
 
 
@@ -173,14 +174,14 @@ class MIP:
 
 
 def propagate(mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
-              split_tile: int = 0, lb=None, ub=None) -> Tuple[np.ndarray, np.ndarray, dict]:
+              split_tile: int = 0, lb=None, ub=None, use_marking: int = -1) -> Tuple[np.ndarray, np.ndarray, dict]:
     """One-shot propagation (upload, propagate, download) with statistics."""
     lib = load_library()
     p = mip.normalized()
     lbo = _f64(p.lb if lb is None else lb).copy()
     ubo = _f64(p.ub if ub is None else ub).copy()
     o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
-                        split_tile=split_tile)
+                        split_tile=split_tile, use_marking=use_marking)
     st = Stats()
     rc = lib.gdp_propagate_once(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val), _pd(p.lhs),
                                 _pd(p.rhs), _pd(lbo), _pd(ubo), _pi(p.vartype), C.byref(o), C.byref(st))
@@ -192,12 +193,12 @@ class Context:
     """Persistent device context: upload once, propagate many bound vectors."""
 
     def __init__(self, mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
-                 split_tile: int = 0):
+                 split_tile: int = 0, use_marking: int = -1):
         self._lib = load_library()
         self.mip = mip.normalized()
         p = self.mip
         o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
-                            split_tile=split_tile)
+                            split_tile=split_tile, use_marking=use_marking)
         h = C.c_void_p()
         rc = self._lib.gdp_context_create(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val),
                                           _pd(p.lhs), _pd(p.rhs), _pi(p.vartype), C.byref(o), C.byref(h))

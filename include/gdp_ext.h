@@ -29,12 +29,17 @@ typedef struct gdp_context gdp_context; /* opaque */
 typedef struct {
     int max_rounds;       /* round cap; <= 0 selects GDP_MAX_NUM_ROUNDS (100) */
     int sync_type;        /* GDP_SYNCTYPE: CPU_LOOP, GPU_LOOP or MEGAKERNEL */
-    int thread_row_max;   /* rows up to this length run one lane per row (bit-exact
-                             left-to-right sums); longer rows are split across CTAs.
-                             0 selects the default (1024). */
-    int split_tile;       /* non-zeros per split-row tile; 0 selects the default (4096) */
+    int thread_row_max;   /* rows up to this length run one lane per row (the reference's
+                             left-to-right sums and row test, bit for bit); longer rows are
+                             split into warp tiles. 0 selects the default (32). */
+    int split_tile;       /* non-zeros per split-row warp tile; 0 selects the default (1024) */
     int device;           /* CUDA device ordinal (default 0) */
-    int reserved[8];      /* must be zero */
+    int use_marking;      /* constraint marking: a round may process only the rows of variables
+                             changed in the previous round (same result as sweeping every row).
+                             1 (default, also -1): adaptive -- marked rounds follow rounds that
+                             tightened fewer than n_vars/16 bounds; 0: always sweep every row;
+                             2: every round after the first is marked */
+    int reserved[7];      /* must be zero */
 } gdp_options;
 
 typedef struct {
@@ -109,7 +114,7 @@ GDP_RETCODE gdp_propagate_once(int n_cons, int n_vars, int nnz, const int *csr_c
  *   - Calls share the array: calls that overlap on the GPU race and must be
  *     serialized by the caller. Each call re-initializes it.
  *   - Rows are summed left to right by one thread each: results equal the
- *     context path's for rows up to 1024 non-zeros.
+ *     context path's for rows up to its thread_row_max non-zeros.
  * stream: CUDA stream (NULL = legacy default stream); the call returns when the
  * propagation has finished. stats may be NULL (device_ms is not measured). */
 #define GDP_NOALLOC_MAX_VARS (1 << 20)

@@ -146,70 +146,178 @@ gdpo_acts gdpo_activities(int row, const int *col, const int *row_ptr, const dou
     return a;
 }
 
-/* ---- the GPU path's summation order for split rows ----
- * Rows longer than split_len are reduced by the GPU in tiles of split_tile
- * non-zeros: thread t of a 256-thread CTA sums elements t, t+256, ... of the
- * tile in order, a warp shuffle tree (offsets 16, 8, 4, 2, 1) combines the 32
- * lanes, the 8 warp partials are combined in warp order and the tile partials
- * in tile order; |a|(ub-lb) is reduced with an exact max. This emulation lets
- * the tests compare the GPU bit for bit on every row. With split_len = 0 the
- * oracle sums every row left to right, the reference's order. */
-static inline void acts_combine(gdpo_acts *a, const gdpo_acts *b) {
+static inline void atomic_max_d(double *addr, double v);
+static inline void atomic_min_d(double *addr, double v);
+
+/* ---- GPU mode: the row rule and summation order of the GB300 kernels ----
+ * Rows up to thread_row_max non-zeros follow the reference exactly. Longer
+ * rows differ in two ways that the GPU kernels use and the tests pin bit for
+ * bit:
+ *  1. the row test uses an FP32 upper bound U >= max |a|(ub-lb) instead of the
+ *     sequential EPS-max: a row is skipped when both infinity counts exceed 1,
+ *     or when min(rhs-minact, maxact-lhs) < 1e20 and U*(1+2^-20) <= that
+ *     minimum. U bounds the reference's maxactdelta from above, so every row
+ *     the reference processes is processed (the per-variable tests are the
+ *     reference's, exact); extra rows only matter when some |a|(ub-lb) lies
+ *     within 2e-9 of the slack.
+ *  2. rows up to split_tile non-zeros are summed by a group of g lanes
+ *     (gdpo_lanes_per_row): lane l sums elements l, l+g, ... in order and a
+ *     shuffle tree combines the group; longer rows are summed per warp tile
+ *     of split_tile non-zeros (lane l sums elements l, l+32, ... of the tile,
+ *     shuffle tree over 32 lanes), tile partials combined in tile order.
+ * U is computed from the doubles by integer rounding to float (outward) and
+ * two round-to-nearest float operations, identically here and on the GPU. */
+typedef struct {
+    double minact, maxact;
+    int minf, maxf;
+    float U;
+} gacc;
+
+static inline uint64_t dbits(double x) { uint64_t b; memcpy(&b, &x, 8); return b; }
+static inline float fbits(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
+
+/* magnitude bits of a double -> float magnitude rounded up (up=1) or down */
+static inline float f32_mag(uint64_t mag, int up) {
+    const int e = (int)(mag >> 52);
+    if (e == 2047) return (mag & 0xFFFFFFFFFFFFFULL) ? fbits(0x7FC00000u) : fbits(0x7F800000u);
+    const int fe = e - 1023 + 127;
+    if (fe >= 255) return up ? fbits(0x7F800000u) : fbits(0x7F7FFFFFu);
+    if (fe <= 0) return (up && mag) ? fbits(0x00800000u) : 0.0f;
+    const uint64_t man = mag & 0xFFFFFFFFFFFFFULL;
+    uint32_t fb = ((uint32_t)fe << 23) | (uint32_t)(man >> 29);
+    if (up && (man & 0x1FFFFFFFULL)) fb += 1u;
+    return fbits(fb);
+}
+/* float >= x (rounded toward +inf) and float <= x (toward -inf) */
+static inline float f32_up(double x) {
+    const uint64_t b = dbits(x), mag = b & 0x7FFFFFFFFFFFFFFFULL;
+    return (b >> 63) ? -f32_mag(mag, 0) : f32_mag(mag, 1);
+}
+static inline float f32_dn(double x) {
+    const uint64_t b = dbits(x), mag = b & 0x7FFFFFFFFFFFFFFFULL;
+    return (b >> 63) ? -f32_mag(mag, 1) : f32_mag(mag, 0);
+}
+static inline float delta_up(double coeff, double l, double u) {
+    const float au = f32_mag(dbits(coeff) & 0x7FFFFFFFFFFFFFFFULL, 1);
+    const float d = f32_up(u) - f32_dn(l);
+    return au * d;
+}
+
+static inline void gacc_init(gacc *s) { s->minact = 0.0; s->maxact = 0.0; s->minf = 0; s->maxf = 0; s->U = 0.0f; }
+
+static inline void gacc_add(gacc *s, double coeff, double l, double u) {
+    const int pos = coeff > O_EPS;
+    const int lneg = l <= -O_INF, upos = u >= O_INF;
+    const int min_inf = pos ? lneg : upos;
+    const int max_inf = pos ? upos : lneg;
+    s->minf += min_inf;
+    s->maxf += max_inf;
+    if (!min_inf) s->minact = s->minact + (coeff > 0 ? coeff * l : coeff * u);
+    if (!max_inf) s->maxact = s->maxact + (coeff > 0 ? coeff * u : coeff * l);
+    s->U = fmaxf(s->U, delta_up(coeff, l, u));
+}
+
+static inline void gacc_combine(gacc *a, const gacc *b) {
     a->minact = a->minact + b->minact;
     a->maxact = a->maxact + b->maxact;
-    a->maxactdelta = fmax(a->maxactdelta, b->maxactdelta);
-    a->minact_inf += b->minact_inf;
-    a->maxact_inf += b->maxact_inf;
+    a->minf += b->minf;
+    a->maxf += b->maxf;
+    a->U = fmaxf(a->U, b->U);
 }
 
-static gdpo_acts acts_tile(int b, int e, const int *col, const double *val, const double *lb,
-                           const double *ub) {
-    gdpo_acts th[256];
-    for (int t = 0; t < 256; t++) {
-        gdpo_acts a = {0.0, 0.0, 0.0, 0, 0};
-        for (int k = b + t; k < e; k += 256) {
-            const int j = col[k];
-            const double coeff = val[k];
-            const double l = lb[j], u = ub[j];
-            const double delta = fabs(coeff) * (u - l);
-            a.maxactdelta = fmax(a.maxactdelta, delta);
-            const int is_min_inf = eps_gt(coeff, 0) ? is_neginf(l) : is_posinf(u);
-            const int is_max_inf = eps_gt(coeff, 0) ? is_posinf(u) : is_neginf(l);
-            a.minact_inf += is_min_inf;
-            a.maxact_inf += is_max_inf;
-            if (!is_min_inf) a.minact = a.minact + (coeff > 0 ? coeff * l : coeff * u);
-            if (!is_max_inf) a.maxact = a.maxact + (coeff > 0 ? coeff * u : coeff * l);
-        }
-        th[t] = a;
+static gacc gacc_tile(int b, int e, const int *col, const double *val, const double *lb, const double *ub) {
+    gacc lane[32];
+    for (int l = 0; l < 32; l++) {
+        gacc_init(&lane[l]);
+        for (int k = b + l; k < e; k += 32) gacc_add(&lane[l], val[k], lb[col[k]], ub[col[k]]);
     }
-    gdpo_acts warp[8];
-    for (int w = 0; w < 8; w++) {
-        gdpo_acts *lane = &th[32 * w];
-        for (int off = 16; off > 0; off >>= 1)
-            for (int i = 0; i < off; i++) acts_combine(&lane[i], &lane[i + off]);
-        warp[w] = lane[0];
-    }
-    gdpo_acts s = warp[0];
-    for (int w = 1; w < 8; w++) acts_combine(&s, &warp[w]);
-    return s;
+    for (int off = 16; off > 0; off >>= 1)
+        for (int i = 0; i < off; i++) gacc_combine(&lane[i], &lane[i + off]);
+    return lane[0];
 }
 
-gdpo_acts gdpo_activities_split(int row, const int *col, const int *row_ptr, const double *val,
-                                const double *lb, const double *ub, int tile) {
+/* Lanes per row of a SELL-g slice: rows longer than thread_row_max and at
+ * most split_tile long get g = the smallest power of two >= ceil(len / 32),
+ * at least 2, at most 32. */
+int gdpo_lanes_per_row(int len, int thread_row_max, int tile) {
+    if (len <= thread_row_max || len > tile) return 1;
+    int g = 2;
+    while (g < 32 && g * 32 < len) g <<= 1;
+    return g;
+}
+
+/* SELL-g row: lane l of the row's group sums elements l, l+g, l+2g, ... in
+ * order, then a shuffle tree (offsets g/2, ..., 1) combines the group. */
+static gacc gacc_group(int b, int e, int g, const int *col, const double *val, const double *lb,
+                       const double *ub) {
+    gacc lane[32];
+    for (int l = 0; l < g; l++) {
+        gacc_init(&lane[l]);
+        for (int k = b + l; k < e; k += g) gacc_add(&lane[l], val[k], lb[col[k]], ub[col[k]]);
+    }
+    for (int off = g / 2; off > 0; off >>= 1)
+        for (int i = 0; i < off; i++) gacc_combine(&lane[i], &lane[i + off]);
+    return lane[0];
+}
+
+static gacc gpu_row_acts(int row, const int *col, const int *row_ptr, const double *val, const double *lb,
+                         const double *ub, int thread_row_max, int tile) {
     const int b0 = row_ptr[row], e0 = row_ptr[row + 1];
-    gdpo_acts a = acts_tile(b0, b0 + tile < e0 ? b0 + tile : e0, col, val, lb, ub);
+    gacc a;
+    if (e0 - b0 <= thread_row_max) {
+        gacc_init(&a);
+        for (int k = b0; k < e0; k++) gacc_add(&a, val[k], lb[col[k]], ub[col[k]]);
+        return a;
+    }
+    if (e0 - b0 <= tile) return gacc_group(b0, e0, gdpo_lanes_per_row(e0 - b0, thread_row_max, tile), col, val, lb, ub);
+    a = gacc_tile(b0, b0 + tile < e0 ? b0 + tile : e0, col, val, lb, ub);
     for (int b = b0 + tile; b < e0; b += tile) {
-        const gdpo_acts t = acts_tile(b, b + tile < e0 ? b + tile : e0, col, val, lb, ub);
-        acts_combine(&a, &t);
+        const gacc t = gacc_tile(b, b + tile < e0 ? b + tile : e0, col, val, lb, ub);
+        gacc_combine(&a, &t);
     }
     return a;
 }
 
-static inline gdpo_acts row_acts(int row, const int *col, const int *row_ptr, const double *val,
-                                 const double *lb, const double *ub, int split_len, int split_tile) {
-    if (split_len > 0 && row_ptr[row + 1] - row_ptr[row] > split_len)
-        return gdpo_activities_split(row, col, row_ptr, val, lb, ub, split_tile);
-    return gdpo_activities(row, col, row_ptr, val, lb, ub);
+int gdpo_gpu_row_go(double minact, double maxact, int minf, int maxf, float U, double lhs, double rhs) {
+    if (minf > 1 && maxf > 1) return 0;
+    const double s = rhs - minact, t = maxact - lhs;
+    const double mn = (t < s) ? t : s;
+    const float Um = U * 1.00000095367431640625f; /* 1 + 2^-20 */
+    if (mn < O_INF && (double)Um <= mn) return 0;
+    return 1;
+}
+
+static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
+                      const double *lhs, const double *rhs, const double *lb, const double *ub,
+                      const int *vartype, double *lb_out, double *ub_out,
+                      unsigned char *var_changed);
+
+/* Rows up to thread_row_max non-zeros: the GPU's FP32 bound only pre-filters,
+ * an exact second pass takes the reference's decision, so these rows follow
+ * the reference exactly (jacobi_row). Longer rows: warp tiles + U rule. */
+static int jacobi_row_gpu(int row, const int *col, const int *row_ptr, const double *val, const double *lhs,
+                          const double *rhs, const double *lb, const double *ub, const int *vartype,
+                          double *lb_out, double *ub_out, unsigned char *var_changed, int thread_row_max,
+                          int tile) {
+    if (row_ptr[row + 1] - row_ptr[row] <= thread_row_max)
+        return jacobi_row(row, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, var_changed);
+    const gacc a = gpu_row_acts(row, col, row_ptr, val, lb, ub, thread_row_max, tile);
+    if (!gdpo_gpu_row_go(a.minact, a.maxact, a.minf, a.maxf, a.U, lhs[row], rhs[row])) return 0;
+    int any = 0;
+    for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
+        const int j = col[k];
+        int lt, ut;
+        double nl, nu;
+        gdpo_tighten_variable(val[k], lhs[row], rhs[row], a.minact, a.maxact, a.minf, a.maxf, vartype[j] == 3,
+                              lb[j], ub[j], &lt, &nl, &ut, &nu);
+        if (lt) atomic_max_d(&lb_out[j], nl);
+        if (ut) atomic_min_d(&ub_out[j], nu);
+        if (lt || ut) {
+            any = 1;
+            if (var_changed) __atomic_store_n(&var_changed[j], (unsigned char)1, __ATOMIC_RELAXED);
+        }
+    }
+    return any;
 }
 
 /* Infeasibility rule of this project (the reference detects none): bounds
@@ -251,8 +359,8 @@ static inline void atomic_min_d(double *addr, double v) {
 static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, const double *lb, const double *ub,
                       const int *vartype, double *lb_out, double *ub_out,
-                      unsigned char *var_changed, int split_len, int split_tile) {
-    const gdpo_acts a = row_acts(row, col, row_ptr, val, lb, ub, split_len, split_tile);
+                      unsigned char *var_changed) {
+    const gdpo_acts a = gdpo_activities(row, col, row_ptr, val, lb, ub);
     int any = 0;
     if (!gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[row],
                                     rhs[row], a.maxactdelta))
@@ -284,7 +392,7 @@ int gdpo_jacobi_round(int m, int n, const int *col, const int *row_ptr, const do
 #endif
     for (int i = 0; i < m; i++) {
         if (mark && !mark[i]) continue;
-        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL, 0, 0);
+        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL);
         if (t && tight_row) tight_row[i] = 1;
         change |= t;
     }
@@ -331,7 +439,7 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
                       const int *vartype, int schedule, int max_rounds, int nthreads,
                       int split_len, int split_tile, gdpo_result *res) {
     gdpo_result r;
-    if (split_tile <= 0) split_len = 0;
+    const int gpu_mode = split_tile > 0;
     memset(&r, 0, sizeof(r));
     r.infeasible_var = -1;
     if (max_rounds <= 0) max_rounds = O_MAX_ROUNDS;
@@ -396,8 +504,12 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
 #endif
             for (int i = 0; i < m; i++) {
                 if (!mark[i]) continue;
-                change |= jacobi_row(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
-                                     ub, var_changed, split_len, split_tile);
+                if (gpu_mode)
+                    change |= jacobi_row_gpu(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
+                                             ub, var_changed, split_len, split_tile);
+                else
+                    change |= jacobi_row(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
+                                         ub, var_changed);
             }
         }
         /* marking for the next round: reference src/propagation_methods.cu:3-13 */

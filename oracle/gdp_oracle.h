@@ -73,15 +73,19 @@ int gdpo_propagate(int m, int n, int nnz, const int *col, const int *row_ptr, co
                    const int *vartype, int schedule, int max_rounds, int nthreads,
                    gdpo_result *res);
 
-/* gdpo_propagate with the GPU path's summation order for rows longer than
- * split_len (tiles of split_tile non-zeros; see gdpo_activities_split).
- * split_len = 0: every row left to right (the reference's order). */
+/* gdpo_propagate in GPU mode when split_tile > 0 (JACOBI schedule): the GB300
+ * kernels' row test (FP32 upper bound of max |a|(ub-lb), see gdp_oracle.c)
+ * and, for rows longer than split_len (the kernels' thread_row_max), their
+ * warp-tile summation order with split_tile non-zeros per tile. split_tile = 0
+ * is the reference mode (identical to gdpo_propagate). */
 int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, double *lb, double *ub,
                       const int *vartype, int schedule, int max_rounds, int nthreads,
                       int split_len, int split_tile, gdpo_result *res);
-gdpo_acts gdpo_activities_split(int row, const int *col, const int *row_ptr, const double *val,
-                                const double *lb, const double *ub, int tile);
+/* lanes per row the GPU mode uses for a row of len non-zeros */
+int gdpo_lanes_per_row(int len, int thread_row_max, int tile);
+/* the GPU mode's row test */
+int gdpo_gpu_row_go(double minact, double maxact, int minf, int maxf, float U, double lhs, double rhs);
 
 /* One JACOBI round on a snapshot, restricted to rows with mark[row] != 0
  * (mark == NULL: every row). Writes candidates into lb_out/ub_out (which must

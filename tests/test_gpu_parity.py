@@ -2,10 +2,11 @@
 reference's golden outputs.
 
 The GPU runs the deterministic Jacobi schedule. Rows up to thread_row_max
-non-zeros are summed left to right by one lane (the reference's order), longer
-rows in a fixed tile tree that the oracle reproduces (split_len/split_tile),
-so every comparison against the oracle with the same split parameters is bit
-for bit; comparisons against the reference's own outputs are bit for bit where
+non-zeros follow the reference exactly (left-to-right sums, the reference's
+row test); longer rows are summed in fixed warp tiles with an FP32-bounded row
+test, which the oracle's GPU mode reproduces (split_len/split_tile). Every
+comparison against the oracle with the same parameters is therefore bit for
+bit, and comparisons against the reference's own outputs are bit for bit where
 no row is split.
 """
 import numpy as np
@@ -20,22 +21,27 @@ from gdp_testutil import (GOLDEN_CASES, REF_TEST_EPS, assert_bitexact, assert_bo
 pytestmark = pytest.mark.gpu
 
 SYNCS = [gdp.CPU_LOOP, gdp.GPU_LOOP, gdp.MEGAKERNEL]
-TRM, TILE = 1024, 4096  # library defaults
+TRM, TILE = 32, 1024  # library defaults
+ALL_LTR = 1 << 20      # thread_row_max that keeps every test row on the left-to-right path
 
 
-def gpu(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=0, tile=0, lb=None, ub=None):
+def gpu(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=0, tile=0, lb=None, ub=None, marking=-1):
     return gdp.propagate(mip, sync_type=sync, max_rounds=max_rounds, thread_row_max=trm, split_tile=tile, lb=lb,
-                         ub=ub)
+                         ub=ub, use_marking=marking)
 
 
-def check_vs_oracle(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=TRM, tile=TILE):
-    lb, ub, st = gpu(mip, sync, max_rounds, trm, tile)
+def check_vs_oracle(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=TRM, tile=TILE, marking=-1):
+    lb, ub, st = gpu(mip, sync, max_rounds, trm, tile, marking=marking)
     ref = oracle.propagate(mip, oracle.JACOBI, max_rounds=max_rounds, split_len=trm, split_tile=tile, nthreads=8)
     assert st["rounds"] == ref.rounds
     assert bool(st["infeasible"]) == ref.infeasible
     if ref.infeasible:
         assert st["infeasible_var"] == ref.infeasible_var
     assert_bitexact(lb, ub, ref.lb, ref.ub, what=f"sync={sync} trm={trm} tile={tile}")
+    if marking == 2 and np.all(np.diff(mip.row_ptr) > 0):
+        # always-on marking processes exactly the rows the oracle's marking processes
+        assert st["rows_processed"] == ref.rows_processed
+        assert st["nnz_processed"] == ref.nnz_processed
     return st
 
 
@@ -44,10 +50,17 @@ def check_vs_oracle(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=TRM, tile=TILE):
 def test_golden_vs_reference_cpu_omp(name, sync):
     """Bit-exact against the reference's own cpu_omp round function (rows unsplit)."""
     mip, g = load_golden(name)
-    lb, ub, st = gpu(mip, sync)
+    lb, ub, st = gpu(mip, sync, trm=ALL_LTR)
     assert st["rounds"] == int(g["rounds_omp"])
     assert st["infeasible"] == int(g["infeasible_omp"])
     assert_bitexact(lb, ub, g["lb_omp"], g["ub_omp"], what=name)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_default_layout_vs_oracle(name):
+    """Library defaults (long rows split into warp tiles) against the oracle's GPU mode."""
+    mip, _ = load_golden(name)
+    check_vs_oracle(mip, gdp.MEGAKERNEL)
 
 
 @pytest.mark.parametrize("name", [c for c in GOLDEN_CASES])
@@ -82,21 +95,33 @@ def test_golden_analytical(name):
 @pytest.mark.parametrize("sync", SYNCS)
 def test_random_small_mip(seed, sync):
     check_vs_oracle(gdpgen.random_mip(0, seed=100 + seed), sync)
+    check_vs_oracle(gdpgen.random_mip(0, seed=100 + seed), sync, marking=2)
 
 
-@pytest.mark.parametrize("trm,tile", [(4, 3), (8, 5), (16, 1), (2, 256)])
+@pytest.mark.parametrize("trm,tile", [(4, 3), (8, 5), (16, 1), (2, 256), (1, 33)])
 def test_split_rows_bitexact(trm, tile):
-    """Force rows through the split (multi-CTA) path; the oracle emulates its tree."""
+    """Force rows through the split (warp-tile) path; the oracle emulates its tree."""
     mip = gdpgen.random_mip(0, seed=7)
     for sync in SYNCS:
         check_vs_oracle(mip, sync, trm=trm, tile=tile)
 
 
+@pytest.mark.parametrize("sync", SYNCS)
+def test_marking_equals_full_sweep(sync):
+    """Processing only rows with a changed variable gives the full-sweep result bit for bit."""
+    mip = gdpgen.random_mip(1, seed=9, m=40_000, n=30_000, len_max=3000, dense_len=6000, n_dense_rows=2)
+    a = gpu(mip, sync, trm=256, tile=512, marking=2)
+    b = gpu(mip, sync, trm=256, tile=512, marking=0)
+    assert a[2]["rounds"] == b[2]["rounds"]
+    assert a[2]["rows_processed"] < b[2]["rows_processed"]
+    assert_bitexact(a[0], a[1], b[0], b[1])
+
+
 @pytest.mark.parametrize("seed", [1, 2])
 def test_power_law_scaled(seed):
     mip = gdpgen.random_mip(1, seed=seed, m=100_000, n=75_000, len_max=5000, dense_len=20_000, n_dense_rows=4)
-    for sync in (gdp.CPU_LOOP, gdp.MEGAKERNEL):
-        st = check_vs_oracle(mip, sync, trm=1024, tile=4096)
+    for sync in SYNCS:
+        st = check_vs_oracle(mip, sync, trm=1024, tile=1024)
         assert st["rounds"] >= 2
 
 
@@ -108,8 +133,10 @@ def test_power_law_small_tiles_and_threshold():
 
 def test_chains_many_rounds():
     mip = gdpgen.chains(6000, chain_max=400, seed=2)
-    st = check_vs_oracle(mip, gdp.MEGAKERNEL, max_rounds=5000)
-    assert st["rounds"] > 100
+    for sync in SYNCS:
+        for marking in (0, 1, 2):
+            st = check_vs_oracle(mip, sync, max_rounds=5000, marking=marking)
+            assert st["rounds"] > 100
 
 
 def test_chains_infeasible():
@@ -201,7 +228,7 @@ def test_reference_python_driver_mirror():
                                           list(mip.vartype), synctype=synctype)
         assert_bitexact(np.array(lbs), np.array(ubs), g["lb_omp"], g["ub_omp"])
     lbs, ubs = gdp.propagateGPUReduction(mip.n, mip.m, mip.nnz, mip.col, mip.row_ptr, mip.val, mip.lhs, mip.rhs,
-                                         mip.lb, mip.ub, mip.vartype)
+                                         mip.lb, mip.ub, mip.vartype)  # Achterberg rows have <= 10 non-zeros
     assert_bitexact(np.array(lbs), np.array(ubs), g["lb_omp"], g["ub_omp"])
 
 
@@ -226,8 +253,23 @@ def test_single_row_and_empty_rows():
 
 def test_stats_accounting():
     mip = gdpgen.random_mip(0, seed=25)
-    _, _, st = gpu(mip, gdp.MEGAKERNEL)
+    _, _, st = gpu(mip, gdp.MEGAKERNEL, marking=0)
     assert st["rows_processed"] == st["rounds"] * mip.m
     assert st["nnz_processed"] == st["rounds"] * mip.nnz
     assert st["bytes_algorithmic"] == st["rounds"] * (12.0 * mip.nnz + 20.0 * mip.m + 36.0 * mip.n)
     assert st["device_ms"] > 0 and st["kernel_launches"] >= 2
+    _, _, sm = gpu(mip, gdp.MEGAKERNEL, marking=2)
+    assert sm["bytes_algorithmic"] == 12.0 * sm["nnz_processed"] + 20.0 * sm["rows_processed"] + \
+        36.0 * mip.n * sm["rounds"]
+
+
+def test_gpu_loop_graph_reused_and_cap_changes():
+    """The GPU_LOOP graph is built once per context and rebuilt when the round cap changes."""
+    mip, _ = load_golden("two_lines")
+    with gdp.Context(mip, sync_type=gdp.GPU_LOOP) as ctx:
+        a = ctx.propagate()
+        b = ctx.propagate()
+        assert a[2]["rounds"] == b[2]["rounds"] == 61
+        ctx.set_options(max_rounds=7, sync_type=gdp.GPU_LOOP)
+        c = ctx.propagate()
+        assert c[2]["rounds"] == 7 and not c[2]["converged"]
