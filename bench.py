@@ -287,7 +287,7 @@ def main():
             "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": rounds,
                        "converged": bool(stats[-1]["converged"]), "infeasible": bool(stats[-1]["infeasible"]),
                        "sync": args.sync, "layout": layout, "marking": args.marking,
-                       "rows_processed": stats[-1]["rows_processed"], "nnz_processed": stats[-1]["nnz_processed"], "parallelism": "replicas" if ws > 1 else "single",
+                       "rows_processed": stats[-1]["rows_processed"], "nnz_processed": stats[-1]["nnz_processed"], "nnz_exact": stats[-1]["nnz_exact"], "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (CSR %.0f MB vs 129 MB L2)" % (mip.nnz * 12 / 1e6),
                        "scale": args.scale},
             "hbm_gbs": achieved, "nnz_per_s": mip.nnz * rounds / (ms_step * 1e-3),

@@ -278,6 +278,8 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     const int npos = std::max(ns + n_lrows, 1);
     const int n_words = (n + 31) / 32;
     P.tile_part = (TilePart *)arena.alloc_bytes(sizeof(TilePart) * (size_t)std::max(n_tiles, 1));
+    P.tile_scr = (TileScr *)arena.alloc_bytes(sizeof(TileScr) * (size_t)std::max(n_tiles, 1));
+    P.row_exact = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
     P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);
     P.bnd = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
     P.bnd_nxt = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
@@ -285,11 +287,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.n_chg_words = n_words;
     P.flags = (RoundFlags *)arena.alloc_bytes(sizeof(RoundFlags) * 3);
     P.barrier = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 2);
-    P.queue = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 4);
+    P.queue = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 8);
     P.max_rounds = opts.max_rounds;
     d_lb = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     d_ub = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    if (!P.tile_part || !P.mark || !P.bnd || !P.bnd_nxt || !P.chg || !P.flags || !P.barrier || !P.queue ||
+    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.mark || !P.bnd || !P.bnd_nxt || !P.chg || !P.flags || !P.barrier || !P.queue ||
         !d_lb || !d_ub) {
         set_error("device allocation failed");
         return GDP_ERROR;
@@ -335,8 +337,9 @@ GDP_RETCODE Context::rounds_cpu_loop(cudaStream_t s, int *launches) {
         GDP_CUDA(launch_round_begin(P, s));
         GDP_CUDA(launch_activity_phase(P, act_blocks, s));
         GDP_CUDA(launch_candidate_phase(P, cand_blocks, s));
+        GDP_CUDA(launch_exact_phase(P, cand_blocks, s));
         GDP_CUDA(launch_finalize(P, vec_blocks, s));
-        *launches += 2 + (P.n_items > 0) + (P.n_mtiles > 0);
+        *launches += 2 + (P.n_items > 0) + 2 * (P.n_mtiles > 0);
         GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
         GDP_CUDA(cudaStreamSynchronize(s));
         go = h_flags[0].change && !h_flags[0].infeasible;
@@ -369,6 +372,7 @@ GDP_RETCODE Context::build_graph(cudaStream_t s) {
     int rc = launch_round_begin(P, cs);
     if (!rc) rc = launch_activity_phase(P, act_blocks, cs);
     if (!rc) rc = launch_candidate_phase(P, cand_blocks, cs);
+    if (!rc) rc = launch_exact_phase(P, cand_blocks, cs);
     if (!rc) rc = launch_finalize(P, vec_blocks, cs);
     if (!rc) rc = launch_condition(P, (unsigned long long)h, cs);
     cudaGraph_t captured = nullptr;
@@ -398,7 +402,7 @@ GDP_RETCODE Context::rounds_gpu_loop(cudaStream_t s, int *launches) {
     GDP_CUDA(cudaGraphLaunch(graph_exec, s));
     GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
     GDP_CUDA(cudaStreamSynchronize(s));
-    *launches += h_flags[0].rounds * (3 + (P.n_items > 0) + (P.n_mtiles > 0)) + 1;
+    *launches += h_flags[0].rounds * (3 + (P.n_items > 0) + 2 * (P.n_mtiles > 0)) + 1;
     return GDP_OKAY;
 }
 
@@ -418,7 +422,8 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
     std::memset(init, 0, sizeof(init));
     init[0].infeasible_var = INT_MAX;
     GDP_CUDA(cudaMemcpyAsync(P.flags, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    GDP_CUDA(cudaMemsetAsync(P.queue, 0, sizeof(unsigned) * 4, s));
+    GDP_CUDA(cudaMemsetAsync(P.queue, 0, sizeof(unsigned) * 8, s));
+    GDP_CUDA(cudaMemsetAsync(P.row_exact, 0, sizeof(int) * (size_t)std::max(P.n_lrows, 1), s));
     GDP_CUDA(cudaMemsetAsync(P.barrier, 0, sizeof(unsigned) * 2, s));
     GDP_CUDA(cudaMemsetAsync(P.chg, 0, sizeof(unsigned) * (size_t)std::max(P.n_chg_words, 1), s));
     GDP_CUDA(launch_interleave(P, lb_in, ub_in, vec_blocks, s));
@@ -453,6 +458,7 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         st->changed_vars = (long long)f.changed_vars;
         st->rows_processed = (long long)f.rows_proc;
         st->nnz_processed = (long long)f.nnz_proc;
+        st->nnz_exact = (long long)f.nnz_exact;
         st->bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc + 36.0 * n * (double)f.rounds;
         st->device_ms = ms;
     }

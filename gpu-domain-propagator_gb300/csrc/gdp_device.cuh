@@ -287,6 +287,112 @@ __device__ __forceinline__ bool reference_row_go(int minf, int maxf, double maxa
     return true;
 }
 
+// ---- FP32 row screen -------------------------------------------------------
+// Before any FP64 work a row is screened with FP32 interval arithmetic: an
+// enclosure of the FP64 activities the exact pass would compute, the same
+// infinity counts, and an upper bound U' >= U of the row filter's FP32 bound.
+// A row the screen proves skippable is skipped by the exact rule too, so the
+// screen changes no result; it only saves FP64 work on rows that cannot
+// tighten anything (most of the non-zeros of a round on wide rows).
+//
+// Double -> float magnitude enclosure by integer work: truncation of the
+// mantissa gives dn <= |x|, one float ulp more gives up >= |x|; magnitudes
+// below 2^-126 enclose as [0, 2^-126], at or above 2^128 as [FLT_MAX, inf].
+struct MagEnc {
+    float dn, up;
+};
+__device__ __forceinline__ MagEnc mag_enc(long long bits) {
+    const unsigned long long mag = (unsigned long long)bits & 0x7FFFFFFFFFFFFFFFULL;
+    const unsigned hi = (unsigned)(mag >> 32);
+    // low 32 bits of (mag >> 29) - (896 << 23): the float bit pattern when in range
+    const unsigned fb = __funnelshift_r((unsigned)mag, hi, 29) - (896u << 23);
+    MagEnc e;
+    if (hi < (897u << 20)) {
+        e.dn = 0.0f;
+        e.up = __uint_as_float(0x00800000u);
+    } else if (hi >= (1151u << 20)) {
+        e.dn = __uint_as_float(0x7F7FFFFFu);
+        e.up = __uint_as_float(0x7F800000u);
+    } else {
+        e.dn = __uint_as_float(fb);
+        e.up = __uint_as_float(fb + 1u);
+    }
+    return e;
+}
+
+// Screen accumulator: [mn_lo, mn_hi] and [mx_lo, mx_hi] enclose the exact sums
+// of the finite activity terms (each term enclosed with directed rounding);
+// S >= sum of the terms' magnitudes bounds the FP64 summation error.
+struct Scr {
+    float mn_lo, mn_hi, mx_lo, mx_hi, S, U;
+    int minf, maxf;
+};
+__device__ __forceinline__ void scr_init(Scr &c) {
+    c.mn_lo = 0.0f; c.mn_hi = 0.0f; c.mx_lo = 0.0f; c.mx_hi = 0.0f; c.S = 0.0f; c.U = 0.0f;
+    c.minf = 0; c.maxf = 0;
+}
+__device__ __forceinline__ void scr_add(Scr &c, long long ab, long long lbb, long long ubb) {
+    const bool pos = gt_eps_bits(ab);
+    const bool lneg = neginf_bits(lbb), upos = posinf_bits(ubb);
+    const bool min_inf = pos ? lneg : upos;
+    const bool max_inf = pos ? upos : lneg;
+    c.minf += min_inf;
+    c.maxf += max_inf;
+    const MagEnc A = mag_enc(ab), L = mag_enc(lbb), Ub = mag_enc(ubb);
+    const bool lsg = lbb < 0, usg = ubb < 0, asg = ab < 0;
+    // U' >= delta_up(a, lb, ub): every operand rounded no closer to zero
+    const float ub_hi = usg ? -Ub.dn : Ub.up, lb_lo = lsg ? -L.up : L.dn;
+    c.U = fmaxf(c.U, __fmul_rn(A.up, __fsub_rn(ub_hi, lb_lo)));
+    const bool gt0 = gt0_bits(ab);
+    // min term a * (gt0 ? lb : ub), max term a * (gt0 ? ub : lb)
+    const MagEnc bmin = gt0 ? L : Ub, bmax = gt0 ? Ub : L;
+    const bool smin = asg != (gt0 ? lsg : usg), smax = asg != (gt0 ? usg : lsg);
+    if (!min_inf) {
+        const float lo = __fmul_rd(A.dn, bmin.dn), hi = __fmul_ru(A.up, bmin.up);
+        c.mn_lo = __fadd_rd(c.mn_lo, smin ? -hi : lo);
+        c.mn_hi = __fadd_ru(c.mn_hi, smin ? -lo : hi);
+        c.S = __fadd_ru(c.S, hi);
+    }
+    if (!max_inf) {
+        const float lo = __fmul_rd(A.dn, bmax.dn), hi = __fmul_ru(A.up, bmax.up);
+        c.mx_lo = __fadd_rd(c.mx_lo, smax ? -hi : lo);
+        c.mx_hi = __fadd_ru(c.mx_hi, smax ? -lo : hi);
+        c.S = __fadd_ru(c.S, hi);
+    }
+}
+__device__ __forceinline__ void scr_combine(Scr &a, const Scr &b) {
+    a.mn_lo = __fadd_rd(a.mn_lo, b.mn_lo);
+    a.mn_hi = __fadd_ru(a.mn_hi, b.mn_hi);
+    a.mx_lo = __fadd_rd(a.mx_lo, b.mx_lo);
+    a.mx_hi = __fadd_ru(a.mx_hi, b.mx_hi);
+    a.S = __fadd_ru(a.S, b.S);
+    a.U = fmaxf(a.U, b.U);
+    a.minf += b.minf;
+    a.maxf += b.maxf;
+}
+// Largest float not above 1e20 (the infinity threshold).
+constexpr float kInfF32Dn = 0x1.5af1d6p+66f;
+// True when the row filter (u_filter_skips, and row_decision's skip branch)
+// certainly skips the row: the FP64 activities of any summation order lie in
+// [lo - E, hi + E] with E = 2^-20 S (the rounding error of n <= 2^31 FP64
+// additions is below n 2^-53 S), and FP64 rounding of rhs - minact and
+// maxact - lhs is monotone, so min(rhs - minact, maxact - lhs) >= the
+// directed-rounded lower end computed here.
+__device__ __forceinline__ bool scr_skips(const Scr &c, double lhs, double rhs) {
+    if (c.minf > 1 && c.maxf > 1) return true;
+    const float E = __fmul_ru(c.S, 9.5367431640625e-7f);
+    const MagEnc R = mag_enc(dbits(rhs)), Lh = mag_enc(dbits(lhs));
+    const bool rsg = dbits(rhs) < 0, lsg = dbits(lhs) < 0;
+    const float rhs_dn = rsg ? -R.up : R.dn, rhs_up = rsg ? -R.dn : R.up;
+    const float lhs_dn = lsg ? -Lh.up : Lh.dn, lhs_up = lsg ? -Lh.dn : Lh.up;
+    const float s_lo = __fsub_rd(rhs_dn, __fadd_ru(c.mn_hi, E));
+    const float s_hi = __fsub_ru(rhs_up, __fsub_rd(c.mn_lo, E));
+    const float t_lo = __fsub_rd(__fsub_rd(c.mx_lo, E), lhs_up);
+    const float t_hi = __fsub_ru(__fadd_ru(c.mx_hi, E), lhs_dn);
+    const float mn_lo = fminf(s_lo, t_lo), mn_hi = fminf(s_hi, t_hi);
+    return mn_hi < kInfF32Dn && __fmul_rn(c.U, kUMargin) <= mn_lo;
+}
+
 // The project's infeasibility rule (the reference detects none).
 __device__ __forceinline__ bool var_infeasible(double lb, double ub) {
     double s = fmax(fabs(lb), fabs(ub));

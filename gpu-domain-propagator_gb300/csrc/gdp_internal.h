@@ -30,6 +30,12 @@ struct TilePart {
     int pad;
 };
 
+// FP32 screen partial of a split-row tile (see Scr in gdp_device.cuh).
+struct TileScr {
+    float mn_lo, mn_hi, mx_lo, mx_hi, S, U;
+    int minf, maxf;
+};
+
 // Device-written round status. [0] is read by the host (CPU_LOOP), by the
 // graph's condition kernel (GPU_LOOP) and by every CTA of the megakernel;
 // [1], [2] are the megakernel's double-buffered per-round change flags.
@@ -42,10 +48,12 @@ struct RoundFlags {
     int done;            // loop finished (GPU_LOOP / MEGAKERNEL)
     int mark_cur;        // this round processes only marked rows (else every row)
     unsigned tight;      // tightenings found in this round (decides the next round's mode)
+    int exact;           // multi-tile rows of this round that need the exact pass
+    int pad;
     unsigned long long changed_vars;  // committed variable changes, all rounds
-    unsigned long long rows_proc;     // rows processed, all rounds
+    unsigned long long rows_proc;     // rows processed (screened), all rounds
     unsigned long long nnz_proc;      // their non-zeros
-    unsigned long long pad2;
+    unsigned long long nnz_exact;     // non-zeros that also went through the exact FP64 pass
 };
 
 enum DeviceError : int {
@@ -73,7 +81,9 @@ struct DevProblem {
     const int *tile_row;    // n_tiles
     const int *tile_begin;  // n_tiles (element offsets into lcol/lval)
     const int *tile_end;
-    TilePart *tile_part;    // n_tiles
+    TilePart *tile_part;    // n_tiles: exact FP64 partials
+    TileScr *tile_scr;      // n_tiles: FP32 screen partials
+    int *row_exact;         // n_lrows: round in which the row needs the exact pass
     int n_mtiles;           // tiles of rows with more than one tile (candidate phase)
     const int *mtiles;
     // warp work items of the activity phase, heaviest first: s >= 0 is slice s,
@@ -98,7 +108,7 @@ struct DevProblem {
     int n_chg_words;
     RoundFlags *flags;
     unsigned *barrier;     // megakernel grid barrier {count, generation}
-    unsigned *queue;       // work counters: [parity * 2 + phase]
+    unsigned *queue;       // work counters: [parity * 4 + phase]
     int max_rounds;
 };
 
@@ -113,6 +123,7 @@ int launch_mark_all(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_round_begin(const DevProblem &P, cudaStream_t s);
 int launch_activity_phase(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_candidate_phase(const DevProblem &P, int blocks, cudaStream_t s);
+int launch_exact_phase(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_finalize(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_t s);
 int launch_megakernel(const DevProblem &P, int grid, cudaStream_t s);

@@ -197,11 +197,46 @@ __device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
     }
 }
 
+__device__ __forceinline__ void scr_group_reduce(Scr &c, int g) {
+    for (int off = g >> 1; off > 0; off >>= 1) {
+        Scr o;
+        o.mn_lo = __shfl_down_sync(kFull, c.mn_lo, off);
+        o.mn_hi = __shfl_down_sync(kFull, c.mn_hi, off);
+        o.mx_lo = __shfl_down_sync(kFull, c.mx_lo, off);
+        o.mx_hi = __shfl_down_sync(kFull, c.mx_hi, off);
+        o.S = __shfl_down_sync(kFull, c.S, off);
+        o.U = __shfl_down_sync(kFull, c.U, off);
+        o.minf = __shfl_down_sync(kFull, c.minf, off);
+        o.maxf = __shfl_down_sync(kFull, c.maxf, off);
+        scr_combine(c, o);
+    }
+}
+
+// Adds the warp's row and non-zero counts to the round statistics.
+__device__ __forceinline__ void count_work(const DevProblem &P, int lane, int rows, int nnz, int nnz_exact) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        rows += __shfl_down_sync(kFull, rows, off);
+        nnz += __shfl_down_sync(kFull, nnz, off);
+        nnz_exact += __shfl_down_sync(kFull, nnz_exact, off);
+    }
+    if (lane == 0) {
+        if (rows) atomicAdd(&P.flags[0].rows_proc, (unsigned long long)rows);
+        if (nnz) atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)nnz);
+        if (nnz_exact) atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)nnz_exact);
+    }
+}
+
 // One SELL-g slice per warp: 32/g rows, g lanes per row. Lane l serves row
 // l >> lg and its elements sub, sub+g, ... (sub = l & (g-1)), stored
-// column-major (step i of lane l at slice_ptr[slice] + 32 i + l). g == 1 rows
-// are summed left to right and take the reference's exact row decision;
-// g > 1 rows are combined by a shuffle tree and use the FP32 bound rule.
+// column-major (step i of lane l at slice_ptr[slice] + 32 i + l).
+//   pass 0: FP32 screen; rows it proves skippable are done.
+//   pass 1: exact FP64 activities of the remaining rows. g == 1 rows are
+//           summed left to right and take the reference's exact row
+//           decision; g > 1 rows are combined by a shuffle tree and use the
+//           FP32 bound rule.
+//   pass 2: (g == 1, rare) the reference's sequential EPS-max.
+//   pass 3: candidates through the warp division queue.
 __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int lane, int round, bool marked,
                                            int *change, unsigned *tight_ctr, WarpSmem &ws) {
     const int lg = __ldg(P.slice_lg + slice);
@@ -220,34 +255,45 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     const double *val = P.sell_val + base;
     const bool leader = act && sub == 0;
 
-    // pass 1: activities + FP32 enclosure, each lane in order, then the group tree
+    // pass 0: FP32 screen
+    bool exact = false;
+    double lhs = 0.0, rhs = 0.0;
+    {
+        Scr c;
+        scr_init(c);
+#pragma unroll 4
+        for (int i = 0; i < cnt; i++) {
+            const int j = __ldcs(col + 32 * i);
+            const double a = __ldcs(val + 32 * i);
+            const double2 b = load_bnd(P, j);
+            scr_add(c, dbits(a), dbits(b.x), dbits(b.y));
+        }
+        if (g > 1) scr_group_reduce(c, g);
+        if (leader) {
+            lhs = __ldg(P.srow_lhs + r);
+            rhs = __ldg(P.srow_rhs + r);
+            exact = !scr_skips(c, lhs, rhs);
+        }
+        exact = __shfl_sync(kFull, exact, rl << lg) && act;
+    }
+    count_work(P, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
+    if (!__any_sync(kFull, exact)) return;
+
+    // pass 1: exact activities + FP32 enclosure, each lane in order, then the group tree
+    const int cnt1 = exact ? cnt : 0;
     Acc s;
     acc_init(s);
 #pragma unroll 4
-    for (int i = 0; i < cnt; i++) {
-        const int j = __ldcs(col + 32 * i);
-        const double a = __ldcs(val + 32 * i);
+    for (int i = 0; i < cnt1; i++) {
+        const int j = __ldg(col + 32 * i);
+        const double a = __ldg(val + 32 * i);
         const double2 b = load_bnd(P, j);
         acc_add<true>(s, a, b.x, b.y);
     }
     if (g > 1) acc_group_reduce(s, g);
-    {
-        int lsum = leader ? len : 0, rows = leader ? 1 : 0;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            lsum += __shfl_down_sync(kFull, lsum, off);
-            rows += __shfl_down_sync(kFull, rows, off);
-        }
-        if (lane == 0) {
-            atomicAdd(&P.flags[0].rows_proc, (unsigned long long)rows);
-            atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)lsum);
-        }
-    }
-    double lhs = 0.0, rhs = 0.0, mn = 0.0;
+    double mn = 0.0;
     int dec = 0;
-    if (leader) {
-        lhs = __ldg(P.srow_lhs + r);
-        rhs = __ldg(P.srow_rhs + r);
+    if (leader && exact) {
         mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
         if (g == 1) dec = row_decision(s.minf, s.maxf, s.U, s.L, mn);
         else dec = u_filter_skips(s.minf, s.maxf, s.U, mn) ? 0 : 1;
@@ -268,7 +314,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     }
     // pass 3: candidates through the warp division queue
     int tight = 0;
-    const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && act;
+    const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && exact;
     if (__any_sync(kFull, go)) {
         if (leader && dec == 1) ws.rc[rl] = make_rowc(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs);
         __syncwarp();
@@ -362,15 +408,25 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
     report_tight(tight, lane, change, tight_ctr);
 }
 
-// Activities of split-row tile t (lane l sums elements l, l+32, ... in order,
-// shuffle tree across lanes). A row that fits in one tile is finished here
-// (decision and candidates); tiles of longer rows store a partial for the
-// candidate phase.
-__device__ __forceinline__ void split_partial(const DevProblem &P, int t, int lane, int round, bool marked,
-                                              int *change, unsigned *tight_ctr, unsigned *qbuf) {
-    const int row = __ldg(P.tile_row + t);
-    if (marked && P.mark[P.n_srows + row] != round) return;
-    const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
+__device__ __forceinline__ void scr_shfl_reduce(Scr &c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Scr o;
+        o.mn_lo = __shfl_down_sync(kFull, c.mn_lo, off);
+        o.mn_hi = __shfl_down_sync(kFull, c.mn_hi, off);
+        o.mx_lo = __shfl_down_sync(kFull, c.mx_lo, off);
+        o.mx_hi = __shfl_down_sync(kFull, c.mx_hi, off);
+        o.S = __shfl_down_sync(kFull, c.S, off);
+        o.U = __shfl_down_sync(kFull, c.U, off);
+        o.minf = __shfl_down_sync(kFull, c.minf, off);
+        o.maxf = __shfl_down_sync(kFull, c.maxf, off);
+        scr_combine(c, o);
+    }
+}
+
+// Exact FP64 partial of the element range [b, e): lane l sums elements l,
+// l+32, ... in order, shuffle tree across lanes; lane 0 holds the result.
+__device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int lane) {
     Acc s;
     acc_init(s);
 #pragma unroll 4
@@ -381,26 +437,90 @@ __device__ __forceinline__ void split_partial(const DevProblem &P, int t, int la
         acc_add<false>(s, a, bb.x, bb.y);
     }
     acc_shfl_reduce(s);
+    return s;
+}
+
+// Activity phase, split-row tile t: the FP32 screen of the tile. A row that
+// fits in one tile is finished here (screen decision, exact pass, candidates);
+// tiles of longer rows store their screen partial for the candidate phase.
+__device__ __forceinline__ void split_partial(const DevProblem &P, int t, int lane, int round, bool marked,
+                                              int *change, unsigned *tight_ctr, unsigned *qbuf) {
+    const int row = __ldg(P.tile_row + t);
+    if (marked && P.mark[P.n_srows + row] != round) return;
+    const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
+    Scr c;
+    scr_init(c);
+#pragma unroll 4
+    for (int k = b + lane; k < e; k += 32) {
+        const int j = __ldcs(P.lcol + k);
+        const double a = __ldcs(P.lval + k);
+        const double2 bb = load_bnd(P, j);
+        scr_add(c, dbits(a), dbits(bb.x), dbits(bb.y));
+    }
+    scr_shfl_reduce(c);
     const int t0 = __ldg(P.lrow_tile0 + row);
     const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
+    int exact = 0;
     if (lane == 0) {
         atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)(e - b));
         if (t == t0) atomicAdd(&P.flags[0].rows_proc, 1ULL);
-        if (!single) {
-            TilePart tp;
-            tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf; tp.U = s.U; tp.pad = 0;
-            P.tile_part[t] = tp;
+        if (single) {
+            exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+            if (exact) atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)(e - b));
+        } else {
+            TileScr ts;
+            ts.mn_lo = c.mn_lo; ts.mn_hi = c.mn_hi; ts.mx_lo = c.mx_lo; ts.mx_hi = c.mx_hi;
+            ts.S = c.S; ts.U = c.U; ts.minf = c.minf; ts.maxf = c.maxf;
+            P.tile_scr[t] = ts;
         }
     }
-    if (single) split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, qbuf);
+    if (!single || !__shfl_sync(kFull, exact, 0)) return;
+    const Acc s = tile_exact(P, b, e, lane);
+    split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, qbuf);
 }
 
-// Candidate phase for tile t of a multi-tile row: lane 0 combines the row's
-// tile partials in tile order.
+// Candidate phase, tile t of a multi-tile row: the row's screen (the tile
+// partials combined by all lanes in a fixed order, so every tile of the row
+// reaches the same decision); a row the screen cannot skip gets this tile's
+// exact FP64 partial, and its first tile flags the row for the exact phase.
 __device__ __forceinline__ void split_cand(const DevProblem &P, int t, int lane, int round, bool marked,
-                                           int *change, unsigned *tight_ctr, unsigned *qbuf) {
+                                           int *exact_ctr) {
     const int row = __ldg(P.tile_row + t);
     if (marked && P.mark[P.n_srows + row] != round) return;
+    const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
+    Scr c;
+    scr_init(c);
+    for (int u = t0 + lane; u < t1; u += 32) {
+        const TileScr p = P.tile_scr[u];
+        Scr o;
+        o.mn_lo = p.mn_lo; o.mn_hi = p.mn_hi; o.mx_lo = p.mx_lo; o.mx_hi = p.mx_hi;
+        o.S = p.S; o.U = p.U; o.minf = p.minf; o.maxf = p.maxf;
+        scr_combine(c, o);
+    }
+    scr_shfl_reduce(c);
+    int exact = 0;
+    if (lane == 0) exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+    if (!__shfl_sync(kFull, exact, 0)) return;
+    const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
+    const Acc s = tile_exact(P, b, e, lane);
+    if (lane == 0) {
+        TilePart tp;
+        tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf; tp.U = s.U; tp.pad = 0;
+        P.tile_part[t] = tp;
+        atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)(e - b));
+        if (t == t0) {
+            P.row_exact[row] = round;
+            atomicAdd(exact_ctr, 1);
+        }
+    }
+}
+
+// Exact phase, tile t of a multi-tile row flagged this round: the row's exact
+// partials combined in tile order, then the decision and this tile's candidates.
+__device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane, int round, int *change,
+                                            unsigned *tight_ctr, unsigned *qbuf) {
+    const int row = __ldg(P.tile_row + t);
+    if (P.row_exact[row] != round) return;
     Acc s;
     acc_init(s);
     if (lane == 0) {
@@ -412,7 +532,7 @@ __device__ __forceinline__ void split_cand(const DevProblem &P, int t, int lane,
         for (int u = t0 + 1; u < t1; u++) {
             const TilePart p = P.tile_part[u];
             Acc o;
-            o.minact = p.minact; o.maxact = p.maxact; o.minf = p.minf; o.maxf = p.maxf; o.U = p.U;
+            o.minact = p.minact; o.maxact = p.maxact; o.minf = p.minf; o.maxf = p.maxf; o.U = p.U; o.L = 0.0f;
             acc_combine(s, o);
         }
     }
@@ -466,11 +586,20 @@ __device__ __forceinline__ void activity_phase(const DevProblem &P, int round, b
 }
 
 __device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
-                                                int *change, unsigned *tight_ctr, WarpSmem &ws, int lane) {
+                                                int *exact_ctr, int lane) {
     for (;;) {
         const int i = warp_next(ctr, lane);
         if (i >= P.n_mtiles) break;
-        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, change, tight_ctr, ws.q);
+        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, exact_ctr);
+    }
+}
+
+__device__ __forceinline__ void exact_phase(const DevProblem &P, int round, unsigned *ctr, int *change,
+                                            unsigned *tight_ctr, WarpSmem &ws, int lane) {
+    for (;;) {
+        const int i = warp_next(ctr, lane);
+        if (i >= P.n_mtiles) break;
+        split_exact(P, __ldg(P.mtiles + i), lane, round, change, tight_ctr, ws.q);
     }
 }
 
@@ -489,11 +618,17 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_activity(DevProblem P) {
 }
 
 __global__ void __launch_bounds__(kCtaThreads, 4) k_candidates(DevProblem P) {
-    __shared__ WarpSmem ws[kWarpsPerCta];
     const int round = P.flags[0].rounds;
     if (P.flags[0].infeasible) return;
-    candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].change, &P.flags[0].tight,
-                    ws[threadIdx.x >> 5], threadIdx.x & 31);
+    candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].exact, threadIdx.x & 31);
+}
+
+__global__ void __launch_bounds__(kCtaThreads, 4) k_exact(DevProblem P) {
+    __shared__ WarpSmem ws[kWarpsPerCta];
+    const int round = P.flags[0].rounds;
+    if (P.flags[0].infeasible || P.flags[0].exact == 0) return;
+    exact_phase(P, round, P.queue + 2, &P.flags[0].change, &P.flags[0].tight, ws[threadIdx.x >> 5],
+                threadIdx.x & 31);
 }
 
 // Every thread derives the same next-round mode from the final tightening count.
@@ -511,9 +646,11 @@ __global__ void k_round_begin(DevProblem P) {
     P.flags[0].mark_cur = r > 0 && next_round_marked(P, P.flags[0].tight);
     P.flags[0].change = 0;
     P.flags[0].tight = 0u;
+    P.flags[0].exact = 0;
     P.flags[0].rounds = r + 1;
     P.queue[0] = 0u;
     P.queue[1] = 0u;
+    P.queue[2] = 0u;
 }
 
 // GPU_LOOP: decides whether the graph's WHILE node runs another round.
@@ -592,8 +729,8 @@ __device__ bool grid_barrier(unsigned *bar, int *error) {
 }
 
 // Round loop on the device. flags[0] holds the sticky state; flags[1 + (round
-// & 1)].change is the per-round change flag and queue[2 * (round & 1) + phase]
-// the per-round work counters, double-buffered so that nothing a CTA may
+// & 1)] the per-round change flag, tightening and exact-row counts, and
+// queue[4 * (round & 1) + phase] the per-round work counters, double-buffered so that nothing a CTA may
 // still read is cleared: the next round's slots are cleared after the current
 // round's first barrier, which every CTA passes only after finishing the
 // previous round.
@@ -609,16 +746,26 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_megakernel(DevProblem P) {
             const int par = round & 1;
             int *change = &P.flags[1 + par].change;
             unsigned *tight = &P.flags[1 + par].tight;
-            activity_phase(P, round, marked, P.queue + 2 * par, change, tight, mine, lane);
+            int *exact = &P.flags[1 + par].exact;
+            unsigned *q = P.queue + 4 * par;
+            activity_phase(P, round, marked, q + 0, change, tight, mine, lane);
             if (!grid_barrier(P.barrier, err)) return;
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 P.flags[1 + (par ^ 1)].change = 0;
                 P.flags[1 + (par ^ 1)].tight = 0u;
-                P.queue[2 * (par ^ 1)] = 0u;
-                P.queue[2 * (par ^ 1) + 1] = 0u;
+                P.flags[1 + (par ^ 1)].exact = 0;
+                P.queue[4 * (par ^ 1) + 0] = 0u;
+                P.queue[4 * (par ^ 1) + 1] = 0u;
+                P.queue[4 * (par ^ 1) + 2] = 0u;
             }
-            candidate_phase(P, round, marked, P.queue + 2 * par + 1, change, tight, mine, lane);
-            if (!grid_barrier(P.barrier, err)) return;
+            if (P.n_mtiles) {
+                candidate_phase(P, round, marked, q + 1, exact, lane);
+                if (!grid_barrier(P.barrier, err)) return;
+                if (*((volatile int *)exact)) {
+                    exact_phase(P, round, q + 2, change, tight, mine, lane);
+                    if (!grid_barrier(P.barrier, err)) return;
+                }
+            }
             marked = next_round_marked(P, *((volatile unsigned *)tight));
             finalize_words(P, round, marked, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
             if (blockIdx.x == 0 && threadIdx.x == 0) P.flags[0].rounds = round;
@@ -676,6 +823,12 @@ int launch_candidate_phase(const DevProblem &P, int blocks, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
+int launch_exact_phase(const DevProblem &P, int blocks, cudaStream_t s) {
+    if (P.n_mtiles == 0) return 0;
+    k_exact<<<blocks, kCtaThreads, 0, s>>>(P);
+    return (int)cudaGetLastError();
+}
+
 int launch_finalize(const DevProblem &P, int blocks, cudaStream_t s) {
     if (P.n_chg_words == 0) return 0;
     k_finalize<<<blocks, 256, 0, s>>>(P);
@@ -690,7 +843,7 @@ int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_
 int phase_occupancy(int *act, int *cand, int *mega) {
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(act, k_activity, kCtaThreads, 0);
     if (e != cudaSuccess) return (int)e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(cand, k_candidates, kCtaThreads, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(cand, k_exact, kCtaThreads, 0);
     if (e != cudaSuccess) return (int)e;
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(mega, k_megakernel, kCtaThreads, 0);
 }

@@ -62,6 +62,7 @@ class Stats(C.Structure):
         ("bytes_algorithmic", C.c_double),
         ("device_ms", C.c_double),
         ("total_ms", C.c_double),
+        ("nnz_exact", C.c_longlong),
     ]
 
     def as_dict(self) -> dict:

@@ -56,6 +56,8 @@ typedef struct {
                                   (CSR col+val, row_ptr+lhs+rhs, lb/ub read+write and vartype) */
     double device_ms;       /* device time of the round loop (CUDA events) */
     double total_ms;        /* host wall time of the call */
+    long long nnz_exact;    /* non-zeros of the rows that the FP32 screen could not skip and that
+                               went through the exact FP64 pass, summed over rounds */
 } gdp_stats;
 
 /* Fills *opts with the defaults. */

@@ -273,3 +273,69 @@ def test_gpu_loop_graph_reused_and_cap_changes():
         ctx.set_options(max_rounds=7, sync_type=gdp.GPU_LOOP)
         c = ctx.propagate()
         assert c[2]["rounds"] == 7 and not c[2]["converged"]
+
+
+def _extreme_mip(seed, m=1500, n=4000, long_rows=6):
+    """Rows whose FP32 screen is stressed: coefficients from 1e-30 to 1e30,
+    bounds from subnormal to 1e19 and every infinity form, zero-slack
+    equalities, exact cancellation pairs, and split-length rows."""
+    rng = np.random.default_rng(seed)
+    lens = np.concatenate([rng.integers(1, 40, m - long_rows), rng.integers(1100, 3000, long_rows)])
+    rng.shuffle(lens)
+    row_ptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    nnz = int(row_ptr[-1])
+    col = np.concatenate([rng.choice(n, L, replace=False) for L in lens]).astype(np.int32)
+    val = rng.choice([-1.0, 1.0], nnz) * 10.0 ** rng.uniform(-30, 30, nnz)
+    small = rng.random(nnz) < 0.5
+    val[small] = rng.choice([-1.0, 1.0], small.sum()) * rng.uniform(0.5, 10, small.sum())
+    # cancellation pairs inside rows: a, -a
+    for i in rng.choice(m, m // 10, replace=False):
+        b, e = row_ptr[i], row_ptr[i + 1]
+        if e - b >= 2:
+            val[b + 1] = -val[b]
+    kind = rng.integers(0, 8, n)
+    lb = -rng.uniform(0, 100, n)
+    ub = rng.uniform(0, 100, n)
+    lb[kind == 1] = -1e20
+    ub[kind == 2] = 1e100
+    lb[kind == 3] = -np.inf
+    ub[kind == 4] = 5e-320  # subnormal
+    lb[kind == 4] = -0.0
+    lb[kind == 5], ub[kind == 5] = -1e19, 1e19
+    lb[kind == 6], ub[kind == 6] = 0.0, 0.0
+    vt = np.where(rng.random(n) < 0.5, 1, 3).astype(np.int32)
+    ilb, iub = np.ceil(lb), np.floor(ub)
+    fin = np.isfinite(ilb) & (np.abs(ilb) < 1e20)
+    lb = np.where((vt != 3) & fin, ilb, lb)
+    fin = np.isfinite(iub) & (np.abs(iub) < 1e20)
+    ub = np.where((vt != 3) & fin, iub, ub)
+    ub = np.maximum(ub, lb)
+    x0 = np.clip(np.zeros(n), np.maximum(lb, -1e6), np.minimum(ub, 1e6))
+    rows = np.repeat(np.arange(m), lens)
+    ax = np.bincount(rows, val * x0[col], m)
+    form = rng.integers(0, 5, m)
+    slack = np.abs(ax) * rng.uniform(0, 1e-3, m)
+    lhs = np.where(form == 0, ax, ax - slack)
+    rhs = np.where(form == 0, ax, ax + slack)
+    lhs[form == 1] = -1e20
+    rhs[form == 2] = np.inf
+    lhs[form == 3], rhs[form == 3] = -1e100, 1e100
+    return gdp.MIP(row_ptr, col, val, lhs, rhs, lb, ub, vt)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+@pytest.mark.parametrize("sync", [gdp.CPU_LOOP, gdp.MEGAKERNEL])
+def test_screen_extreme_magnitudes(seed, sync):
+    """The FP32 screen only skips rows the exact rule skips: bit-exact with the
+    oracle on magnitudes that overflow, underflow and cancel in FP32."""
+    mip = _extreme_mip(seed)
+    st = check_vs_oracle(mip, sync)
+    assert st["nnz_exact"] <= st["nnz_processed"]
+    st = check_vs_oracle(mip, sync, trm=4, tile=64, marking=2)
+
+
+def test_screen_skips_work():
+    """On the power-law instance the screen keeps most non-zeros away from the FP64 pass."""
+    mip = gdpgen.random_mip(1, seed=3, m=60_000, n=45_000, n_dense_rows=2, dense_len=20_000)
+    st = check_vs_oracle(mip, gdp.MEGAKERNEL)
+    assert st["nnz_exact"] < 0.5 * st["nnz_processed"]
