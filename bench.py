@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--marking", type=int, default=1, help="1: process only rows with a changed variable")
     ap.add_argument("--trm", type=int, default=0, help="thread_row_max (0: library default)")
     ap.add_argument("--tile", type=int, default=0, help="split_tile (0: library default)")
+    ap.add_argument("--workload", choices=["plain", "nodes", "instances", "chains"], default="plain",
+                    help="plain: the power-law MIP (the bench line); nodes / instances / chains: batched "
+                         "workloads timed against per-member plain propagations")
+    ap.add_argument("--members", type=int, default=0, help="batch members (0: the workload's default)")
     return ap.parse_args()
 
 
@@ -201,11 +205,142 @@ def run_reference(args, ws, rank):
     return 0
 
 
+BATCH_WORKLOADS = {
+    "nodes": "256 branch-and-bound nodes of one power-law MIP (m=200,000, n=150,000, Zipf(1.8) rows, ~2.4M nnz): "
+             "root fixpoint + k~U{1..50} integer variables fixed to a random in-domain value",
+    "instances": "64 power-law MIPs, m log-uniform in [1,000, 500,000], n=0.75m",
+    "chains": "128 chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
+              "[100,000, 1,000,000], 60% integer vars, 15% infinite bounds, 10% made infeasible",
+}
+
+
+def _batch_members(args):
+    import gdpgen
+    rng = np.random.default_rng(4242)
+    if args.workload == "nodes":
+        mip = gdpgen.random_mip(1, seed=2000, m=int(200_000 * args.scale), n=int(150_000 * args.scale),
+                                n_dense_rows=0)
+        return mip, None
+    if args.workload == "instances":
+        k = args.members or 64
+        ms = np.exp(rng.uniform(np.log(1_000), np.log(500_000 * args.scale), k)).astype(int)
+        return None, [gdpgen.random_mip(1, seed=3000 + i, m=int(m), n=int(0.75 * m), n_dense_rows=0)
+                      for i, m in enumerate(ms)]
+    k = args.members or 128
+    ms = np.exp(rng.uniform(np.log(100_000 * args.scale), np.log(1_000_000 * args.scale), k)).astype(int)
+    bad = set(rng.choice(k, max(1, k // 10), replace=False).tolist())
+    return None, [gdpgen.chains(int(m), chain_max=5000, seed=4000 + i, infeasible=i in bad)
+                  for i, m in enumerate(ms)]
+
+
+def _node_bounds(mip, root_lb, root_ub, n_nodes, seed):
+    rng = np.random.default_rng(seed)
+    ints = np.flatnonzero((mip.vartype != 3) & (root_ub - root_lb >= 1) & (np.abs(root_lb) < 1e19)
+                          & (np.abs(root_ub) < 1e19))
+    lbs, ubs = [], []
+    for _ in range(n_nodes):
+        lb, ub = root_lb.copy(), root_ub.copy()
+        fix = rng.choice(ints, size=min(len(ints), int(rng.integers(1, 51))), replace=False)
+        v = np.minimum(np.floor(lb[fix] + rng.random(len(fix)) * (ub[fix] - lb[fix] + 1)), ub[fix])
+        lb[fix] = v
+        ub[fix] = v
+        lbs.append(lb)
+        ubs.append(ub)
+    return lbs, ubs
+
+
+def run_batched(args, ws, rank, local):
+    """A batch timed against the same members propagated one by one through the
+    plain single-problem path (full sweeps every round, the reference's
+    schedule) and through the single-problem path with its adaptive marking."""
+    import torch
+
+    import gdp
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    mip, mips = _batch_members(args)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if args.workload == "nodes":
+        ctx = gdp.Context(mip, sync_type=gdp.MEGAKERNEL)
+        rlb, rub, rst = ctx.propagate()
+        members = _node_bounds(mip, rlb, rub, args.members or 256, seed=5)
+        batch = gdp.Batch.nodes(ctx, len(members[0]))
+        plain_mips = [mip] * len(members[0])
+        sizes = {"m": mip.m, "n": mip.n, "nnz": mip.nnz, "root_rounds": rst["rounds"]}
+    else:
+        batch = gdp.Batch.instances(mips)
+        members = ([m.lb for m in mips], [m.ub for m in mips])
+        plain_mips = mips
+        sizes = {"members": len(mips), "m_total": int(sum(m.m for m in mips)),
+                 "nnz_total": int(sum(m.nnz for m in mips))}
+    build_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        batch.propagate(*members)
+    clocks = Clocks(local)
+    clocks.start()
+    dev_ms, e2e_ms = [], []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        blb, bub, sts, tot = batch.propagate(*members)
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+        dev_ms.append(tot["device_ms"])
+    clk = clocks.stop()
+    value = statistics.median(dev_ms)
+
+    # plain: every member alone, device-resident bounds, CUDA-event time of its round loop
+    def plain_total(marking):
+        ctxs = {}
+        total, rounds, agree = 0.0, [], True
+        for k, pm in enumerate(plain_mips):
+            key = id(pm)
+            if key not in ctxs:
+                ctxs[key] = gdp.Context(pm, sync_type=gdp.MEGAKERNEL, use_marking=marking)
+            c = ctxs[key]
+            d_lb = torch.tensor(members[0][k], dtype=torch.float64, device="cuda")
+            d_ub = torch.tensor(members[1][k], dtype=torch.float64, device="cuda")
+            st = c.propagate_device(d_lb.data_ptr(), d_ub.data_ptr(), torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            total += st["device_ms"]
+            rounds.append(st["rounds"])
+            agree &= (st["rounds"] == sts[k]["rounds"] and bool(st["infeasible"]) == bool(sts[k]["infeasible"])
+                      and np.array_equal(d_lb.cpu().numpy().view(np.int64), blb[k].view(np.int64))
+                      and np.array_equal(d_ub.cpu().numpy().view(np.int64), bub[k].view(np.int64)))
+        for c in ctxs.values():
+            c.close()
+        return total, rounds, agree
+
+    plain_full_ms, rounds_full, agree_full = plain_total(0)
+    plain_adapt_ms, _, agree_adapt = plain_total(1)
+    line = {"metric": "ms-to-fixpoint", "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOADS[args.workload], **sizes, "scale": args.scale,
+                       "batch_rounds": tot["rounds"], "infeasible_members": tot["infeasible"],
+                       "rows_processed": tot["rows_processed"], "nnz_processed": tot["nnz_processed"],
+                       "nnz_exact": tot["nnz_exact"], "graph": batch.uses_graph, "parallelism": "single"},
+            "plain": {"full_sweep_ms": plain_full_ms, "adaptive_marking_ms": plain_adapt_ms,
+                      "rounds_max": max(rounds_full), "rounds_sum": int(sum(rounds_full)),
+                      "bitexact_full_sweep": bool(agree_full), "bitexact_adaptive": bool(agree_adapt),
+                      "speedup_vs_full_sweep": plain_full_ms / value,
+                      "speedup_vs_adaptive": plain_adapt_ms / value},
+            "e2e": {"value": statistics.median(e2e_ms), "unit": "ms",
+                    "h2d_bytes_per_step": int(16 * sum(len(x) for x in members[0])),
+                    "d2h_bytes_per_step": int(16 * sum(len(x) for x in members[0]))},
+            "gpu_launches": int(tot["kernel_launches"]), "clocks": clk,
+            "setup_s": {"generate": gen_s, "build": build_s}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.workload != "plain":
+        return run_batched(args, ws, rank, local)
 
     import torch
 

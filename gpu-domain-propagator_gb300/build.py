@@ -24,7 +24,8 @@ OBJ = PKG / "lib" / "obj"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["gdp_round.cu", "gdp_context.cu", "gdp_capi.cu", "gdp_noalloc.cu", "gdp_layout.cu"]
+CUDA_SOURCES = ["gdp_round.cu", "gdp_context.cu", "gdp_capi.cu", "gdp_noalloc.cu", "gdp_layout.cu", "gdp_batch.cu",
+                "gdp_batch_host.cu"]
 
 
 def _nvcc() -> str:

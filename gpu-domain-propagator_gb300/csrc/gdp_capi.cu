@@ -4,7 +4,9 @@
 #include <chrono>
 #include <exception>
 #include <new>
+#include <string>
 
+#include "gdp_batch.h"
 #include "gdp_context.h"
 #include "interface.h"
 
@@ -12,6 +14,10 @@ using gdp::Context;
 
 struct gdp_context {
     Context impl;
+};
+
+struct gdp_batch {
+    gdp::Batch impl;
 };
 
 namespace {
@@ -90,6 +96,61 @@ GDP_RETCODE gdp_context_create(int n_cons, int n_vars, int nnz, const int *col, 
         const GDP_RETCODE rc = c->impl.init(n_cons, n_vars, nnz, col, row_ptr, val, lhs, rhs, vartypes, opts);
         if (rc != GDP_OKAY) { delete c; return rc; }
         *out = c;
+        return GDP_OKAY;
+    });
+}
+
+GDP_RETCODE gdp_batch_create(int n_inst, const int *n_cons, const int *n_vars, const int *nnz,
+                             const int *const *col, const int *const *row_ptr, const double *const *val,
+                             const double *const *lhs, const double *const *rhs, const int *const *vartypes,
+                             const gdp_options *opts, gdp_batch **out) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!out) { gdp::set_error("null output pointer"); return GDP_ERROR; }
+        *out = nullptr;
+        if (n_inst <= 0 || !n_cons || !n_vars || !nnz || !col || !row_ptr || !val || !lhs || !rhs || !vartypes) {
+            gdp::set_error("a batch needs n_inst > 0 and every per-instance array");
+            return GDP_ERROR;
+        }
+        for (int k = 0; k < n_inst; k++)
+            if (n_cons[k] <= 0 || n_vars[k] <= 0 || nnz[k] <= 0) {
+                gdp::set_error("instance " + std::to_string(k) + " needs n_cons, n_vars and nnz > 0");
+                return GDP_ERROR;
+            }
+        gdp_batch *b = new gdp_batch();
+        const GDP_RETCODE rc =
+            b->impl.init_instances(n_inst, n_cons, n_vars, nnz, col, row_ptr, val, lhs, rhs, vartypes, opts);
+        if (rc != GDP_OKAY) { delete b; return rc; }
+        *out = b;
+        return GDP_OKAY;
+    });
+}
+
+GDP_RETCODE gdp_batch_create_nodes(gdp_context *ctx, int n_nodes, gdp_batch **out) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!out) { gdp::set_error("null output pointer"); return GDP_ERROR; }
+        *out = nullptr;
+        if (!ctx) { gdp::set_error("null context"); return GDP_ERROR; }
+        gdp_batch *b = new gdp_batch();
+        const GDP_RETCODE rc = b->impl.init_nodes(&ctx->impl, n_nodes);
+        if (rc != GDP_OKAY) { delete b; return rc; }
+        *out = b;
+        return GDP_OKAY;
+    });
+}
+
+GDP_RETCODE gdp_batch_propagate(gdp_batch *b, double *const *lbs, double *const *ubs, gdp_stats *member_stats,
+                                gdp_stats *total) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!b) { gdp::set_error("null batch"); return GDP_ERROR; }
+        return b->impl.propagate(lbs, ubs, member_stats, total);
+    });
+}
+
+int gdp_batch_uses_graph(const gdp_batch *b) { return b && b->impl.graph_ok ? 1 : 0; }
+
+GDP_RETCODE gdp_batch_destroy(gdp_batch *b) {
+    return guarded([&]() -> GDP_RETCODE {
+        delete b;
         return GDP_OKAY;
     });
 }

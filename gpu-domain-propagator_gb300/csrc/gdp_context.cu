@@ -106,6 +106,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     if (validate_csr(m, n, nnz, col, row_ptr, val, vartype) != GDP_OKAY) return GDP_ERROR;
 
     GDP_CUDA(cudaSetDevice(opts.device));
+    cudaGetLastError();  // every call below is checked; start from a clean error state
     GDP_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     GDP_CUDA(cudaEventCreate(&ev0));
     GDP_CUDA(cudaEventCreate(&ev1));
@@ -245,6 +246,12 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.sell_col, const int, sell_col);
     GDP_UP(P.sell_val, const double, sell_val);
     GDP_UP(P.srow_len, const int, srow_len);
+    {
+        std::vector<int> pos_slice(std::max(ns, 1), 0);
+        for (int s = 0; s < n_slices; s++)
+            for (int p = slice_row0[s]; p < slice_row0[s + 1]; p++) pos_slice[p] = s;
+        GDP_UP(P.pos_slice, const int, pos_slice);
+    }
     GDP_UP(P.srow_lhs, const double, srow_lhs);
     GDP_UP(P.srow_rhs, const double, srow_rhs);
     P.n_lrows = n_lrows;
@@ -279,6 +286,13 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     const int n_words = (n + 31) / 32;
     P.tile_part = (TilePart *)arena.alloc_bytes(sizeof(TilePart) * (size_t)std::max(n_tiles, 1));
     P.tile_scr = (TileScr *)arena.alloc_bytes(sizeof(TileScr) * (size_t)std::max(n_tiles, 1));
+    // deferred exact pass: per-class row queues (classes are contiguous position ranges)
+    P.defer_exact = 1;
+    for (int c = 0; c < 6; c++) { P.cls_begin[c] = 0; P.cls_end[c] = 0; }
+    for (int sl = n_slices - 1; sl >= 0; sl--) P.cls_begin[slice_lg[sl]] = slice_row0[sl];
+    for (int sl = 0; sl < n_slices; sl++) P.cls_end[slice_lg[sl]] = slice_row0[sl + 1];
+    P.xrow = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
+    P.xctr = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 32);
     P.row_exact = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
     P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);
     P.bnd = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
@@ -291,15 +305,16 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.max_rounds = opts.max_rounds;
     d_lb = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     d_ub = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.mark || !P.bnd || !P.bnd_nxt || !P.chg || !P.flags || !P.barrier || !P.queue ||
+    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.xrow || !P.xctr || !P.mark || !P.bnd || !P.bnd_nxt || !P.chg || !P.flags || !P.barrier || !P.queue ||
         !d_lb || !d_ub) {
         set_error("device allocation failed");
         return GDP_ERROR;
     }
 
     vec_blocks = std::max(1, std::min((std::max(n, npos) + 255) / 256, 8 * n_sms));
-    // marking index (variable -> row positions), built on the device from the layout
-    if (P.use_marking) {
+    // marking index (variable -> row positions), built on the device from the
+    // layout (also used by node batches when this context's rounds never mark)
+    {
         int *vp = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1));
         int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
         int *scratch = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1 + (n + 1 + 1023) / 1024 + 1));
@@ -311,7 +326,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     int act_bps = 0, cand_bps = 0, mega_bps = 0;
     GDP_CUDA(phase_occupancy(&act_bps, &cand_bps, &mega_bps));
     act_blocks = std::max(1, std::min(act_bps * n_sms, (P.n_items + kWarpsPerCta - 1) / kWarpsPerCta));
-    cand_blocks = std::max(1, std::min(cand_bps * n_sms, (P.n_mtiles + kWarpsPerCta - 1) / kWarpsPerCta));
+    cand_blocks = std::max(1, cand_bps * n_sms);  // the exact-rows phase shares this launch
     mega_grid = std::max(1, mega_bps) * n_sms;
     GDP_CUDA(cudaStreamSynchronize(stream));
     return GDP_OKAY;
@@ -339,7 +354,7 @@ GDP_RETCODE Context::rounds_cpu_loop(cudaStream_t s, int *launches) {
         GDP_CUDA(launch_candidate_phase(P, cand_blocks, s));
         GDP_CUDA(launch_exact_phase(P, cand_blocks, s));
         GDP_CUDA(launch_finalize(P, vec_blocks, s));
-        *launches += 2 + (P.n_items > 0) + 2 * (P.n_mtiles > 0);
+        *launches += 2 + (P.n_items > 0) + (P.n_mtiles > 0 || P.defer_exact) + (P.n_mtiles > 0);
         GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
         GDP_CUDA(cudaStreamSynchronize(s));
         go = h_flags[0].change && !h_flags[0].infeasible;
@@ -402,7 +417,7 @@ GDP_RETCODE Context::rounds_gpu_loop(cudaStream_t s, int *launches) {
     GDP_CUDA(cudaGraphLaunch(graph_exec, s));
     GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
     GDP_CUDA(cudaStreamSynchronize(s));
-    *launches += h_flags[0].rounds * (3 + (P.n_items > 0) + 2 * (P.n_mtiles > 0)) + 1;
+    *launches += h_flags[0].rounds * (3 + (P.n_items > 0) + (P.n_mtiles > 0 || P.defer_exact) + (P.n_mtiles > 0)) + 1;
     return GDP_OKAY;
 }
 
@@ -418,11 +433,13 @@ GDP_RETCODE Context::rounds_megakernel(cudaStream_t s, int *launches) {
 GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_out, double *ub_out,
                          cudaStream_t s, gdp_stats *st) {
     P.max_rounds = opts.max_rounds;
+    certified = false;
     RoundFlags init[3];
     std::memset(init, 0, sizeof(init));
     init[0].infeasible_var = INT_MAX;
     GDP_CUDA(cudaMemcpyAsync(P.flags, init, sizeof(init), cudaMemcpyHostToDevice, s));
     GDP_CUDA(cudaMemsetAsync(P.queue, 0, sizeof(unsigned) * 8, s));
+    GDP_CUDA(cudaMemsetAsync(P.xctr, 0, sizeof(unsigned) * 32, s));
     GDP_CUDA(cudaMemsetAsync(P.row_exact, 0, sizeof(int) * (size_t)std::max(P.n_lrows, 1), s));
     GDP_CUDA(cudaMemsetAsync(P.barrier, 0, sizeof(unsigned) * 2, s));
     GDP_CUDA(cudaMemsetAsync(P.chg, 0, sizeof(unsigned) * (size_t)std::max(P.n_chg_words, 1), s));
@@ -446,9 +463,14 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         if (st) st->device_error = f.error;
         return GDP_ERROR;
     }
+    // P.bnd now holds a fixpoint certified by a round that changed nothing
+    certified = !f.infeasible && !f.change;
     if (st) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev0, ev1);
+        if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess) {
+            ms = -1.f;
+            cudaGetLastError();
+        }
         st->rounds = f.rounds;
         st->infeasible = f.infeasible;
         st->infeasible_var = f.infeasible ? f.infeasible_var : -1;

@@ -43,6 +43,8 @@ public:
     int n_sms = 0, vec_blocks = 1, act_blocks = 1, cand_blocks = 1, mega_grid = 1;
     int n_srows = 0, n_slices = 0, n_lrows = 0, n_tiles = 0;
     long long sell_elems = 0;
+    // the last propagation converged feasibly: P.bnd is a fixpoint of the problem
+    bool certified = false;
     // GPU_LOOP graph (built on first use, reused while the context lives)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;

@@ -59,6 +59,7 @@ struct RoundFlags {
 enum DeviceError : int {
     kErrNone = 0,
     kErrBarrierTimeout = 1,  // a grid barrier wait exceeded its spin limit
+    kErrQueueOverflow = 2,   // a batched work queue ran out of room (a bug: capacities are exact bounds)
 };
 
 struct DevProblem {
@@ -97,7 +98,20 @@ struct DevProblem {
     // always (tests).
     int use_marking;
     unsigned mark_threshold;
+    // deferred exact pass (single-problem kernels): rows the FP32 screen
+    // cannot skip are queued per lanes-per-row class (log2 g = 0..5) and run in
+    // the next phase 32/g rows per warp, so the FP64 pipe sees full warps.
+    // Class lg's queue is xrow[cls_begin[lg] .. cls_end[lg]) (its row positions
+    // are exactly that range, slices being sorted by g).
+    int defer_exact;
+    int cls_begin[6], cls_end[6];
+    int *xrow;             // n_srows
+    unsigned *xctr;        // [parity * 16 + lg]: queue tails, [parity * 16 + 8 + lg]: pull counters
     int *mark;             // round in which the position is processed next (0: none)
+    // batched engine only (null otherwise): slice of each SELL row position and
+    // the round in which each slice was last queued
+    const int *pos_slice;  // n_srows
+    int *slice_stamp;      // n_slices
     const int *var_ptr;    // n + 1
     const int *var_pos;    // positions of each variable's rows
     // bounds

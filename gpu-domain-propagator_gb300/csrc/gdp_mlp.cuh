@@ -1,0 +1,126 @@
+// gdp_mlp.cuh -- the row-marking MLP on the device: 16 -> 64 -> 64 -> 1 with
+// ReLU, BF16 weights and activations, FP32 accumulation.
+//
+// Forward for a tile of 16 rows (one warp): layers 1 and 2 on the tensor cores
+// (mma.sync m16n8k16, BF16 x BF16 -> FP32); layer 1's accumulator fragments
+// become layer 2's A fragments in registers (after ReLU and rounding to BF16),
+// so activations never leave the warp. Layer 3 is a 64-term FP32 dot product
+// per row, reduced across the 4 lanes that hold the row.
+//
+// Fragment layouts (PTX ISA, mma.m16n8k16 with .bf16 inputs; g = lane >> 2,
+// t = lane & 3):
+//   A (16 x 16, row-major): {A[g][2t..2t+1]}, {A[g+8][2t..]}, {A[g][2t+8..]},
+//                           {A[g+8][2t+8..]}  -- four 32-bit registers
+//   B (16 x 8, "col"):      {B[2t..2t+1][g]}, {B[2t+8..2t+9][g]}
+//   C (16 x 8, FP32):       C[g][2t], C[g][2t+1], C[g+8][2t], C[g+8][2t+1]
+// A weight matrix W[n][k] stored row-major is exactly the "col" B operand of
+// x @ W^T, so B registers are 32-bit loads of two adjacent k of row n.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace gdp {
+
+constexpr int kMlpIn = 16, kMlpH = 64;
+
+// Device view of one model. Master weights are FP32 (training); the forward
+// reads the BF16 copies.
+struct MlpDev {
+    const __nv_bfloat16 *w1;   // [64][16]
+    const __nv_bfloat16 *w2;   // [64][64]
+    const __nv_bfloat16 *w2t;  // [64][64] transposed (backward)
+    const __nv_bfloat16 *w3;   // [64]
+    const float *b1, *b2, *b3;  // [64], [64], [1]
+};
+
+__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo (low half)
+    return *reinterpret_cast<const unsigned *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// B operand registers of W[n0 + g][k0 + 2t ..] (row-major W with ld columns).
+__device__ __forceinline__ void load_b(const __nv_bfloat16 *W, int ld, int n0, int k0, int lane, unsigned &b0,
+                                       unsigned &b1) {
+    const int g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16 *p = W + (size_t)(n0 + g) * ld + k0 + 2 * t;
+    b0 = __ldg(reinterpret_cast<const unsigned *>(p));
+    b1 = __ldg(reinterpret_cast<const unsigned *>(p + 8));
+}
+
+// Layer outputs of a 16-row tile in C-fragment layout: acc[n-tile][4].
+struct MlpTile {
+    float a1[8][4];  // layer-1 pre-activations (16 x 64)
+    float a2[8][4];  // layer-2 pre-activations (16 x 64)
+    float z[2];      // logits of rows g and g+8 (valid in every lane of the quad)
+};
+
+// Forward of the 16 x 16 input tile given as A registers (BF16).
+__device__ __forceinline__ void mlp_forward_tile(const MlpDev &M, const unsigned (&x)[4], int lane, MlpTile &T) {
+    const int t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const float bl = __ldg(M.b1 + nt * 8 + 2 * t), bh = __ldg(M.b1 + nt * 8 + 2 * t + 1);
+        T.a1[nt][0] = bl; T.a1[nt][1] = bh; T.a1[nt][2] = bl; T.a1[nt][3] = bh;
+        unsigned b0, b1;
+        load_b(M.w1, kMlpIn, nt * 8, 0, lane, b0, b1);
+        mma_bf16(T.a1[nt], x, b0, b1);
+    }
+    // layer-1 accumulators -> layer-2 A fragments (ReLU, BF16)
+    unsigned h[4][4];
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+        const float *c0 = T.a1[2 * kt], *c1 = T.a1[2 * kt + 1];
+        h[kt][0] = pack_bf16(fmaxf(c0[0], 0.f), fmaxf(c0[1], 0.f));
+        h[kt][1] = pack_bf16(fmaxf(c0[2], 0.f), fmaxf(c0[3], 0.f));
+        h[kt][2] = pack_bf16(fmaxf(c1[0], 0.f), fmaxf(c1[1], 0.f));
+        h[kt][3] = pack_bf16(fmaxf(c1[2], 0.f), fmaxf(c1[3], 0.f));
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const float bl = __ldg(M.b2 + nt * 8 + 2 * t), bh = __ldg(M.b2 + nt * 8 + 2 * t + 1);
+        T.a2[nt][0] = bl; T.a2[nt][1] = bh; T.a2[nt][2] = bl; T.a2[nt][3] = bh;
+#pragma unroll
+        for (int kt = 0; kt < 4; kt++) {
+            unsigned b0, b1;
+            load_b(M.w2, kMlpH, nt * 8, kt * 16, lane, b0, b1);
+            mma_bf16(T.a2[nt], h[kt], b0, b1);
+        }
+    }
+    // layer 3: FP32 dot of ReLU(a2) with w3, partial per lane, quad reduction
+    float z0 = 0.f, z1 = 0.f;
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const float wl = __bfloat162float(M.w3[nt * 8 + 2 * t]), wh = __bfloat162float(M.w3[nt * 8 + 2 * t + 1]);
+        z0 = fmaf(fmaxf(T.a2[nt][0], 0.f), wl, z0);
+        z0 = fmaf(fmaxf(T.a2[nt][1], 0.f), wh, z0);
+        z1 = fmaf(fmaxf(T.a2[nt][2], 0.f), wl, z1);
+        z1 = fmaf(fmaxf(T.a2[nt][3], 0.f), wh, z1);
+    }
+    z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
+    z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+    const float b3 = __ldg(M.b3);
+    T.z[0] = z0 + b3;
+    T.z[1] = z1 + b3;
+}
+
+// A registers of a 16 x 16 BF16 tile stored row-major in shared memory.
+__device__ __forceinline__ void load_a_smem(const __nv_bfloat16 *X, int lane, unsigned (&a)[4]) {
+    const int g = lane >> 2, t = lane & 3;
+    a[0] = *reinterpret_cast<const unsigned *>(X + g * 16 + 2 * t);
+    a[1] = *reinterpret_cast<const unsigned *>(X + (g + 8) * 16 + 2 * t);
+    a[2] = *reinterpret_cast<const unsigned *>(X + g * 16 + 2 * t + 8);
+    a[3] = *reinterpret_cast<const unsigned *>(X + (g + 8) * 16 + 2 * t + 8);
+}
+
+}  // namespace gdp

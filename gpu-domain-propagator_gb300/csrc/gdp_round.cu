@@ -1,612 +1,12 @@
 // gdp_round.cu -- one Jacobi propagation round on sm_103a, as phase kernels
 // (CPU_LOOP and GPU_LOOP drivers) and as a persistent cooperative megakernel
-// that runs every round in one launch (MEGAKERNEL driver).
-//
-// A round reads the round-start bounds (cur), writes every tightening into nxt
-// with an FP64 min/max atomic and flags the variable in a bitmap; the finalize
-// phase copies flagged variables nxt -> cur, applies the infeasibility rule
-// and marks the rows of changed variables for the next round. The result does
-// not depend on scheduling: each row's sums run in a fixed order from the
-// snapshot and min/max commute.
-//
-// GB300's FP64 pipe (about 1.75 lane-ops per clock per SM) is the scarce
-// resource, so the kernels spend it only on the reference's arithmetic: 2 DMUL
-// + 2 DADD per non-zero for the activities. Classification against the
-// +-1e20 infinity thresholds is integer work on the bit patterns, the
-// reference's row test (canConsBeTightened) is pre-filtered with an FP32 upper
-// bound of max |a|(ub - lb) and decided exactly only for rows that survive,
-// and the candidate divisions of a warp are gathered into a queue and run 32
-// at a time instead of diverging.
-//
-// Reference: the round body of GPUAtomicDomainPropagation
-// (src/kernels/atomic_kernel.cuh:9-450) and of the megakernel
-// (src/kernels/atomic_megakernel.cuh:14-490), re-planned for a snapshot
-// schedule; math from src/propagation_methods.cuh:78-276.
-#include <climits>
-#include <cuda_runtime.h>
-
-#include "gdp_device.cuh"
-#include "gdp_internal.h"
+// that runs every round in one launch (MEGAKERNEL driver). The round's device
+// functions live in gdp_round.cuh.
+#include "gdp_round.cuh"
 
 namespace gdp {
 
 namespace {
-
-constexpr unsigned kFull = 0xffffffffu;
-constexpr int kQueueCap = 128;  // >= 31 pending + 64 pushed per step
-
-__device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
-    atomicOr(P.chg + (j >> 5), 1u << (j & 31));
-}
-
-// Bounds are written by the finalize phase of the same megakernel launch, so
-// they are read with coherent loads (never the read-only path).
-__device__ __forceinline__ double2 load_bnd(const DevProblem &P, int j) { return P.bnd[j]; }
-
-// Row constants of tightenVariable (src/propagation_methods.cuh:223-276), with
-// float thresholds that decide most per-element EPS tests without FP64:
-// d <= x if d_hi <= f32_dn(x); fl(d - x) > 1e-9 if d_lo > f32_up(fl(x + 4e-9))
-// (then d - x > 3e-9 for |x| < 2^24, and d > x with ulp(x) > 3.7e-9 above).
-struct RowC {
-    double slack, surplus;  // rhs - minact, lhs - maxact
-    double neg_surplus;     // maxact - lhs
-    int minf, maxf;
-    int ok;                 // bit 0: rhs side usable, bit 1: lhs side usable
-    float slack_dn, slack_hi, nsur_dn, nsur_hi;
-};
-
-__device__ __forceinline__ RowC make_rowc(double minact, double maxact, int minf, int maxf, double lhs,
-                                          double rhs) {
-    RowC c;
-    c.slack = dsub(rhs, minact);
-    c.surplus = dsub(lhs, maxact);
-    c.neg_surplus = dsub(maxact, lhs);
-    c.minf = minf;
-    c.maxf = maxf;
-    const bool rhs_ok = !posinf_bits(dbits(rhs)) && !neginf_bits(dbits(minact));
-    const bool lhs_ok = !neginf_bits(dbits(lhs)) && !posinf_bits(dbits(maxact));
-    c.ok = (rhs_ok ? 1 : 0) | (lhs_ok ? 2 : 0);
-    c.slack_dn = f32_dn(dbits(c.slack));
-    c.slack_hi = f32_up(dbits(dadd(c.slack, 4e-9)));
-    c.nsur_dn = f32_dn(dbits(c.neg_surplus));
-    c.nsur_hi = f32_up(dbits(dadd(c.neg_surplus, 4e-9)));
-    return c;
-}
-
-// 0: EPSGT(d, x) is false, 1: true, 2: undecided from the enclosure.
-__device__ __forceinline__ int side_test(const DeltaBox &b, float x_dn, float x_hi) {
-    if (b.hi <= x_dn) return 0;
-    if (b.lo > x_hi) return 1;
-    return 2;
-}
-
-// Which candidate sides of element (a, lb, ub) need a division. Bit 0: upper
-// bound (tightenVarUpperBound), bit 1: lower bound (tightenVarLowerBound).
-// The FP64 product |a|(ub-lb) -- equal bit for bit to the reference's
-// coeff*(ub-lb) / coeff*(lb-ub) -- is formed only when the enclosure leaves a
-// test undecided.
-__device__ __forceinline__ int candidate_sides(const RowC &c, double a, double lb, double ub) {
-    const long long ab = dbits(a), lbb = dbits(lb), ubb = dbits(ub);
-    const DeltaBox box = delta_box(ab, lbb, ubb);
-    int rs = (c.ok & 1) ? side_test(box, c.slack_dn, c.slack_hi) : 0;
-    int ls = (c.ok & 2) ? side_test(box, c.nsur_dn, c.nsur_hi) : 0;
-    if (rs == 2 || ls == 2) {
-        const double d = dmul(fabs(a), dsub(ub, lb));
-        if (rs == 2) rs = eps_gt_fast(d, c.slack) ? 1 : 0;
-        if (ls == 2) ls = eps_gt_fast(d, c.neg_surplus) ? 1 : 0;
-    }
-    const bool pos = gt0_bits(ab);
-    const bool u_side = pos ? rs : ls;
-    const bool l_side = pos ? ls : rs;
-    const int nu = pos ? c.minf : c.maxf;
-    const int nl = pos ? c.maxf : c.minf;
-    const bool u_ok = u_side && (nu == 0 || (nu == 1 && neginf_bits(lbb)));
-    const bool l_ok = l_side && (nl == 0 || (nl == 1 && posinf_bits(ubb)));
-    return (u_ok ? 1 : 0) | (l_ok ? 2 : 0);
-}
-
-// One candidate (side 0: upper, 1: lower) of variable j; applies it with an
-// FP64 atomic if EPS-better than the snapshot. Returns true if it tightened.
-__device__ __forceinline__ bool apply_side(const DevProblem &P, const RowC &c, int j, double a, int side) {
-    const double2 b = load_bnd(P, j);
-    const bool pos = gt0_bits(dbits(a));
-    const bool cont = __ldg(P.is_cont + j) != 0;
-    if (side == 0) {
-        const int ninf = pos ? c.minf : c.maxf;
-        double nb = ddiv(pos ? c.slack : c.surplus, a);
-        if (ninf == 0) nb = dadd(nb, b.x);
-        if (!cont) nb = eps_floor(nb);
-        if (eps_lt(nb, b.y)) {
-            atomic_min_f64(&P.bnd_nxt[j].y, nb);
-            mark_changed(P, j);
-            return true;
-        }
-    } else {
-        const int ninf = pos ? c.maxf : c.minf;
-        double nb = ddiv(pos ? c.surplus : c.slack, a);
-        if (ninf == 0) nb = dadd(nb, b.y);
-        if (!cont) nb = eps_ceil(nb);
-        if (eps_gt(nb, b.x)) {
-            atomic_max_f64(&P.bnd_nxt[j].x, nb);
-            mark_changed(P, j);
-            return true;
-        }
-    }
-    return false;
-}
-
-// ---- warp division queue --------------------------------------------------
-// Items are 32-bit codes; the caller decodes them. push() appends each lane's
-// items (ballot + prefix), drain() runs full batches of 32.
-struct WarpQueue {
-    unsigned *q;
-    int cnt;  // warp-uniform
-};
-
-template <class Run>
-__device__ __forceinline__ void queue_drain(WarpQueue &Q, int lane, bool all, Run &&run) {
-    while (Q.cnt >= 32 || (all && Q.cnt > 0)) {
-        const int take = Q.cnt < 32 ? Q.cnt : 32;
-        if (lane < take) run(Q.q[lane]);
-        __syncwarp();
-        const int rest = Q.cnt - take;
-        for (int i = lane; i < rest; i += 32) Q.q[i] = Q.q[take + i];
-        __syncwarp();
-        Q.cnt = rest;
-    }
-}
-
-__device__ __forceinline__ void queue_push(WarpQueue &Q, int lane, int sides, unsigned code_base) {
-    const unsigned bu = __ballot_sync(kFull, sides & 1);
-    const unsigned bl = __ballot_sync(kFull, sides & 2);
-    const unsigned lt = (1u << lane) - 1u;
-    if (sides & 1) Q.q[Q.cnt + __popc(bu & lt)] = code_base | 0u;
-    if (sides & 2) Q.q[Q.cnt + __popc(bu) + __popc(bl & lt)] = code_base | 1u;
-    __syncwarp();
-    Q.cnt += __popc(bu) + __popc(bl);
-}
-
-// Warp-aggregated round bookkeeping: change flag and tightening count.
-__device__ __forceinline__ void report_tight(int tight, int lane, int *change, unsigned *tight_ctr) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) tight += __shfl_down_sync(kFull, tight, off);
-    if (lane == 0 && tight) {
-        *change = 1;
-        atomicAdd(tight_ctr, (unsigned)tight);
-    }
-}
-
-// ---- SELL-g rows: one warp per slice, g lanes per row ----------------------
-struct WarpSmem {
-    RowC rc[32];
-    unsigned q[kQueueCap];
-};
-
-// Combines the partial accumulators of a group of g lanes (g a power of two,
-// warp-uniform) into its first lane: shuffle tree with offsets g/2, ..., 1.
-__device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
-    for (int off = g >> 1; off > 0; off >>= 1) {
-        Acc o;
-        o.minact = __shfl_down_sync(kFull, s.minact, off);
-        o.maxact = __shfl_down_sync(kFull, s.maxact, off);
-        o.minf = __shfl_down_sync(kFull, s.minf, off);
-        o.maxf = __shfl_down_sync(kFull, s.maxf, off);
-        o.U = __shfl_down_sync(kFull, s.U, off);
-        o.L = __shfl_down_sync(kFull, s.L, off);
-        acc_combine(s, o);
-    }
-}
-
-__device__ __forceinline__ void scr_group_reduce(Scr &c, int g) {
-    for (int off = g >> 1; off > 0; off >>= 1) {
-        Scr o;
-        o.mn_lo = __shfl_down_sync(kFull, c.mn_lo, off);
-        o.mn_hi = __shfl_down_sync(kFull, c.mn_hi, off);
-        o.mx_lo = __shfl_down_sync(kFull, c.mx_lo, off);
-        o.mx_hi = __shfl_down_sync(kFull, c.mx_hi, off);
-        o.S = __shfl_down_sync(kFull, c.S, off);
-        o.U = __shfl_down_sync(kFull, c.U, off);
-        o.minf = __shfl_down_sync(kFull, c.minf, off);
-        o.maxf = __shfl_down_sync(kFull, c.maxf, off);
-        scr_combine(c, o);
-    }
-}
-
-// Adds the warp's row and non-zero counts to the round statistics.
-__device__ __forceinline__ void count_work(const DevProblem &P, int lane, int rows, int nnz, int nnz_exact) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        rows += __shfl_down_sync(kFull, rows, off);
-        nnz += __shfl_down_sync(kFull, nnz, off);
-        nnz_exact += __shfl_down_sync(kFull, nnz_exact, off);
-    }
-    if (lane == 0) {
-        if (rows) atomicAdd(&P.flags[0].rows_proc, (unsigned long long)rows);
-        if (nnz) atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)nnz);
-        if (nnz_exact) atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)nnz_exact);
-    }
-}
-
-// One SELL-g slice per warp: 32/g rows, g lanes per row. Lane l serves row
-// l >> lg and its elements sub, sub+g, ... (sub = l & (g-1)), stored
-// column-major (step i of lane l at slice_ptr[slice] + 32 i + l).
-//   pass 0: FP32 screen; rows it proves skippable are done.
-//   pass 1: exact FP64 activities of the remaining rows. g == 1 rows are
-//           summed left to right and take the reference's exact row
-//           decision; g > 1 rows are combined by a shuffle tree and use the
-//           FP32 bound rule.
-//   pass 2: (g == 1, rare) the reference's sequential EPS-max.
-//   pass 3: candidates through the warp division queue.
-__device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int lane, int round, bool marked,
-                                           int *change, unsigned *tight_ctr, WarpSmem &ws) {
-    const int lg = __ldg(P.slice_lg + slice);
-    const int g = 1 << lg;
-    const int row0 = __ldg(P.slice_row0 + slice);
-    const int nrows = __ldg(P.slice_row0 + slice + 1) - row0;
-    const int rl = lane >> lg, sub = lane & (g - 1);
-    const int r = row0 + rl;
-    bool act = rl < nrows;
-    if (act && marked) act = P.mark[r] == round;
-    if (!__any_sync(kFull, act)) return;
-    const int len = act ? __ldg(P.srow_len + r) : 0;
-    const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;  // my elements
-    const long long base = __ldg(P.slice_ptr + slice) + lane;
-    const int *col = P.sell_col + base;
-    const double *val = P.sell_val + base;
-    const bool leader = act && sub == 0;
-
-    // pass 0: FP32 screen
-    bool exact = false;
-    double lhs = 0.0, rhs = 0.0;
-    {
-        Scr c;
-        scr_init(c);
-#pragma unroll 4
-        for (int i = 0; i < cnt; i++) {
-            const int j = __ldcs(col + 32 * i);
-            const double a = __ldcs(val + 32 * i);
-            const double2 b = load_bnd(P, j);
-            scr_add(c, dbits(a), dbits(b.x), dbits(b.y));
-        }
-        if (g > 1) scr_group_reduce(c, g);
-        if (leader) {
-            lhs = __ldg(P.srow_lhs + r);
-            rhs = __ldg(P.srow_rhs + r);
-            exact = !scr_skips(c, lhs, rhs);
-        }
-        exact = __shfl_sync(kFull, exact, rl << lg) && act;
-    }
-    count_work(P, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
-    if (!__any_sync(kFull, exact)) return;
-
-    // pass 1: exact activities + FP32 enclosure, each lane in order, then the group tree
-    const int cnt1 = exact ? cnt : 0;
-    Acc s;
-    acc_init(s);
-#pragma unroll 4
-    for (int i = 0; i < cnt1; i++) {
-        const int j = __ldg(col + 32 * i);
-        const double a = __ldg(val + 32 * i);
-        const double2 b = load_bnd(P, j);
-        acc_add<true>(s, a, b.x, b.y);
-    }
-    if (g > 1) acc_group_reduce(s, g);
-    double mn = 0.0;
-    int dec = 0;
-    if (leader && exact) {
-        mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
-        if (g == 1) dec = row_decision(s.minf, s.maxf, s.U, s.L, mn);
-        else dec = u_filter_skips(s.minf, s.maxf, s.U, mn) ? 0 : 1;
-    }
-    // pass 2 (g == 1 only): the reference's sequential EPS-max, where the
-    // enclosure leaves the row test undecided
-    if (__any_sync(kFull, dec == 2)) {
-        double m = 0.0;
-        const int len2 = dec == 2 ? len : 0;
-        for (int k = 0; k < len2; k++) {
-            const int j = __ldg(col + 32 * k);
-            const double a = __ldg(val + 32 * k);
-            const double2 b = load_bnd(P, j);
-            const double d = dmul(fabs(a), dsub(b.y, b.x));
-            if (eps_gt_fast(d, m)) m = d;
-        }
-        if (dec == 2) dec = reference_row_go(s.minf, s.maxf, m, mn) ? 1 : 0;
-    }
-    // pass 3: candidates through the warp division queue
-    int tight = 0;
-    const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && exact;
-    if (__any_sync(kFull, go)) {
-        if (leader && dec == 1) ws.rc[rl] = make_rowc(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs);
-        __syncwarp();
-        WarpQueue Q{ws.q, 0};
-        const long long sbase = base - lane;
-        auto run = [&](unsigned code) {
-            const int owner = (code >> 1) & 31;
-            const int i = (int)(code >> 6);
-            const long long e = sbase + 32LL * i + owner;
-            const int j = __ldg(P.sell_col + e);
-            const double a = __ldg(P.sell_val + e);
-            tight += apply_side(P, ws.rc[owner >> lg], j, a, (int)(code & 1u)) ? 1 : 0;
-        };
-        int maxcnt = go ? cnt : 0;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) maxcnt = max(maxcnt, __shfl_xor_sync(kFull, maxcnt, off));
-        for (int i = 0; i < maxcnt; i++) {
-            int sides = 0;
-            if (go && i < cnt) {
-                const int j = __ldg(col + 32 * i);
-                const double a = __ldg(val + 32 * i);
-                const double2 b = load_bnd(P, j);
-                sides = candidate_sides(ws.rc[rl], a, b.x, b.y);
-            }
-            queue_push(Q, lane, sides, ((unsigned)i << 6) | ((unsigned)lane << 1));
-            queue_drain(Q, lane, false, run);
-        }
-        queue_drain(Q, lane, true, run);
-    }
-    report_tight(tight, lane, change, tight_ctr);
-}
-
-// ---- split rows: one warp per tile ----------------------------------------
-__device__ __forceinline__ void acc_shfl_reduce(Acc &s) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        Acc o;
-        o.minact = __shfl_down_sync(kFull, s.minact, off);
-        o.maxact = __shfl_down_sync(kFull, s.maxact, off);
-        o.minf = __shfl_down_sync(kFull, s.minf, off);
-        o.maxf = __shfl_down_sync(kFull, s.maxf, off);
-        o.U = __shfl_down_sync(kFull, s.U, off);
-        acc_combine(s, o);
-    }
-}
-
-// Decision (the FP32 bound rule) and candidates of split row `row` over the
-// element range [b, e) of one tile, from the row's complete activities held by
-// lane 0; the warp queues the divisions.
-__device__ __forceinline__ void split_row_candidates(const DevProblem &P, int row, int b, int e, const Acc &s0,
-                                                     int lane, int *change, unsigned *tight_ctr, unsigned *qbuf) {
-    RowC c;
-    int go = 0;
-    if (lane == 0) {
-        const double lhs = __ldg(P.lrow_lhs + row), rhs = __ldg(P.lrow_rhs + row);
-        const double mn = row_min_slack(s0.minact, s0.maxact, lhs, rhs);
-        go = !u_filter_skips(s0.minf, s0.maxf, s0.U, mn);
-        c = make_rowc(s0.minact, s0.maxact, s0.minf, s0.maxf, lhs, rhs);
-    }
-    go = __shfl_sync(kFull, go, 0);
-    if (!go) return;
-    c.slack = __shfl_sync(kFull, c.slack, 0);
-    c.surplus = __shfl_sync(kFull, c.surplus, 0);
-    c.neg_surplus = __shfl_sync(kFull, c.neg_surplus, 0);
-    c.minf = __shfl_sync(kFull, c.minf, 0);
-    c.maxf = __shfl_sync(kFull, c.maxf, 0);
-    c.ok = __shfl_sync(kFull, c.ok, 0);
-    c.slack_dn = __shfl_sync(kFull, c.slack_dn, 0);
-    c.slack_hi = __shfl_sync(kFull, c.slack_hi, 0);
-    c.nsur_dn = __shfl_sync(kFull, c.nsur_dn, 0);
-    c.nsur_hi = __shfl_sync(kFull, c.nsur_hi, 0);
-    int tight = 0;
-    WarpQueue Q{qbuf, 0};
-    auto run = [&](unsigned code) {
-        const int k = b + (int)(code >> 1);
-        tight += apply_side(P, c, __ldg(P.lcol + k), __ldg(P.lval + k), (int)(code & 1u)) ? 1 : 0;
-    };
-    for (int k0 = b; k0 < e; k0 += 32) {
-        const int k = k0 + lane;
-        int sides = 0;
-        if (k < e) {
-            const int j = __ldg(P.lcol + k);
-            const double a = __ldg(P.lval + k);
-            const double2 bb = load_bnd(P, j);
-            sides = candidate_sides(c, a, bb.x, bb.y);
-        }
-        queue_push(Q, lane, sides, (unsigned)(k - b) << 1);
-        queue_drain(Q, lane, false, run);
-    }
-    queue_drain(Q, lane, true, run);
-    report_tight(tight, lane, change, tight_ctr);
-}
-
-__device__ __forceinline__ void scr_shfl_reduce(Scr &c) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        Scr o;
-        o.mn_lo = __shfl_down_sync(kFull, c.mn_lo, off);
-        o.mn_hi = __shfl_down_sync(kFull, c.mn_hi, off);
-        o.mx_lo = __shfl_down_sync(kFull, c.mx_lo, off);
-        o.mx_hi = __shfl_down_sync(kFull, c.mx_hi, off);
-        o.S = __shfl_down_sync(kFull, c.S, off);
-        o.U = __shfl_down_sync(kFull, c.U, off);
-        o.minf = __shfl_down_sync(kFull, c.minf, off);
-        o.maxf = __shfl_down_sync(kFull, c.maxf, off);
-        scr_combine(c, o);
-    }
-}
-
-// Exact FP64 partial of the element range [b, e): lane l sums elements l,
-// l+32, ... in order, shuffle tree across lanes; lane 0 holds the result.
-__device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int lane) {
-    Acc s;
-    acc_init(s);
-#pragma unroll 4
-    for (int k = b + lane; k < e; k += 32) {
-        const int j = __ldg(P.lcol + k);
-        const double a = __ldg(P.lval + k);
-        const double2 bb = load_bnd(P, j);
-        acc_add<false>(s, a, bb.x, bb.y);
-    }
-    acc_shfl_reduce(s);
-    return s;
-}
-
-// Activity phase, split-row tile t: the FP32 screen of the tile. A row that
-// fits in one tile is finished here (screen decision, exact pass, candidates);
-// tiles of longer rows store their screen partial for the candidate phase.
-__device__ __forceinline__ void split_partial(const DevProblem &P, int t, int lane, int round, bool marked,
-                                              int *change, unsigned *tight_ctr, unsigned *qbuf) {
-    const int row = __ldg(P.tile_row + t);
-    if (marked && P.mark[P.n_srows + row] != round) return;
-    const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
-    Scr c;
-    scr_init(c);
-#pragma unroll 4
-    for (int k = b + lane; k < e; k += 32) {
-        const int j = __ldcs(P.lcol + k);
-        const double a = __ldcs(P.lval + k);
-        const double2 bb = load_bnd(P, j);
-        scr_add(c, dbits(a), dbits(bb.x), dbits(bb.y));
-    }
-    scr_shfl_reduce(c);
-    const int t0 = __ldg(P.lrow_tile0 + row);
-    const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
-    int exact = 0;
-    if (lane == 0) {
-        atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)(e - b));
-        if (t == t0) atomicAdd(&P.flags[0].rows_proc, 1ULL);
-        if (single) {
-            exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
-            if (exact) atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)(e - b));
-        } else {
-            TileScr ts;
-            ts.mn_lo = c.mn_lo; ts.mn_hi = c.mn_hi; ts.mx_lo = c.mx_lo; ts.mx_hi = c.mx_hi;
-            ts.S = c.S; ts.U = c.U; ts.minf = c.minf; ts.maxf = c.maxf;
-            P.tile_scr[t] = ts;
-        }
-    }
-    if (!single || !__shfl_sync(kFull, exact, 0)) return;
-    const Acc s = tile_exact(P, b, e, lane);
-    split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, qbuf);
-}
-
-// Candidate phase, tile t of a multi-tile row: the row's screen (the tile
-// partials combined by all lanes in a fixed order, so every tile of the row
-// reaches the same decision); a row the screen cannot skip gets this tile's
-// exact FP64 partial, and its first tile flags the row for the exact phase.
-__device__ __forceinline__ void split_cand(const DevProblem &P, int t, int lane, int round, bool marked,
-                                           int *exact_ctr) {
-    const int row = __ldg(P.tile_row + t);
-    if (marked && P.mark[P.n_srows + row] != round) return;
-    const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
-    Scr c;
-    scr_init(c);
-    for (int u = t0 + lane; u < t1; u += 32) {
-        const TileScr p = P.tile_scr[u];
-        Scr o;
-        o.mn_lo = p.mn_lo; o.mn_hi = p.mn_hi; o.mx_lo = p.mx_lo; o.mx_hi = p.mx_hi;
-        o.S = p.S; o.U = p.U; o.minf = p.minf; o.maxf = p.maxf;
-        scr_combine(c, o);
-    }
-    scr_shfl_reduce(c);
-    int exact = 0;
-    if (lane == 0) exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
-    if (!__shfl_sync(kFull, exact, 0)) return;
-    const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
-    const Acc s = tile_exact(P, b, e, lane);
-    if (lane == 0) {
-        TilePart tp;
-        tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf; tp.U = s.U; tp.pad = 0;
-        P.tile_part[t] = tp;
-        atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)(e - b));
-        if (t == t0) {
-            P.row_exact[row] = round;
-            atomicAdd(exact_ctr, 1);
-        }
-    }
-}
-
-// Exact phase, tile t of a multi-tile row flagged this round: the row's exact
-// partials combined in tile order, then the decision and this tile's candidates.
-__device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane, int round, int *change,
-                                            unsigned *tight_ctr, unsigned *qbuf) {
-    const int row = __ldg(P.tile_row + t);
-    if (P.row_exact[row] != round) return;
-    Acc s;
-    acc_init(s);
-    if (lane == 0) {
-        const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
-        {
-            const TilePart p = P.tile_part[t0];
-            s.minact = p.minact; s.maxact = p.maxact; s.minf = p.minf; s.maxf = p.maxf; s.U = p.U;
-        }
-        for (int u = t0 + 1; u < t1; u++) {
-            const TilePart p = P.tile_part[u];
-            Acc o;
-            o.minact = p.minact; o.maxact = p.maxact; o.minf = p.minf; o.maxf = p.maxf; o.U = p.U; o.L = 0.0f;
-            acc_combine(s, o);
-        }
-    }
-    split_row_candidates(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, qbuf);
-}
-
-// Commit changed variables nxt -> cur, apply the infeasibility rule, mark the
-// rows of changed variables for the next round, clear the bitmap.
-__device__ __forceinline__ void finalize_words(const DevProblem &P, int round, bool push_marks, int tid,
-                                               int nthreads) {
-    unsigned long long changed = 0;
-    for (int w = tid; w < P.n_chg_words; w += nthreads) {
-        unsigned bits = P.chg[w];
-        if (!bits) continue;
-        P.chg[w] = 0u;
-        changed += __popc(bits);
-        while (bits) {
-            const int j = w * 32 + __ffs(bits) - 1;
-            bits &= bits - 1;
-            const double2 b = P.bnd_nxt[j];
-            P.bnd[j] = b;
-            if (var_infeasible(b.x, b.y)) {
-                P.flags[0].infeasible = 1;
-                atomicMin(&P.flags[0].infeasible_var, j);
-            }
-            if (push_marks)
-                for (int p = __ldg(P.var_ptr + j); p < __ldg(P.var_ptr + j + 1); p++)
-                    P.mark[__ldg(P.var_pos + p)] = round + 1;
-        }
-    }
-    if (changed) atomicAdd(&P.flags[0].changed_vars, changed);
-}
-
-// ---- work distribution ----------------------------------------------------
-// Warp-level dynamic queue over items sorted heaviest first.
-__device__ __forceinline__ int warp_next(unsigned *ctr, int lane) {
-    unsigned v = 0;
-    if (lane == 0) v = atomicAdd(ctr, 1u);
-    return (int)__shfl_sync(kFull, v, 0);
-}
-
-__device__ __forceinline__ void activity_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
-                                               int *change, unsigned *tight_ctr, WarpSmem &ws, int lane) {
-    for (;;) {
-        const int i = warp_next(ctr, lane);
-        if (i >= P.n_items) break;
-        const int it = __ldg(P.items + i);
-        if (it >= 0) sell_slice(P, it, lane, round, marked, change, tight_ctr, ws);
-        else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws.q);
-    }
-}
-
-__device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
-                                                int *exact_ctr, int lane) {
-    for (;;) {
-        const int i = warp_next(ctr, lane);
-        if (i >= P.n_mtiles) break;
-        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, exact_ctr);
-    }
-}
-
-__device__ __forceinline__ void exact_phase(const DevProblem &P, int round, unsigned *ctr, int *change,
-                                            unsigned *tight_ctr, WarpSmem &ws, int lane) {
-    for (;;) {
-        const int i = warp_next(ctr, lane);
-        if (i >= P.n_mtiles) break;
-        split_exact(P, __ldg(P.mtiles + i), lane, round, change, tight_ctr, ws.q);
-    }
-}
-
-// Whether the round after one with `tight` tightenings runs on marked rows.
-__device__ __forceinline__ bool next_round_marked(const DevProblem &P, unsigned tight) {
-    return P.use_marking == 2 || (P.use_marking == 1 && tight < P.mark_threshold);
-}
 
 // ---- phase kernels (CPU_LOOP / GPU_LOOP) -----------------------------------
 __global__ void __launch_bounds__(kCtaThreads, 4) k_activity(DevProblem P) {
@@ -618,8 +18,11 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_activity(DevProblem P) {
 }
 
 __global__ void __launch_bounds__(kCtaThreads, 4) k_candidates(DevProblem P) {
+    __shared__ WarpSmem ws[kWarpsPerCta];
     const int round = P.flags[0].rounds;
     if (P.flags[0].infeasible) return;
+    if (exact_rows_queued(P, 0))
+        exact_rows_phase(P, 0, &P.flags[0].change, &P.flags[0].tight, ws[threadIdx.x >> 5], threadIdx.x & 31);
     candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].exact, threadIdx.x & 31);
 }
 
@@ -651,6 +54,8 @@ __global__ void k_round_begin(DevProblem P) {
     P.queue[0] = 0u;
     P.queue[1] = 0u;
     P.queue[2] = 0u;
+    if (P.xctr)
+        for (int i = 0; i < 16; i++) P.xctr[i] = 0u;
 }
 
 // GPU_LOOP: decides whether the graph's WHILE node runs another round.
@@ -692,49 +97,13 @@ __global__ void __launch_bounds__(256) k_mark_all(DevProblem P) {
 }
 
 // ---- megakernel -----------------------------------------------------------
-// Grid barrier with a bounded wait: thread 0 of each CTA reads the barrier
-// generation, arrives, and spins until the generation moves. Any CTA that
-// waits longer than kSpinLimitCycles (or sees another CTA's error) records
-// kErrBarrierTimeout and every CTA leaves the round loop at its next barrier.
-constexpr long long kSpinLimitCycles = 4000000000LL;  // about 2 s at 2 GHz
-
-__device__ bool grid_barrier(unsigned *bar, int *error) {
-    __syncthreads();
-    int ok = 1;
-    if (threadIdx.x == 0) {
-        volatile unsigned *vgen = bar + 1;
-        const unsigned my_gen = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
-            bar[0] = 0u;
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*vgen == my_gen) {
-                if (*((volatile int *)error) != kErrNone) { ok = 0; break; }
-                if (clock64() - t0 > kSpinLimitCycles) {
-                    atomicExch(error, (int)kErrBarrierTimeout);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        if (*((volatile int *)error) != kErrNone) ok = 0;
-    }
-    return __syncthreads_and(ok) != 0;
-}
-
 // Round loop on the device. flags[0] holds the sticky state; flags[1 + (round
 // & 1)] the per-round change flag, tightening and exact-row counts, and
-// queue[4 * (round & 1) + phase] the per-round work counters, double-buffered so that nothing a CTA may
-// still read is cleared: the next round's slots are cleared after the current
+// queue[4 * (round & 1) + phase] the per-round work counters, double-buffered
+// so that nothing a CTA may still read is cleared: the next round's slots are cleared after the current
 // round's first barrier, which every CTA passes only after finishing the
 // previous round.
-__global__ void __launch_bounds__(kCtaThreads, 4) k_megakernel(DevProblem P) {
+__global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
     __shared__ WarpSmem ws[kWarpsPerCta];
     const int lane = threadIdx.x & 31;
     WarpSmem &mine = ws[threadIdx.x >> 5];
@@ -748,7 +117,7 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_megakernel(DevProblem P) {
             unsigned *tight = &P.flags[1 + par].tight;
             int *exact = &P.flags[1 + par].exact;
             unsigned *q = P.queue + 4 * par;
-            activity_phase(P, round, marked, q + 0, change, tight, mine, lane);
+            activity_phase(P, round, marked, q + 0, change, tight, mine, lane, par);
             if (!grid_barrier(P.barrier, err)) return;
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 P.flags[1 + (par ^ 1)].change = 0;
@@ -757,11 +126,15 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_megakernel(DevProblem P) {
                 P.queue[4 * (par ^ 1) + 0] = 0u;
                 P.queue[4 * (par ^ 1) + 1] = 0u;
                 P.queue[4 * (par ^ 1) + 2] = 0u;
+                if (P.xctr)
+                    for (int i = 0; i < 16; i++) P.xctr[16 * (par ^ 1) + i] = 0u;
             }
-            if (P.n_mtiles) {
-                candidate_phase(P, round, marked, q + 1, exact, lane);
+            const bool xrows = exact_rows_queued(P, par);
+            if (xrows || P.n_mtiles) {
+                if (xrows) exact_rows_phase(P, par, change, tight, mine, lane);
+                if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, lane);
                 if (!grid_barrier(P.barrier, err)) return;
-                if (*((volatile int *)exact)) {
+                if (P.n_mtiles && *((volatile int *)exact)) {
                     exact_phase(P, round, q + 2, change, tight, mine, lane);
                     if (!grid_barrier(P.barrier, err)) return;
                 }
@@ -818,7 +191,7 @@ int launch_activity_phase(const DevProblem &P, int blocks, cudaStream_t s) {
 }
 
 int launch_candidate_phase(const DevProblem &P, int blocks, cudaStream_t s) {
-    if (P.n_mtiles == 0) return 0;
+    if (P.n_mtiles == 0 && !P.defer_exact) return 0;
     k_candidates<<<blocks, kCtaThreads, 0, s>>>(P);
     return (int)cudaGetLastError();
 }

@@ -101,6 +101,16 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     lib.gdp_propagate_noalloc.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8 + \
         [C.c_int, C.c_void_p, C.POINTER(Stats)]
     lib.gdp_propagate_noalloc.restype = C.c_int
+    _PP_INT, _PP_DBL = C.POINTER(_P_INT), C.POINTER(_P_DBL)
+    lib.gdp_batch_create.argtypes = [C.c_int, _P_INT, _P_INT, _P_INT, _PP_INT, _PP_INT, _PP_DBL, _PP_DBL,
+                                     _PP_DBL, _PP_INT, C.POINTER(Options), C.POINTER(C.c_void_p)]
+    lib.gdp_batch_create_nodes.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+    lib.gdp_batch_propagate.argtypes = [C.c_void_p, _PP_DBL, _PP_DBL, C.POINTER(Stats), C.POINTER(Stats)]
+    lib.gdp_batch_uses_graph.argtypes = [C.c_void_p]
+    lib.gdp_batch_destroy.argtypes = [C.c_void_p]
+    for name in ("gdp_batch_create", "gdp_batch_create_nodes", "gdp_batch_propagate", "gdp_batch_uses_graph",
+                 "gdp_batch_destroy"):
+        getattr(lib, name).restype = C.c_int
     for name in ("gdp_default_options", "gdp_context_create", "gdp_context_destroy", "gdp_propagate",
                  "gdp_propagate_device", "gdp_context_set_options", "gdp_context_layout",
                  "gdp_propagate_once", "propagateConstraintsGPUAtomicDouble",
@@ -247,6 +257,74 @@ class Context:
                                               C.c_void_p(stream_ptr or None), C.byref(st)),
                "gdp_propagate_device")
         return st.as_dict()
+
+
+class Batch:
+    """Many problems, or many node bound vectors of one Context's problem,
+    propagated together in one persistent launch (gdp_batch_*)."""
+
+    def __init__(self, handle, lib, sizes, keep=None):
+        self._h, self._lib, self._sizes, self._keep = handle, lib, sizes, keep
+
+    @classmethod
+    def instances(cls, mips, max_rounds: int = 0, thread_row_max: int = 0, split_tile: int = 0,
+                  use_marking: int = -1) -> "Batch":
+        lib = load_library()
+        ps = [m.normalized() for m in mips]
+        k = len(ps)
+        arr_i = lambda xs: (C.c_int * k)(*xs)
+        col = (_P_INT * k)(*[_pi(p.col) for p in ps])
+        rp = (_P_INT * k)(*[_pi(p.row_ptr) for p in ps])
+        val = (_P_DBL * k)(*[_pd(p.val) for p in ps])
+        lhs = (_P_DBL * k)(*[_pd(p.lhs) for p in ps])
+        rhs = (_P_DBL * k)(*[_pd(p.rhs) for p in ps])
+        vt = (_P_INT * k)(*[_pi(p.vartype) for p in ps])
+        o = default_options(max_rounds=max_rounds, thread_row_max=thread_row_max, split_tile=split_tile,
+                            use_marking=use_marking)
+        h = C.c_void_p()
+        rc = lib.gdp_batch_create(k, arr_i([p.m for p in ps]), arr_i([p.n for p in ps]),
+                                  arr_i([p.nnz for p in ps]), col, rp, val, lhs, rhs, vt, C.byref(o), C.byref(h))
+        _check(rc, "gdp_batch_create")
+        b = cls(h, lib, [p.n for p in ps], keep=ps)
+        b.mips = ps
+        return b
+
+    @classmethod
+    def nodes(cls, ctx: "Context", n_nodes: int) -> "Batch":
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.gdp_batch_create_nodes(ctx._h, int(n_nodes), C.byref(h)), "gdp_batch_create_nodes")
+        return cls(h, lib, [ctx.mip.n] * int(n_nodes), keep=ctx)
+
+    @property
+    def uses_graph(self) -> bool:
+        return bool(self._lib.gdp_batch_uses_graph(self._h))
+
+    def propagate(self, lbs, ubs):
+        """lbs, ubs: one array per member. Returns (lbs, ubs, member stats, total stats)."""
+        k = len(self._sizes)
+        lbo = [_f64(x).copy() for x in lbs]
+        ubo = [_f64(x).copy() for x in ubs]
+        for i in range(k):
+            if len(lbo[i]) != self._sizes[i] or len(ubo[i]) != self._sizes[i]:
+                raise GDPError(f"member {i}: expected {self._sizes[i]} bounds")
+        pl = (_P_DBL * k)(*[_pd(x) for x in lbo])
+        pu = (_P_DBL * k)(*[_pd(x) for x in ubo])
+        st = (Stats * k)()
+        tot = Stats()
+        _check(self._lib.gdp_batch_propagate(self._h, pl, pu, st, C.byref(tot)), "gdp_batch_propagate")
+        return lbo, ubo, [s.as_dict() for s in st], tot.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gdp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 NOALLOC_MAX_VARS = 1 << 20

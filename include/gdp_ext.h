@@ -99,6 +99,42 @@ GDP_RETCODE gdp_propagate_once(int n_cons, int n_vars, int nnz, const int *csr_c
                                const double *lhss, const double *rhss, double *lbs, double *ubs,
                                const int *vartypes, const gdp_options *opts, gdp_stats *stats);
 
+/* ---- batched propagation (no counterpart in the reference, which
+ * propagates one problem per call) ----------------------------------------
+ * A batch propagates many problems ("instances"), or many bound vectors of one
+ * context's problem ("nodes", e.g. branch-and-bound children), together in
+ * one persistent cooperative launch that is captured once into a CUDA graph
+ * and replayed. Every member gets the bounds, round count and infeasibility
+ * verdict that a single-problem propagation of it returns; members that
+ * converge early stop costing work. */
+typedef struct gdp_batch gdp_batch;
+
+/* Instances: per-instance host arrays with the reference's CSR meaning.
+ * opts (may be NULL) applies to every instance. */
+GDP_RETCODE gdp_batch_create(int n_inst, const int *n_cons, const int *n_vars, const int *nnz,
+                             const int *const *csr_col_indices, const int *const *csr_row_ptrs,
+                             const double *const *csr_vals, const double *const *lhss,
+                             const double *const *rhss, const int *const *vartypes,
+                             const gdp_options *opts, gdp_batch **out);
+
+/* Nodes of ctx's problem (ctx must outlive the batch). When ctx's last
+ * propagation converged feasibly, round 1 of every node processes only the
+ * rows of the variables whose bounds differ from that fixpoint (the other rows
+ * are at their fixpoint already); otherwise round 1 processes every row. */
+GDP_RETCODE gdp_batch_create_nodes(gdp_context *ctx, int n_nodes, gdp_batch **out);
+
+/* lbs[k], ubs[k]: member k's bounds (host, in/out, n_vars of member k).
+ * member_stats: one entry per member, or NULL; total: batch sums (rounds = the
+ * largest member round count, device_ms = the whole launch), or NULL. */
+GDP_RETCODE gdp_batch_propagate(gdp_batch *b, double *const *lbs, double *const *ubs,
+                                gdp_stats *member_stats, gdp_stats *total);
+
+/* 1 if the batch runs as a captured CUDA graph (known after the first
+ * propagation), 0 if it launches the same sequence directly. */
+int gdp_batch_uses_graph(const gdp_batch *b);
+
+GDP_RETCODE gdp_batch_destroy(gdp_batch *b);
+
 /* Propagation that allocates no memory, for callers that cannot call
  * cudaMalloc (e.g. a solver or framework whose device memory belongs to its
  * own pool and that propagates many nodes in a loop, where cudaMalloc/cudaFree
