@@ -56,10 +56,15 @@ def parse():
     ap.add_argument("--marking", type=int, default=1, help="1: process only rows with a changed variable")
     ap.add_argument("--trm", type=int, default=0, help="thread_row_max (0: library default)")
     ap.add_argument("--tile", type=int, default=0, help="split_tile (0: library default)")
-    ap.add_argument("--workload", choices=["plain", "nodes", "instances", "chains"], default="plain",
+    ap.add_argument("--workload", choices=["plain", "nodes", "instances", "chains", "cover"], default="plain",
                     help="plain: the power-law MIP (the bench line); nodes / instances / chains: batched "
                          "workloads timed against per-member plain propagations")
     ap.add_argument("--members", type=int, default=0, help="batch members (0: the workload's default)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="plain: pick row bins and loop schedule with gdp_autotune first (untimed)")
+    ap.add_argument("--train-seeds", type=int, default=200, help="cover: instances traced for training")
+    ap.add_argument("--eval-seeds", type=int, default=50, help="cover: held-out instances evaluated")
+    ap.add_argument("--train-scale", type=float, default=0.1, help="cover: size of the traced instances")
     return ap.parse_args()
 
 
@@ -334,11 +339,93 @@ def run_batched(args, ws, rank, local):
     return 0
 
 
+COVER = ("set-covering/knapsack MIPs: 500,000 covering rows (0/1 coefficients, length U{5..60}, rhs>=1) + "
+         "50,000 knapsack rows (int coefficients U{1..1000}, capacity 0.3 row sum) over 400,000 binary and "
+         "50,000 continuous vars")
+
+
+def run_cover(args, ws, rank, local):
+    """Learned marking on covering/knapsack MIPs: the MLP is trained on the GPU
+    on traces of `train_seeds` instances and evaluated on `eval_seeds` held-out
+    seeds against plain full-sweep propagation (the reference's schedule) and
+    exact marking (the engine without the model)."""
+    import torch
+
+    import gdp
+    import gdpgen
+    import marking
+    torch.cuda.set_device(local)
+    sc = args.scale
+    t0 = time.perf_counter()
+    ts = args.train_scale
+    train = (gdpgen.cover_knapsack(int(500_000 * ts), int(50_000 * ts), int(400_000 * ts), int(50_000 * ts),
+                                   seed=10_000 + i) for i in range(args.train_seeds))
+    x, y = marking.collect_traces(train, capacity=50_000)
+    trace_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    model, tau, info = marking.train_marking_model(x, y, epochs=4, batch=8192, seed=1, recall=0.98)
+    train_s = time.perf_counter() - t0
+    plain_ms = exact_ms = learned_ms = 0.0
+    agree = 0
+    rows = {"plain": 0, "exact": 0, "learned": 0}
+    nnz = {"plain": 0, "exact": 0, "learned": 0}
+    rounds = {"plain": [], "exact": [], "learned": []}
+    e2e = []
+    clocks = Clocks(local)
+    clocks.start()
+    for i in range(args.eval_seeds):
+        mip = gdpgen.cover_knapsack(int(500_000 * sc), int(50_000 * sc), int(400_000 * sc), int(50_000 * sc),
+                                    seed=20_000 + i)
+        res = {}
+        for name, marking_mode, use_model in (("plain", 0, False), ("exact", 1, False), ("learned", 1, True)):
+            with gdp.Context(mip, sync_type=gdp.MEGAKERNEL, use_marking=marking_mode) as ctx:
+                if use_model:
+                    ctx.set_model(model, tau)
+                for _ in range(args.warmup if i == 0 else 0):
+                    ctx.propagate()
+                t1 = time.perf_counter()
+                lb, ub, st = ctx.propagate()
+                if name == "learned":
+                    e2e.append((time.perf_counter() - t1) * 1e3)
+            res[name] = (lb, ub, st)
+            rows[name] += st["rows_processed"]
+            nnz[name] += st["nnz_processed"]
+            rounds[name].append(st["rounds"])
+        plain_ms += res["plain"][2]["device_ms"]
+        exact_ms += res["exact"][2]["device_ms"]
+        learned_ms += res["learned"][2]["device_ms"]
+        agree += int(np.array_equal(res["learned"][0], res["plain"][0]) and
+                     np.array_equal(res["learned"][1], res["plain"][1]))
+    clk = clocks.stop()
+    line = {"metric": "ms-to-fixpoint", "value": learned_ms, "unit": "ms", "n_gpus": ws, "steps": args.eval_seeds,
+            "warmup": args.warmup, "ms_per_step": learned_ms / max(1, args.eval_seeds), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": COVER, "scale": sc, "train_seeds": args.train_seeds,
+                       "train_scale": args.train_scale, "eval_seeds": args.eval_seeds,
+                       "train_samples": info["samples"], "positive_rate": info["positive_rate"],
+                       "train_loss": info["loss"], "threshold": tau, "train_recall": info["recall"],
+                       "selected_rate": info["selected_rate"], "trace_s": trace_s, "train_s": train_s,
+                       "rows_processed": rows, "nnz_processed": nnz,
+                       "rounds_mean": {k: float(np.mean(v)) for k, v in rounds.items()},
+                       "parallelism": "single"},
+            "plain": {"full_sweep_ms": plain_ms, "exact_marking_ms": exact_ms,
+                      "speedup_vs_full_sweep": plain_ms / max(learned_ms, 1e-9),
+                      "speedup_vs_exact_marking": exact_ms / max(learned_ms, 1e-9),
+                      "bitexact_with_full_sweep": f"{agree}/{args.eval_seeds}"},
+            "e2e": {"value": float(np.sum(e2e)), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 2 * args.eval_seeds, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.workload == "cover":
+        return run_cover(args, ws, rank, local)
     if args.workload != "plain":
         return run_batched(args, ws, rank, local)
 
@@ -348,9 +435,17 @@ def main():
     torch.cuda.set_device(local)
     sync = {"megakernel": gdp.MEGAKERNEL, "cpu_loop": gdp.CPU_LOOP, "gpu_loop": gdp.GPU_LOOP}[args.sync]
     mip, gen_s = make_instance(args, rank)
+    tuned = None
+    if args.autotune:
+        t0 = time.perf_counter()
+        opts, tms, trials = gdp.autotune(mip, repeats=1, max_rounds=args.max_rounds, use_marking=args.marking)
+        tuned = {"options": opts, "ms": tms, "seconds": time.perf_counter() - t0, "trials": len(trials)}
+        sync, args.trm, args.tile = opts["sync_type"], opts["thread_row_max"], opts["split_tile"]
+        args.sync = {gdp.MEGAKERNEL: "megakernel", gdp.GPU_LOOP: "gpu_loop", gdp.CPU_LOOP: "cpu_loop"}[sync]
     t0 = time.perf_counter()
     ctx = gdp.Context(mip, sync_type=sync, max_rounds=args.max_rounds, thread_row_max=args.trm,
-                      split_tile=args.tile, use_marking=args.marking)
+                      split_tile=args.tile, use_marking=args.marking,
+                      ctas_per_sm=tuned["options"]["ctas_per_sm"] if tuned else 0)
     ctx_s = time.perf_counter() - t0
     layout = ctx.layout()
     stream = torch.cuda.current_stream()
@@ -434,6 +529,8 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk,
             "setup_s": {"generate": gen_s, "context": ctx_s}}
+    if tuned:
+        line["config"]["autotune"] = tuned
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(mip, rounds, args.cpu_budget_s, args.max_rounds)
     if rank == 0:

@@ -8,6 +8,7 @@
 
 #include "gdp_batch.h"
 #include "gdp_context.h"
+#include "gdp_mlp.h"
 #include "interface.h"
 
 using gdp::Context;
@@ -152,6 +153,36 @@ GDP_RETCODE gdp_batch_destroy(gdp_batch *b) {
     return guarded([&]() -> GDP_RETCODE {
         delete b;
         return GDP_OKAY;
+    });
+}
+
+GDP_RETCODE gdp_context_set_model(gdp_context *ctx, const gdp_mlp *model, float threshold, int min_len) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!ctx) { gdp::set_error("null context"); return GDP_ERROR; }
+        return ctx->impl.set_model(model ? &model->impl : nullptr, threshold, min_len);
+    });
+}
+
+GDP_RETCODE gdp_context_trace(gdp_context *ctx, double *lbs, double *ubs, int capacity, float *features,
+                              float *labels, int *n_samples, gdp_stats *stats) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!ctx || !lbs || !ubs) { gdp::set_error("null context or bounds"); return GDP_ERROR; }
+        const auto t0 = std::chrono::steady_clock::now();
+        const GDP_RETCODE rc = ctx->impl.trace(lbs, ubs, capacity, features, labels, n_samples, stats);
+        if (stats)
+            stats->total_ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    });
+}
+
+GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *col, const int *row_ptr, const double *val,
+                         const double *lhs, const double *rhs, const double *lbs, const double *ubs,
+                         const int *vartypes, const gdp_options *base, int repeats, gdp_options *best,
+                         double *best_ms, gdp_tune_trial *trials, int max_trials, int *n_trials) {
+    return guarded([&]() -> GDP_RETCODE {
+        return gdp::autotune(n_cons, n_vars, nnz, col, row_ptr, val, lhs, rhs, lbs, ubs, vartypes, base, repeats,
+                             best, best_ms, trials, max_trials, n_trials);
     });
 }
 

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "gdp_context.h"
+#include "gdp_learned.h"
 
 namespace gdp {
 
@@ -325,6 +326,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     }
     int act_bps = 0, cand_bps = 0, mega_bps = 0;
     GDP_CUDA(phase_occupancy(&act_bps, &cand_bps, &mega_bps));
+    if (opts.ctas_per_sm > 0) {
+        act_bps = std::min(act_bps, opts.ctas_per_sm);
+        cand_bps = std::min(cand_bps, opts.ctas_per_sm);
+        mega_bps = std::min(mega_bps, opts.ctas_per_sm);
+    }
     act_blocks = std::max(1, std::min(act_bps * n_sms, (P.n_items + kWarpsPerCta - 1) / kWarpsPerCta));
     cand_blocks = std::max(1, cand_bps * n_sms);  // the exact-rows phase shares this launch
     mega_grid = std::max(1, mega_bps) * n_sms;
@@ -449,7 +455,8 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
     int launches = 3;
     GDP_CUDA(cudaEventRecord(ev0, s));
     GDP_RETCODE rc;
-    if (opts.sync_type == MEGAKERNEL) rc = rounds_megakernel(s, &launches);
+    if (P.learned) rc = rounds_learned(s, &launches);
+    else if (opts.sync_type == MEGAKERNEL) rc = rounds_megakernel(s, &launches);
     else if (opts.sync_type == GPU_LOOP) rc = rounds_gpu_loop(s, &launches);
     else rc = rounds_cpu_loop(s, &launches);
     if (rc != GDP_OKAY) return rc;
@@ -481,10 +488,96 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         st->rows_processed = (long long)f.rows_proc;
         st->nnz_processed = (long long)f.nnz_proc;
         st->nnz_exact = (long long)f.nnz_exact;
+        st->rows_deferred = (long long)f.rows_deferred;
+        st->full_rounds = f.full_rounds;
         st->bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc + 36.0 * n * (double)f.rounds;
         st->device_ms = ms;
     }
     return GDP_OKAY;
+}
+
+// Learned marking: every round in one launch of the learned round loop.
+GDP_RETCODE Context::rounds_learned(cudaStream_t s, int *launches) {
+    DevProblem Q = P;
+    Q.defer_exact = 0;  // labels and row state need each row's outcome in its own warp
+    GDP_CUDA((cudaError_t)launch_learned(Q, learned_grid, vec_blocks, s));
+    *launches += 2;
+    GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
+    GDP_CUDA(cudaStreamSynchronize(s));
+    return GDP_OKAY;
+}
+
+GDP_RETCODE Context::alloc_learned_state() {
+    if (P.dirty) return GDP_OKAY;
+    const size_t ns = (size_t)std::max(P.n_srows, 1);
+    P.dirty = (int *)arena.alloc_bytes(sizeof(int) * ns);
+    P.dcount = (int *)arena.alloc_bytes(sizeof(int) * ns);
+    P.last_proc = (int *)arena.alloc_bytes(sizeof(int) * ns);
+    P.last_tight = (int *)arena.alloc_bytes(sizeof(int) * ns);
+    P.rstat = (float2 *)arena.alloc_bytes(sizeof(float2) * ns);
+    P.rinfo = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * ns);
+    P.trace_n = (unsigned *)arena.alloc_bytes(sizeof(unsigned));
+    if (!P.dirty || !P.dcount || !P.last_proc || !P.last_tight || !P.rstat || !P.rinfo || !P.trace_n) {
+        set_error("device allocation failed (learned marking state)");
+        return GDP_ERROR;
+    }
+    int bps = 0;
+    GDP_CUDA((cudaError_t)learned_occupancy(&bps));
+    learned_grid = std::max(1, bps) * n_sms;
+    return GDP_OKAY;
+}
+
+GDP_RETCODE Context::set_model(const Mlp *m, float threshold, int min_len) {
+    if (!m) {
+        P.learned = 0;
+        return GDP_OKAY;
+    }
+    if (alloc_learned_state() != GDP_OKAY) return GDP_ERROR;
+    P.mlp = m->dev();
+    P.tau = threshold;
+    P.learn_min_len = std::max(0, min_len);
+    P.learned = 1;
+    return GDP_OKAY;
+}
+
+GDP_RETCODE Context::trace(double *lbs, double *ubs, int capacity, float *x_out, float *y_out, int *n_out,
+                           gdp_stats *st) {
+    if (capacity < 0 || (capacity > 0 && (!x_out || !y_out)) || !n_out) {
+        set_error("bad trace arguments");
+        return GDP_ERROR;
+    }
+    if (alloc_learned_state() != GDP_OKAY) return GDP_ERROR;
+    const size_t cap = (size_t)std::max(capacity, 1);
+    float *dx = nullptr, *dy = nullptr;
+    GDP_CUDA(cudaMalloc(&dx, sizeof(float) * 16 * cap));
+    GDP_CUDA(cudaMalloc(&dy, sizeof(float) * cap));
+    const int saved = P.learned;
+    P.learned = 2;
+    P.trace_x = dx;
+    P.trace_y = dy;
+    P.trace_cap = (unsigned)capacity;
+    GDP_RETCODE rc = GDP_OKAY;
+    if (cudaMemsetAsync(P.trace_n, 0, sizeof(unsigned), stream) != cudaSuccess) rc = GDP_ERROR;
+    if (rc == GDP_OKAY) rc = propagate_host(lbs, ubs, st);
+    P.learned = saved;
+    P.trace_x = nullptr;
+    P.trace_y = nullptr;
+    P.trace_cap = 0;
+    unsigned cnt = 0;
+    if (rc == GDP_OKAY) {
+        if (cudaMemcpy(&cnt, P.trace_n, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) rc = GDP_ERROR;
+        const unsigned keep = std::min(cnt, (unsigned)capacity);
+        if (rc == GDP_OKAY && keep) {
+            if (cudaMemcpy(x_out, dx, sizeof(float) * 16 * keep, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                cudaMemcpy(y_out, dy, sizeof(float) * keep, cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = GDP_ERROR;
+        }
+        *n_out = (int)keep;
+        if (rc != GDP_OKAY) set_error("trace download failed");
+    }
+    cudaFree(dx);
+    cudaFree(dy);
+    return rc;
 }
 
 GDP_RETCODE Context::propagate_host(double *lbs, double *ubs, gdp_stats *st) {

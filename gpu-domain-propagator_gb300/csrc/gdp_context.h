@@ -8,6 +8,7 @@
 
 #include "gdp_ext.h"
 #include "gdp_internal.h"
+#include "gdp_mlp.h"
 
 namespace gdp {
 
@@ -21,6 +22,11 @@ struct Arena {
     void *alloc_bytes(size_t bytes);
 };
 
+GDP_RETCODE autotune(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
+                     const double *lhs, const double *rhs, const double *lbs, const double *ubs,
+                     const int *vartype, const gdp_options *base, int repeats, gdp_options *best,
+                     double *best_ms, gdp_tune_trial *trials, int max_trials, int *n_trials);
+
 GDP_RETCODE validate_csr(int m, int n, int nnz, const int *col, const int *row_ptr,
                          const double *val, const int *vartype);
 
@@ -31,6 +37,12 @@ public:
                      const double *lhs, const double *rhs, const int *vartype, const gdp_options *o);
     GDP_RETCODE propagate_host(double *lbs, double *ubs, gdp_stats *st);
     GDP_RETCODE propagate_device(double *d_lbs, double *d_ubs, cudaStream_t s, gdp_stats *st);
+    // Learned marking with model m (NULL: off), logit threshold and the
+    // shortest row length the model decides for.
+    GDP_RETCODE set_model(const Mlp *m, float threshold, int min_len);
+    // Trace propagation: exact marking, logging up to `capacity` samples.
+    GDP_RETCODE trace(double *lbs, double *ubs, int capacity, float *x_out, float *y_out, int *n_out,
+                      gdp_stats *st);
 
     int m = 0, n = 0, nnz = 0;
     gdp_options opts{};
@@ -40,7 +52,7 @@ public:
     Arena arena;
     DevProblem P{};
     double *d_lb = nullptr, *d_ub = nullptr;  // staging for host bounds
-    int n_sms = 0, vec_blocks = 1, act_blocks = 1, cand_blocks = 1, mega_grid = 1;
+    int n_sms = 0, vec_blocks = 1, act_blocks = 1, cand_blocks = 1, mega_grid = 1, learned_grid = 1;
     int n_srows = 0, n_slices = 0, n_lrows = 0, n_tiles = 0;
     long long sell_elems = 0;
     // the last propagation converged feasibly: P.bnd is a fixpoint of the problem
@@ -56,6 +68,8 @@ private:
     GDP_RETCODE rounds_cpu_loop(cudaStream_t s, int *launches);
     GDP_RETCODE rounds_gpu_loop(cudaStream_t s, int *launches);
     GDP_RETCODE rounds_megakernel(cudaStream_t s, int *launches);
+    GDP_RETCODE rounds_learned(cudaStream_t s, int *launches);
+    GDP_RETCODE alloc_learned_state();
 };
 
 }  // namespace gdp

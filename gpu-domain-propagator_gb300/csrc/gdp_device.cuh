@@ -378,8 +378,7 @@ constexpr float kInfF32Dn = 0x1.5af1d6p+66f;
 // additions is below n 2^-53 S), and FP64 rounding of rhs - minact and
 // maxact - lhs is monotone, so min(rhs - minact, maxact - lhs) >= the
 // directed-rounded lower end computed here.
-__device__ __forceinline__ bool scr_skips(const Scr &c, double lhs, double rhs) {
-    if (c.minf > 1 && c.maxf > 1) return true;
+__device__ __forceinline__ void scr_slack(const Scr &c, double lhs, double rhs, float &mn_lo, float &mn_hi) {
     const float E = __fmul_ru(c.S, 9.5367431640625e-7f);
     const MagEnc R = mag_enc(dbits(rhs)), Lh = mag_enc(dbits(lhs));
     const bool rsg = dbits(rhs) < 0, lsg = dbits(lhs) < 0;
@@ -389,7 +388,13 @@ __device__ __forceinline__ bool scr_skips(const Scr &c, double lhs, double rhs) 
     const float s_hi = __fsub_ru(rhs_up, __fsub_rd(c.mn_lo, E));
     const float t_lo = __fsub_rd(__fsub_rd(c.mx_lo, E), lhs_up);
     const float t_hi = __fsub_ru(__fadd_ru(c.mx_hi, E), lhs_dn);
-    const float mn_lo = fminf(s_lo, t_lo), mn_hi = fminf(s_hi, t_hi);
+    mn_lo = fminf(s_lo, t_lo);
+    mn_hi = fminf(s_hi, t_hi);
+}
+__device__ __forceinline__ bool scr_skips(const Scr &c, double lhs, double rhs) {
+    if (c.minf > 1 && c.maxf > 1) return true;
+    float mn_lo, mn_hi;
+    scr_slack(c, lhs, rhs, mn_lo, mn_hi);
     return mn_hi < kInfF32Dn && __fmul_rn(c.U, kUMargin) <= mn_lo;
 }
 

@@ -20,6 +20,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "gdp_mlp.cuh"
+
 namespace gdp {
 
 // Partial activities of a split-row tile (and of a whole split row).
@@ -49,11 +51,12 @@ struct RoundFlags {
     int mark_cur;        // this round processes only marked rows (else every row)
     unsigned tight;      // tightenings found in this round (decides the next round's mode)
     int exact;           // multi-tile rows of this round that need the exact pass
-    int pad;
+    int full_rounds;     // learned marking: rounds that swept every row
     unsigned long long changed_vars;  // committed variable changes, all rounds
     unsigned long long rows_proc;     // rows processed (screened), all rounds
     unsigned long long nnz_proc;      // their non-zeros
     unsigned long long nnz_exact;     // non-zeros that also went through the exact FP64 pass
+    unsigned long long rows_deferred; // learned marking: marked rows the model left for a later round
 };
 
 enum DeviceError : int {
@@ -107,6 +110,21 @@ struct DevProblem {
     int cls_begin[6], cls_end[6];
     int *xrow;             // n_srows
     unsigned *xctr;        // [parity * 16 + lg]: queue tails, [parity * 16 + 8 + lg]: pull counters
+    // learned marking (SELL rows; null when no model is attached). learned:
+    // 1 = rounds process the marked rows the model selects, 2 = trace (every
+    // marked row is processed and logged with its label).
+    int learned;
+    float tau;             // logit threshold of the selection
+    int learn_min_len;     // marked rows shorter than this are always processed
+    MlpDev mlp;
+    int *dirty;            // round since which the row has a changed variable (0: clean)
+    int *dcount;           // variable changes in the row since it was last processed
+    int *last_proc, *last_tight;  // last round the row was processed / tightened a bound
+    float2 *rstat;         // last screen: normalised slack, log-ratio of U to the slack
+    unsigned *rinfo;       // last screen: minf (2 bits), maxf (2 bits), exact (bit 4), go (bit 5), streak (bits 8..15)
+    float *trace_x, *trace_y;  // trace: features (16 per sample) and labels
+    unsigned *trace_n;
+    unsigned trace_cap;
     int *mark;             // round in which the position is processed next (0: none)
     // batched engine only (null otherwise): slice of each SELL row position and
     // the round in which each slice was last queued

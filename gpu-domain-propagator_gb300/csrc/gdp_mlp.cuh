@@ -114,6 +114,53 @@ __device__ __forceinline__ void mlp_forward_tile(const MlpDev &M, const unsigned
     T.z[1] = z1 + b3;
 }
 
+// Inference-only forward of a 16-row tile: the same arithmetic as
+// mlp_forward_tile, evaluated n-tile by n-tile so that only the layer-1
+// activations (16 registers) stay live. z0, z1: logits of rows g and g + 8.
+__device__ __forceinline__ void mlp_infer_tile(const MlpDev &M, const unsigned (&x)[4], int lane, float &z0,
+                                               float &z1) {
+    const int t = lane & 3;
+    unsigned h[4][4];
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            const int nt = 2 * kt + half;
+            const float bl = __ldg(M.b1 + nt * 8 + 2 * t), bh = __ldg(M.b1 + nt * 8 + 2 * t + 1);
+            float c[4] = {bl, bh, bl, bh};
+            unsigned b0, b1;
+            load_b(M.w1, kMlpIn, nt * 8, 0, lane, b0, b1);
+            mma_bf16(c, x, b0, b1);
+            h[kt][2 * half] = pack_bf16(fmaxf(c[0], 0.f), fmaxf(c[1], 0.f));
+            h[kt][2 * half + 1] = pack_bf16(fmaxf(c[2], 0.f), fmaxf(c[3], 0.f));
+        }
+    }
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+        const float bl = __ldg(M.b2 + nt * 8 + 2 * t), bh = __ldg(M.b2 + nt * 8 + 2 * t + 1);
+        float c[4] = {bl, bh, bl, bh};
+#pragma unroll
+        for (int kt = 0; kt < 4; kt++) {
+            unsigned b0, b1;
+            load_b(M.w2, kMlpH, nt * 8, kt * 16, lane, b0, b1);
+            mma_bf16(c, h[kt], b0, b1);
+        }
+        const float wl = __bfloat162float(M.w3[nt * 8 + 2 * t]), wh = __bfloat162float(M.w3[nt * 8 + 2 * t + 1]);
+        s0 = fmaf(fmaxf(c[0], 0.f), wl, s0);
+        s0 = fmaf(fmaxf(c[1], 0.f), wh, s0);
+        s1 = fmaf(fmaxf(c[2], 0.f), wl, s1);
+        s1 = fmaf(fmaxf(c[3], 0.f), wh, s1);
+    }
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+    const float b3 = __ldg(M.b3);
+    z0 = s0 + b3;
+    z1 = s1 + b3;
+}
+
 // A registers of a 16 x 16 BF16 tile stored row-major in shared memory.
 __device__ __forceinline__ void load_a_smem(const __nv_bfloat16 *X, int lane, unsigned (&a)[4]) {
     const int g = lane >> 2, t = lane & 3;

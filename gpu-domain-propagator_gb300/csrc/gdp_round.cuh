@@ -186,6 +186,14 @@ struct WarpSmem {
     long long base[32];  // deferred exact pass: first element of each lane
 };
 
+// Learned marking: features, scores and per-row outcomes of one slice.
+struct LearnSmem {
+    __nv_bfloat16 feat[32][16];
+    float z[32];
+    int tight[32];
+    int go[32];
+};
+
 // Combines the partial accumulators of a group of g lanes (g a power of two,
 // warp-uniform) into its first lane: shuffle tree with offsets g/2, ..., 1.
 __device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
@@ -242,7 +250,8 @@ __device__ __forceinline__ void count_work(const DevProblem &P, int lane, int ro
 //   pass 3: candidates through the warp division queue.
 __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int lane, bool exact, int len,
                                                 int cnt, double lhs, double rhs, int *change,
-                                                unsigned *tight_ctr, WarpSmem &ws) {
+                                                unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
+                                                int *row_go = nullptr) {
     const int g = 1 << lg;
     const int rl = lane >> lg, sub = lane & (g - 1);
     const bool leader = exact && sub == 0;
@@ -281,6 +290,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
     }
     int tight = 0;
     const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && exact;
+    if (row_go && leader) row_go[rl] = go ? 1 : 0;
     if (__any_sync(kFull, go)) {
         if (leader && dec == 1) ws.rc[rl] = make_rowc(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs);
         __syncwarp();
@@ -291,7 +301,10 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
             const long long e = ws.base[owner] + 32LL * i;
             const int j = __ldg(P.sell_col + e);
             const double a = __ldg(P.sell_val + e);
-            tight += apply_side(P, ws.rc[owner >> lg], j, a, (int)(code & 1u)) ? 1 : 0;
+            if (apply_side(P, ws.rc[owner >> lg], j, a, (int)(code & 1u))) {
+                tight++;
+                if (row_tight) atomicAdd(row_tight + (owner >> lg), 1);
+            }
         };
         int maxcnt = go ? cnt : 0;
 #pragma unroll

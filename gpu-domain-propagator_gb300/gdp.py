@@ -36,6 +36,11 @@ class GDPError(RuntimeError):
     pass
 
 
+class TuneTrial(C.Structure):
+    _fields_ = [("thread_row_max", C.c_int), ("split_tile", C.c_int), ("sync_type", C.c_int),
+                ("ctas_per_sm", C.c_int), ("rounds", C.c_int), ("pad_", C.c_int), ("ms", C.c_double)]
+
+
 class Options(C.Structure):
     _fields_ = [
         ("max_rounds", C.c_int),
@@ -44,7 +49,8 @@ class Options(C.Structure):
         ("split_tile", C.c_int),
         ("device", C.c_int),
         ("use_marking", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("ctas_per_sm", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 
@@ -63,6 +69,9 @@ class Stats(C.Structure):
         ("device_ms", C.c_double),
         ("total_ms", C.c_double),
         ("nnz_exact", C.c_longlong),
+        ("rows_deferred", C.c_longlong),
+        ("full_rounds", C.c_int),
+        ("pad_", C.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -110,6 +119,26 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     lib.gdp_batch_destroy.argtypes = [C.c_void_p]
     for name in ("gdp_batch_create", "gdp_batch_create_nodes", "gdp_batch_propagate", "gdp_batch_uses_graph",
                  "gdp_batch_destroy"):
+        getattr(lib, name).restype = C.c_int
+    _P_F = C.POINTER(C.c_float)
+    lib.gdp_mlp_create.argtypes = [C.c_ulonglong, C.c_int, C.POINTER(C.c_void_p)]
+    lib.gdp_mlp_destroy.argtypes = [C.c_void_p]
+    lib.gdp_mlp_get_params.argtypes = [C.c_void_p, _P_F]
+    lib.gdp_mlp_set_params.argtypes = [C.c_void_p, _P_F]
+    lib.gdp_mlp_forward.argtypes = [C.c_void_p, C.c_int, _P_F, _P_F]
+    lib.gdp_mlp_gradient.argtypes = [C.c_void_p, C.c_int, _P_F, _P_F, _P_F, _P_F, _P_F]
+    lib.gdp_mlp_train.argtypes = [C.c_void_p, C.c_int, _P_F, _P_F, _P_F, C.c_int, C.c_int, C.c_float,
+                                  C.c_ulonglong, _P_F]
+    lib.gdp_context_set_model.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_int]
+    lib.gdp_autotune.argtypes = _LEGACY_ARGS[:8] + [_P_DBL, _P_DBL, _P_INT, C.POINTER(Options), C.c_int,
+                                                    C.POINTER(Options), C.POINTER(C.c_double),
+                                                    C.POINTER(TuneTrial), C.c_int, C.POINTER(C.c_int)]
+    lib.gdp_autotune.restype = C.c_int
+    lib.gdp_context_trace.argtypes = [C.c_void_p, _P_DBL, _P_DBL, C.c_int, _P_F, _P_F, C.POINTER(C.c_int),
+                                      C.POINTER(Stats)]
+    for name in ("gdp_mlp_create", "gdp_mlp_destroy", "gdp_mlp_get_params", "gdp_mlp_set_params",
+                 "gdp_mlp_forward", "gdp_mlp_gradient", "gdp_mlp_train", "gdp_context_set_model",
+                 "gdp_context_trace"):
         getattr(lib, name).restype = C.c_int
     for name in ("gdp_default_options", "gdp_context_create", "gdp_context_destroy", "gdp_propagate",
                  "gdp_propagate_device", "gdp_context_set_options", "gdp_context_layout",
@@ -204,12 +233,12 @@ class Context:
     """Persistent device context: upload once, propagate many bound vectors."""
 
     def __init__(self, mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
-                 split_tile: int = 0, use_marking: int = -1):
+                 split_tile: int = 0, use_marking: int = -1, ctas_per_sm: int = 0):
         self._lib = load_library()
         self.mip = mip.normalized()
         p = self.mip
         o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
-                            split_tile=split_tile, use_marking=use_marking)
+                            split_tile=split_tile, use_marking=use_marking, ctas_per_sm=ctas_per_sm)
         h = C.c_void_p()
         rc = self._lib.gdp_context_create(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val),
                                           _pd(p.lhs), _pd(p.rhs), _pi(p.vartype), C.byref(o), C.byref(h))
@@ -250,6 +279,27 @@ class Context:
         _check(self._lib.gdp_propagate(self._h, _pd(lbo), _pd(ubo), C.byref(st)), "gdp_propagate")
         return lbo, ubo, st.as_dict()
 
+    def set_model(self, model, threshold: float = 0.0, min_len: int = 8) -> None:
+        """Learned marking with `model` (an Mlp; None turns it off), a logit
+        threshold, and the shortest row length the model decides for."""
+        self._model = model
+        _check(self._lib.gdp_context_set_model(self._h, model._h if model is not None else None,
+                                               float(threshold), int(min_len)), "gdp_context_set_model")
+
+    def trace(self, lb=None, ub=None, capacity: int = 1 << 20):
+        """Trace propagation: returns (features [k, 16], labels [k], lb, ub, stats)."""
+        lbo = _f64(self.mip.lb if lb is None else lb).copy()
+        ubo = _f64(self.mip.ub if ub is None else ub).copy()
+        x = np.zeros((max(capacity, 1), 16), np.float32)
+        y = np.zeros(max(capacity, 1), np.float32)
+        k = C.c_int()
+        st = Stats()
+        _check(self._lib.gdp_context_trace(self._h, _pd(lbo), _pd(ubo), int(capacity),
+                                           x.ctypes.data_as(C.POINTER(C.c_float)),
+                                           y.ctypes.data_as(C.POINTER(C.c_float)), C.byref(k), C.byref(st)),
+               "gdp_context_trace")
+        return x[:k.value].copy(), y[:k.value].copy(), lbo, ubo, st.as_dict()
+
     def propagate_device(self, d_lb_ptr: int, d_ub_ptr: int, stream_ptr: int = 0) -> dict:
         """Propagates device-resident bounds (raw device pointers, e.g. torch data_ptr())."""
         st = Stats()
@@ -257,6 +307,27 @@ class Context:
                                               C.c_void_p(stream_ptr or None), C.byref(st)),
                "gdp_propagate_device")
         return st.as_dict()
+
+
+def autotune(mip: MIP, repeats: int = 2, max_rounds: int = 0, use_marking: int = -1):
+    """gdp_autotune: the fastest (thread_row_max, split_tile, sync_type,
+    ctas_per_sm) for `mip`. Returns (options dict, best ms, list of trials)."""
+    lib = load_library()
+    p = mip.normalized()
+    base = default_options(max_rounds=max_rounds, use_marking=use_marking)
+    best = Options()
+    ms = C.c_double()
+    trials = (TuneTrial * 64)()
+    k = C.c_int()
+    rc = lib.gdp_autotune(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val), _pd(p.lhs), _pd(p.rhs),
+                          _pd(p.lb), _pd(p.ub), _pi(p.vartype), C.byref(base), int(repeats), C.byref(best),
+                          C.byref(ms), trials, 64, C.byref(k))
+    _check(rc, "gdp_autotune")
+    opts = {name: getattr(best, name) for name in ("thread_row_max", "split_tile", "sync_type", "ctas_per_sm",
+                                                   "use_marking", "max_rounds")}
+    table = [{name: getattr(trials[i], name) for name, _ in TuneTrial._fields_ if name != "pad_"}
+             for i in range(k.value)]
+    return opts, ms.value, table
 
 
 class Batch:
@@ -318,6 +389,77 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.gdp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+MLP_FEATURES = 16
+MLP_PARAMS = 5313
+
+
+def _pf(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Mlp:
+    """The row-marking MLP (gdp_mlp_*): 16 -> 64 -> 64 -> 1, BF16/FP32, on the GPU."""
+
+    def __init__(self, seed: int = 0, device: int = 0):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.gdp_mlp_create(int(seed), int(device), C.byref(h)), "gdp_mlp_create")
+        self._h = h
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.zeros(MLP_PARAMS, np.float32)
+        _check(self._lib.gdp_mlp_get_params(self._h, _pf(out)), "gdp_mlp_get_params")
+        return out
+
+    @params.setter
+    def params(self, p) -> None:
+        p = _f32(p)
+        if p.size != MLP_PARAMS:
+            raise GDPError(f"expected {MLP_PARAMS} parameters")
+        _check(self._lib.gdp_mlp_set_params(self._h, _pf(p)), "gdp_mlp_set_params")
+
+    def forward(self, x) -> np.ndarray:
+        x = _f32(x).reshape(-1, MLP_FEATURES)
+        z = np.zeros(len(x), np.float32)
+        _check(self._lib.gdp_mlp_forward(self._h, len(x), _pf(x), _pf(z)), "gdp_mlp_forward")
+        return z
+
+    def gradient(self, x, y, w=None):
+        x = _f32(x).reshape(-1, MLP_FEATURES)
+        y = _f32(y)
+        w = _f32(np.ones(len(x)) if w is None else w)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        _check(self._lib.gdp_mlp_gradient(self._h, len(x), _pf(x), _pf(y), _pf(w), _pf(g), C.byref(loss)),
+               "gdp_mlp_gradient")
+        return float(loss.value), g
+
+    def train(self, x, y, w=None, epochs: int = 5, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> float:
+        x = _f32(x).reshape(-1, MLP_FEATURES)
+        y = _f32(y)
+        w = _f32(np.ones(len(x)) if w is None else w)
+        loss = C.c_float()
+        _check(self._lib.gdp_mlp_train(self._h, len(x), _pf(x), _pf(y), _pf(w), int(epochs), int(batch),
+                                       float(lr), int(seed), C.byref(loss)), "gdp_mlp_train")
+        return float(loss.value)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gdp_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -39,7 +39,9 @@ typedef struct {
                              1 (default, also -1): adaptive -- marked rounds follow rounds that
                              tightened fewer than n_vars/16 bounds; 0: always sweep every row;
                              2: every round after the first is marked */
-    int reserved[7];      /* must be zero */
+    int ctas_per_sm;      /* resident CTAs per SM of the persistent round loop and of the phase
+                             kernels; 0 (default) = as many as fit */
+    int reserved[6];      /* must be zero */
 } gdp_options;
 
 typedef struct {
@@ -58,6 +60,9 @@ typedef struct {
     double total_ms;        /* host wall time of the call */
     long long nnz_exact;    /* non-zeros of the rows that the FP32 screen could not skip and that
                                went through the exact FP64 pass, summed over rounds */
+    long long rows_deferred; /* learned marking: marked rows the model left for a later round */
+    int full_rounds;        /* learned marking: rounds that swept every row (incl. the certification) */
+    int pad_;
 } gdp_stats;
 
 /* Fills *opts with the defaults. */
@@ -134,6 +139,85 @@ GDP_RETCODE gdp_batch_propagate(gdp_batch *b, double *const *lbs, double *const 
 int gdp_batch_uses_graph(const gdp_batch *b);
 
 GDP_RETCODE gdp_batch_destroy(gdp_batch *b);
+
+/* ---- learned row marking (no counterpart in the reference) ------------------
+ * A 16 -> 64 -> 64 -> 1 MLP (ReLU; BF16 weights and activations, FP32
+ * accumulation; forward and the activation-gradient product on the tensor
+ * cores) scores, from per-row features, whether processing a row that a
+ * changed variable marked will tighten a bound. Parameters are one FP32
+ * vector of GDP_MLP_PARAMS floats: W1[64][16], b1[64], W2[64][64], b2[64],
+ * w3[64], b3. Features are GDP_MLP_FEATURES floats per row (see
+ * gdp_context_trace). */
+#define GDP_MLP_FEATURES 16
+#define GDP_MLP_PARAMS 5313
+typedef struct gdp_mlp gdp_mlp;
+
+/* He-uniform weights from `seed`, zero biases, on `device`. */
+GDP_RETCODE gdp_mlp_create(unsigned long long seed, int device, gdp_mlp **out);
+GDP_RETCODE gdp_mlp_destroy(gdp_mlp *m);
+GDP_RETCODE gdp_mlp_get_params(const gdp_mlp *m, float *params);
+/* Sets the FP32 master parameters (and resets the optimizer state). */
+GDP_RETCODE gdp_mlp_set_params(gdp_mlp *m, const float *params);
+/* logits[i] of the n x 16 host features x (rounded to BF16 on the device). */
+GDP_RETCODE gdp_mlp_forward(gdp_mlp *m, int n, const float *x, float *logits);
+/* Gradient (GDP_MLP_PARAMS floats) and value of the weighted binary
+ * cross-entropy sum_i w_i BCE(sigmoid(z_i), y_i) / sum_i w_i at the current
+ * parameters. */
+GDP_RETCODE gdp_mlp_gradient(gdp_mlp *m, int n, const float *x, const float *y, const float *w, float *grad,
+                             float *loss);
+/* Adam (beta 0.9 / 0.999) over minibatches of `batch` samples for `epochs`
+ * passes, on the device; final_loss (may be NULL): the last epoch's mean loss. */
+GDP_RETCODE gdp_mlp_train(gdp_mlp *m, int n, const float *x, const float *y, const float *w, int epochs,
+                          int batch, float lr, unsigned long long seed, float *final_loss);
+
+/* Attaches `model` (NULL detaches) to ctx: its propagations then run learned
+ * rounds. A learned round processes the marked rows (rows with a variable
+ * changed since they were last processed) whose logit is >= threshold, plus
+ * every marked row shorter than min_len non-zeros; the others stay marked for a
+ * later round. Rows longer than split_tile are always processed when marked. A
+ * learned round that changes nothing is followed by a round over every marked
+ * row, one of those that changes nothing by a round over every row, and the
+ * propagation ends only when such a full round changes nothing (or at
+ * max_rounds), so the bounds are a certified fixpoint whatever the model
+ * predicts. The model must outlive its use by ctx; learned propagations always
+ * run as one persistent launch. */
+GDP_RETCODE gdp_context_set_model(gdp_context *ctx, const gdp_mlp *model, float threshold, int min_len);
+
+/* Trace propagation of ctx's problem from lbs/ubs (host, in/out) with exact
+ * marking (every marked row processed): for each marked row of a marked round
+ * the 16 features before processing go to features[16 * i ..] and the label
+ * (1: processing it tightened a bound) to labels[i], for the first `capacity`
+ * such rows; *n_samples receives their count. Features: log2(1+len)/16;
+ * last screen's infinity counts minf/3, maxf/3 (capped at 3); normalised slack
+ * and log-ratio of the activity-delta bound to the slack; lhs infinite; rhs
+ * infinite; equality row; rounds since the row last tightened, was last
+ * processed, and has been marked (each min(.,63)/63); changed variables since
+ * last processed / len; unproductive-processing streak/15; last screen said
+ * exact; last row test said go; never processed. */
+GDP_RETCODE gdp_context_trace(gdp_context *ctx, double *lbs, double *ubs, int capacity, float *features,
+                              float *labels, int *n_samples, gdp_stats *stats);
+
+/* ---- autotuner (no counterpart in the reference) ---------------------------
+ * Times the propagation of one problem from lbs/ubs (host, not modified) under
+ * candidate row bins (thread_row_max in {16, 32, 64} x split_tile in {512,
+ * 1024, 2048}) and loop schedules (MEGAKERNEL with 2, 3 or all-fitting CTAs
+ * per SM, GPU_LOOP), `repeats` times each (best device time counts), starting
+ * from `base` (may be NULL) for every other option. *best receives the
+ * fastest options and *best_ms their device time; trials (may be NULL)
+ * receives up to max_trials records and *n_trials their count. The layouts
+ * only change the summation order of rows longer than thread_row_max (each
+ * layout is bit-exact with the oracle's matching GPU mode), so on slowly
+ * converging continuous bounds the round count may differ by a round between
+ * candidates; the time to the fixpoint is what counts. */
+typedef struct {
+    int thread_row_max, split_tile, sync_type, ctas_per_sm, rounds, pad_;
+    double ms;
+} gdp_tune_trial;
+GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *csr_col_indices, const int *csr_row_ptrs,
+                         const double *csr_vals, const double *lhss, const double *rhss, const double *lbs,
+                         const double *ubs, const int *vartypes, const gdp_options *base, int repeats,
+                         gdp_options *best, double *best_ms, gdp_tune_trial *trials, int max_trials,
+                         int *n_trials);
 
 /* Propagation that allocates no memory, for callers that cannot call
  * cudaMalloc (e.g. a solver or framework whose device memory belongs to its
