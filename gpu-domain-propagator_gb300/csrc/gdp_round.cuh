@@ -601,19 +601,24 @@ __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane
                                             unsigned *tight_ctr, unsigned *qbuf) {
     const int row = __ldg(P.tile_row + t);
     if (P.row_exact[row] != round) return;
+    // lanes load 32 partials at a time; lane 0 folds them in tile order
+    const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
     Acc s;
     acc_init(s);
-    if (lane == 0) {
-        const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
-        {
-            const TilePart p = P.tile_part[t0];
-            s.minact = p.minact; s.maxact = p.maxact; s.minf = p.minf; s.maxf = p.maxf; s.U = p.U;
-        }
-        for (int u = t0 + 1; u < t1; u++) {
-            const TilePart p = P.tile_part[u];
+    for (int b = t0; b < t1; b += 32) {
+        TilePart p = {0.0, 0.0, 0, 0, 0.0f, 0};
+        if (b + lane < t1) p = P.tile_part[b + lane];
+        const int cnt = min(32, t1 - b);
+        for (int i = 0; i < cnt; i++) {
             Acc o;
-            o.minact = p.minact; o.maxact = p.maxact; o.minf = p.minf; o.maxf = p.maxf; o.U = p.U; o.L = 0.0f;
-            acc_combine(s, o);
+            o.minact = __shfl_sync(kFull, p.minact, i);
+            o.maxact = __shfl_sync(kFull, p.maxact, i);
+            o.minf = __shfl_sync(kFull, p.minf, i);
+            o.maxf = __shfl_sync(kFull, p.maxf, i);
+            o.U = __shfl_sync(kFull, p.U, i);
+            o.L = 0.0f;
+            if (b + i == t0) s = o;
+            else acc_combine(s, o);
         }
     }
     split_row_candidates(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, qbuf);
