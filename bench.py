@@ -274,7 +274,7 @@ def run_batched(args, ws, rank, local):
         plain_mips = [mip] * len(members[0])
         sizes = {"m": mip.m, "n": mip.n, "nnz": mip.nnz, "root_rounds": rst["rounds"]}
     else:
-        batch = gdp.Batch.instances(mips)
+        batch = gdp.Batch.instances(mips, autotune=args.autotune)
         members = ([m.lb for m in mips], [m.ub for m in mips])
         plain_mips = mips
         sizes = {"members": len(mips), "m_total": int(sum(m.m for m in mips)),
@@ -323,7 +323,8 @@ def run_batched(args, ws, rank, local):
             "config": {"workload": BATCH_WORKLOADS[args.workload], **sizes, "scale": args.scale,
                        "batch_rounds": tot["rounds"], "infeasible_members": tot["infeasible"],
                        "rows_processed": tot["rows_processed"], "nnz_processed": tot["nnz_processed"],
-                       "nnz_exact": tot["nnz_exact"], "graph": batch.uses_graph, "parallelism": "single"},
+                       "nnz_exact": tot["nnz_exact"], "graph": batch.uses_graph, "parallelism": "single",
+                       "autotune": getattr(batch, "tuned", None)},
             "plain": {"full_sweep_ms": plain_full_ms, "adaptive_marking_ms": plain_adapt_ms,
                       "rounds_max": max(rounds_full), "rounds_sum": int(sum(rounds_full)),
                       "bitexact_full_sweep": bool(agree_full), "bitexact_adaptive": bool(agree_adapt),
@@ -517,7 +518,7 @@ def main():
             "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": rounds,
                        "converged": bool(stats[-1]["converged"]), "infeasible": bool(stats[-1]["infeasible"]),
                        "sync": args.sync, "layout": layout, "marking": args.marking,
-                       "rows_processed": stats[-1]["rows_processed"], "nnz_processed": stats[-1]["nnz_processed"], "nnz_exact": stats[-1]["nnz_exact"], "parallelism": "replicas" if ws > 1 else "single",
+                       "rows_processed": stats[-1]["rows_processed"], "nnz_processed": stats[-1]["nnz_processed"], "nnz_exact": stats[-1]["nnz_exact"], "divisions": stats[-1]["divisions"], "rows_exact": stats[-1]["rows_exact"], "rows_go": stats[-1]["rows_go"], "changed_vars": stats[-1]["changed_vars"], "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (CSR %.0f MB vs 129 MB L2)" % (mip.nnz * 12 / 1e6),
                        "scale": args.scale},
             "hbm_gbs": achieved, "nnz_per_s": mip.nnz * rounds / (ms_step * 1e-3),

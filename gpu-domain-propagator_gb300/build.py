@@ -25,7 +25,7 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["gdp_round.cu", "gdp_context.cu", "gdp_capi.cu", "gdp_noalloc.cu", "gdp_layout.cu", "gdp_batch.cu",
-                "gdp_batch_host.cu", "gdp_mlp.cu", "gdp_learned.cu", "gdp_tune.cu"]
+                "gdp_batch_host.cu", "gdp_mlp.cu", "gdp_learned.cu", "gdp_tune.cu", "gdp_mps.cu"]
 
 
 def _nvcc() -> str:

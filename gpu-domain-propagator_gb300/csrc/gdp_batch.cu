@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
             const int fs_items = *((volatile int *)(B.fs_prefix + nfs));
             const int n_entries = (int)min(*((volatile unsigned *)(B.tail + par)), B.cap_entries);
             const unsigned long long *ent = B.entries + (size_t)par * B.cap_entries;
+            stats_zero(mine, lane);
             for (;;) {
                 const int i = warp_next(ctr + 0, lane);
                 if (i >= fs_items + n_entries) break;
@@ -204,9 +205,10 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
                 unsigned *tight = &Pu.flags[1 + par].tight;
                 if (it >= 0) {
                     sell_slice(Pu, it, lane, r, marked, change, tight, mine);
-                } else if (split_partial(Pu, -it - 1, lane, r, marked, change, tight, mine.q) && lane == 0) {
+                } else if (split_partial(Pu, -it - 1, lane, r, marked, change, tight, mine) && lane == 0) {
                     push_tile(B.cq, B.tail + 2, B.cap_tiles, B.error, u, -it - 1);
                 }
+                stats_flush(Pu, mine, lane);  // statistics belong to the item's unit
             }
         }
         if (!grid_barrier(B.barrier, B.error)) return;
@@ -227,8 +229,9 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
                 const unsigned long long e = B.cq[i];
                 const int u = (int)(e >> 32), t = (int)(unsigned)e;
                 const DevProblem &Pu = B.units[u];
-                if (split_cand(Pu, t, lane, r, false, &Pu.flags[1 + par].exact) && lane == 0)
+                if (split_cand(Pu, t, lane, r, false, &Pu.flags[1 + par].exact, mine) && lane == 0)
                     push_tile(B.xq, B.tail + 3, B.cap_tiles, B.error, u, t);
+                stats_flush(Pu, mine, lane);
             }
             if (!grid_barrier(B.barrier, B.error)) return;
             // ---- C
@@ -240,7 +243,8 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
                     const unsigned long long e = B.xq[i];
                     const int u = (int)(e >> 32), t = (int)(unsigned)e;
                     const DevProblem &Pu = B.units[u];
-                    split_exact(Pu, t, lane, r, &Pu.flags[1 + par].change, &Pu.flags[1 + par].tight, mine.q);
+                    split_exact(Pu, t, lane, r, &Pu.flags[1 + par].change, &Pu.flags[1 + par].tight, mine);
+                    stats_flush(Pu, mine, lane);
                 }
                 if (!grid_barrier(B.barrier, B.error)) return;
             }
@@ -266,7 +270,7 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
             unsigned bits = Pu.chg[wl];
             if (!bits) continue;
             Pu.chg[wl] = 0u;
-            atomicAdd(&Pu.flags[0].changed_vars, (unsigned long long)__popc(bits));
+            atomicAdd(&Pu.flags[0].changed_vars, (unsigned long long)__popc(bits));  // per word, per unit
             const bool push = more && unit_next_marked(Pu, r);
             while (bits) {
                 const int j = wl * 32 + __ffs(bits) - 1;

@@ -55,7 +55,7 @@ public:
     int max_rounds = GDP_MAX_NUM_ROUNDS;
 
 private:
-    GDP_RETCODE finish_init(int device);
+    GDP_RETCODE finish_init(int device, int ctas_per_sm);
     GDP_RETCODE enqueue(cudaStream_t s);
 
     std::vector<std::unique_ptr<Context>> inst_;  // instances (units in heaviest-first order)

@@ -78,7 +78,7 @@ GDP_RETCODE Batch::init_instances(int n_inst, const int *n_cons, const int *n_va
     }
     seed_mode_.assign(n_units, 0);
     ref_ = nullptr;
-    return finish_init(opts.device);
+    return finish_init(opts.device, opts.ctas_per_sm);
 }
 
 GDP_RETCODE Batch::init_nodes(Context *ctx, int n_nodes) {
@@ -114,10 +114,10 @@ GDP_RETCODE Batch::init_nodes(Context *ctx, int n_nodes) {
     }
     seed_mode_.assign(n_units, 1);
     ref_ = ctx->P.bnd;  // read only while the context's last propagation is certified
-    return finish_init(ctx->opts.device);
+    return finish_init(ctx->opts.device, ctx->opts.ctas_per_sm);
 }
 
-GDP_RETCODE Batch::finish_init(int device) {
+GDP_RETCODE Batch::finish_init(int device, int ctas_per_sm) {
     GDP_BCUDA(cudaSetDevice(device));
     GDP_BCUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     GDP_BCUDA(cudaEventCreate(&ev0_));
@@ -197,6 +197,7 @@ GDP_RETCODE Batch::finish_init(int device) {
     int bps = 0, sms = 0;
     GDP_BCUDA((cudaError_t)batch_occupancy(&bps));
     GDP_BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    if (ctas_per_sm > 0) bps = std::min(bps, ctas_per_sm);
     grid = std::max(1, bps) * sms;
     GDP_BCUDA(cudaStreamSynchronize(stream_));
     return GDP_OKAY;

@@ -489,6 +489,9 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         st->nnz_processed = (long long)f.nnz_proc;
         st->nnz_exact = (long long)f.nnz_exact;
         st->rows_deferred = (long long)f.rows_deferred;
+        st->divisions = (long long)f.divisions;
+        st->rows_exact = (long long)f.rows_exact;
+        st->rows_go = (long long)f.rows_go;
         st->full_rounds = f.full_rounds;
         st->bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc + 36.0 * n * (double)f.rounds;
         st->device_ms = ms;

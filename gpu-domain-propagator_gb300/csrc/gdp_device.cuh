@@ -220,18 +220,18 @@ __device__ __forceinline__ DeltaBox delta_box(long long ab, long long lbb, long 
 }
 
 // Activity accumulator: the reference's computeActivities terms with integer
-// classification (no FP64 compares) and an FP32 enclosure [L, U] of the
-// maximum of |a| (ub - lb) (the reference's maxactdelta, before its EPS rule).
+// classification (no FP64 compares), and an FP32 upper bound U of the maximum
+// of |a| (ub - lb) (used by the row test of rows summed by several lanes).
 struct Acc {
     double minact, maxact;
     int minf, maxf;
-    float U, L;
+    float U;
 };
 __device__ __forceinline__ void acc_init(Acc &s) {
-    s.minact = 0.0; s.maxact = 0.0; s.minf = 0; s.maxf = 0; s.U = 0.0f; s.L = 0.0f;
+    s.minact = 0.0; s.maxact = 0.0; s.minf = 0; s.maxf = 0; s.U = 0.0f;
 }
-template <bool kLower>
-__device__ __forceinline__ void acc_add(Acc &s, double a, double lb, double ub) {
+// The activity terms and infinity counts of one element.
+__device__ __forceinline__ void acc_add_terms(Acc &s, double a, double lb, double ub) {
     const long long ab = dbits(a), lbb = dbits(lb), ubb = dbits(ub);
     const bool pos = gt_eps_bits(ab);
     const bool lneg = neginf_bits(lbb), upos = posinf_bits(ubb);
@@ -242,8 +242,11 @@ __device__ __forceinline__ void acc_add(Acc &s, double a, double lb, double ub) 
     const bool gt0 = gt0_bits(ab);
     if (!min_inf) s.minact = dadd(s.minact, dmul(a, gt0 ? lb : ub));
     if (!max_inf) s.maxact = dadd(s.maxact, dmul(a, gt0 ? ub : lb));
-    s.U = fmaxf(s.U, delta_up(ab, lbb, ubb));
-    if (kLower) s.L = fmaxf(s.L, delta_box(ab, lbb, ubb).lo);
+}
+// Terms, infinity counts and the FP32 bound U.
+__device__ __forceinline__ void acc_add(Acc &s, double a, double lb, double ub) {
+    acc_add_terms(s, a, lb, ub);
+    s.U = fmaxf(s.U, delta_up(dbits(a), dbits(lb), dbits(ub)));
 }
 __device__ __forceinline__ void acc_combine(Acc &a, const Acc &b) {
     a.minact = dadd(a.minact, b.minact);
@@ -251,22 +254,6 @@ __device__ __forceinline__ void acc_combine(Acc &a, const Acc &b) {
     a.minf += b.minf;
     a.maxf += b.maxf;
     a.U = fmaxf(a.U, b.U);
-    a.L = fmaxf(a.L, b.L);
-}
-
-// Exact decision from the enclosure where possible. The reference's
-// sequential maxactdelta m satisfies M - 1e-9 <= m <= M for the true maximum
-// M >= 0 of |a|(ub-lb) (an element below the running value by at most 1e-9 is
-// skipped, so the running value never trails the maximum by more), and
-// L <= M <= U. Returns 0: skip, 1: process, 2: undecided (needs the exact
-// sequential pass). mn is min(rhs - minact, maxact - lhs).
-__device__ __forceinline__ int row_decision(int minf, int maxf, float U, float L, double mn) {
-    if (minf > 1 && maxf > 1) return 0;
-    if (mn < kInf && (double)__fmul_rn(U, kUMargin) <= mn) return 0;  // m <= M <= U <= mn
-    // m - mn >= L - 1e-9 - mn > 3e-9 - 1e-9: then fl(m - mn) > 1e-9 (see eps_gt_sure)
-    const double mn_hi = dadd(mn, 4e-9);
-    if ((double)widen_dn(L) > mn_hi) return 1;
-    return 2;
 }
 
 // min(rhs - minact, maxact - lhs) as std::min(s, t) in canConsBeTightened.
@@ -372,8 +359,9 @@ __device__ __forceinline__ void scr_combine(Scr &a, const Scr &b) {
 }
 // Largest float not above 1e20 (the infinity threshold).
 constexpr float kInfF32Dn = 0x1.5af1d6p+66f;
-// True when the row filter (u_filter_skips, and row_decision's skip branch)
-// certainly skips the row: the FP64 activities of any summation order lie in
+// True when the row filter certainly skips the row (u_filter_skips, and the
+// reference's test, whose sequential maxactdelta m satisfies m <= M <= U for the
+// true maximum M of |a|(ub - lb)): the FP64 activities of any summation order lie in
 // [lo - E, hi + E] with E = 2^-20 S (the rounding error of n <= 2^31 FP64
 // additions is below n 2^-53 S), and FP64 rounding of rhs - minact and
 // maxact - lhs is monotone, so min(rhs - minact, maxact - lhs) >= the

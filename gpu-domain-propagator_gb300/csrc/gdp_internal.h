@@ -57,6 +57,9 @@ struct RoundFlags {
     unsigned long long nnz_proc;      // their non-zeros
     unsigned long long nnz_exact;     // non-zeros that also went through the exact FP64 pass
     unsigned long long rows_deferred; // learned marking: marked rows the model left for a later round
+    unsigned long long divisions;     // candidate divisions (bound candidates computed)
+    unsigned long long rows_exact;    // SELL rows through the exact FP64 pass
+    unsigned long long rows_go;       // ... of which had their candidates computed
 };
 
 enum DeviceError : int {

@@ -155,7 +155,7 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
         exact = !scr_skips(c, lhs, rhs);
         st = screen_stats(c, lhs, rhs);
     }
-    count_work(P, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
+    count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
     __syncwarp();
     if (__any_sync(kFull, exact)) {
@@ -189,13 +189,17 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
 __device__ __forceinline__ void learned_activity_phase(const DevProblem &P, int round, int kind, unsigned *ctr,
                                                        int *change, unsigned *tight_ctr, WarpSmem &ws,
                                                        LearnSmem &L, int lane) {
+    stats_zero(ws, lane);
+    WarpCursor cur;
+    cur.start(ctr, 1u, lane);
     for (;;) {
-        const int i = warp_next(ctr, lane);
+        const int i = cur.next(lane);
         if (i >= P.n_items) break;
         const int it = __ldg(P.items + i);
         if (it >= 0) sell_slice_learned(P, it, lane, round, kind, change, tight_ctr, ws, L);
-        else split_partial(P, -it - 1, lane, round, kind != kRoundFull, change, tight_ctr, ws.q);
+        else split_partial(P, -it - 1, lane, round, kind != kRoundFull, change, tight_ctr, ws);
     }
+    stats_flush(P, ws, lane);
 }
 
 // Commit changed variables; mark their rows for the next round: SELL rows
@@ -229,7 +233,7 @@ __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round,
             }
         }
     }
-    if (changed) atomicAdd(&P.flags[0].changed_vars, changed);
+    flush_changed(P, changed);
 }
 
 __global__ void __launch_bounds__(kCtaThreads, 2) k_megakernel_learned(DevProblem P) {
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2) k_megakernel_learned(DevProble
                 if (full) P.flags[0].full_rounds += 1;
             }
             if (P.n_mtiles) {
-                candidate_phase(P, round, !full, q + 1, exact, lane);
+                candidate_phase(P, round, !full, q + 1, exact, mine, lane);
                 if (!grid_barrier(P.barrier, err)) return;
                 if (*((volatile int *)exact)) {
                     exact_phase(P, round, q + 2, change, tight, mine, lane);

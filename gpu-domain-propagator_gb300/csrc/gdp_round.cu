@@ -23,7 +23,8 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_candidates(DevProblem P) {
     if (P.flags[0].infeasible) return;
     if (exact_rows_queued(P, 0))
         exact_rows_phase(P, 0, &P.flags[0].change, &P.flags[0].tight, ws[threadIdx.x >> 5], threadIdx.x & 31);
-    candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].exact, threadIdx.x & 31);
+    candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].exact, ws[threadIdx.x >> 5],
+                    threadIdx.x & 31);
 }
 
 __global__ void __launch_bounds__(kCtaThreads, 4) k_exact(DevProblem P) {
@@ -132,7 +133,7 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
             const bool xrows = exact_rows_queued(P, par);
             if (xrows || P.n_mtiles) {
                 if (xrows) exact_rows_phase(P, par, change, tight, mine, lane);
-                if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, lane);
+                if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, mine, lane);
                 if (!grid_barrier(P.barrier, err)) return;
                 if (P.n_mtiles && *((volatile int *)exact)) {
                     exact_phase(P, round, q + 2, change, tight, mine, lane);

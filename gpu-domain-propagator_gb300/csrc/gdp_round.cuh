@@ -143,7 +143,8 @@ __device__ __forceinline__ bool apply_side(const DevProblem &P, const RowC &c, i
 // items (ballot + prefix), drain() runs full batches of 32.
 struct WarpQueue {
     unsigned *q;
-    int cnt;  // warp-uniform
+    int cnt;     // warp-uniform
+    int pushed;  // warp-uniform: candidate sides queued (each one division)
 };
 
 template <class Run>
@@ -167,6 +168,7 @@ __device__ __forceinline__ void queue_push(WarpQueue &Q, int lane, int sides, un
     if (sides & 2) Q.q[Q.cnt + __popc(bu) + __popc(bl & lt)] = code_base | 1u;
     __syncwarp();
     Q.cnt += __popc(bu) + __popc(bl);
+    Q.pushed += __popc(bu) + __popc(bl);
 }
 
 // Warp-aggregated round bookkeeping: change flag and tightening count.
@@ -184,6 +186,49 @@ struct WarpSmem {
     RowC rc[32];
     unsigned q[kQueueCap];
     long long base[32];  // deferred exact pass: first element of each lane
+    // work statistics of this warp, written by lane 0 and flushed to the
+    // round flags once per phase (not once per item: same-address atomics
+    // from every warp for every item would serialise in L2)
+    unsigned long long st_rows, st_nnz, st_exact, st_div, st_xrows, st_go;
+};
+
+__device__ __forceinline__ void stats_zero(WarpSmem &ws, int lane) {
+    if (lane == 0) {
+        ws.st_rows = 0; ws.st_nnz = 0; ws.st_exact = 0; ws.st_div = 0;
+        ws.st_xrows = 0; ws.st_go = 0;
+    }
+}
+__device__ __forceinline__ void stats_flush(const DevProblem &P, WarpSmem &ws, int lane) {
+    if (lane == 0) {
+        if (ws.st_rows) atomicAdd(&P.flags[0].rows_proc, ws.st_rows);
+        if (ws.st_nnz) atomicAdd(&P.flags[0].nnz_proc, ws.st_nnz);
+        if (ws.st_exact) atomicAdd(&P.flags[0].nnz_exact, ws.st_exact);
+        if (ws.st_div) atomicAdd(&P.flags[0].divisions, ws.st_div);
+        if (ws.st_xrows) atomicAdd(&P.flags[0].rows_exact, ws.st_xrows);
+        if (ws.st_go) atomicAdd(&P.flags[0].rows_go, ws.st_go);
+        ws.st_rows = 0; ws.st_nnz = 0; ws.st_exact = 0; ws.st_div = 0;
+        ws.st_xrows = 0; ws.st_go = 0;
+    }
+}
+
+// Warp-level dynamic work counter that keeps the next claim in flight while
+// the current item is processed: the contended atomic's round trip overlaps
+// with useful work instead of stalling the warp between items.
+struct WarpCursor {
+    unsigned *ctr;
+    unsigned step;
+    unsigned pre;  // lane 0: the claim in flight
+    __device__ __forceinline__ void start(unsigned *c, unsigned stp, int lane) {
+        ctr = c;
+        step = stp;
+        pre = 0;
+        if (lane == 0) pre = atomicAdd(c, stp);
+    }
+    __device__ __forceinline__ int next(int lane) {
+        const int i = (int)__shfl_sync(kFull, pre, 0);
+        if (lane == 0) pre = atomicAdd(ctr, step);
+        return i;
+    }
 };
 
 // Learned marking: features, scores and per-row outcomes of one slice.
@@ -204,7 +249,6 @@ __device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
         o.minf = __shfl_down_sync(kFull, s.minf, off);
         o.maxf = __shfl_down_sync(kFull, s.maxf, off);
         o.U = __shfl_down_sync(kFull, s.U, off);
-        o.L = __shfl_down_sync(kFull, s.L, off);
         acc_combine(s, o);
     }
 }
@@ -225,7 +269,7 @@ __device__ __forceinline__ void scr_group_reduce(Scr &c, int g) {
 }
 
 // Adds the warp's row and non-zero counts to the round statistics.
-__device__ __forceinline__ void count_work(const DevProblem &P, int lane, int rows, int nnz, int nnz_exact) {
+__device__ __forceinline__ void count_work(WarpSmem &ws, int lane, int rows, int nnz, int nnz_exact) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         rows += __shfl_down_sync(kFull, rows, off);
@@ -233,9 +277,9 @@ __device__ __forceinline__ void count_work(const DevProblem &P, int lane, int ro
         nnz_exact += __shfl_down_sync(kFull, nnz_exact, off);
     }
     if (lane == 0) {
-        if (rows) atomicAdd(&P.flags[0].rows_proc, (unsigned long long)rows);
-        if (nnz) atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)nnz);
-        if (nnz_exact) atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)nnz_exact);
+        ws.st_rows += (unsigned long long)rows;
+        ws.st_nnz += (unsigned long long)nnz;
+        ws.st_exact += (unsigned long long)nnz_exact;
     }
 }
 
@@ -243,11 +287,11 @@ __device__ __forceinline__ void count_work(const DevProblem &P, int lane, int ro
 // lane l serves row l >> lg (active if `exact`), its elements at
 // ws.base[l] + 32 i for i < cnt (element sub + g i of the row, sub = l & (g-1)).
 // The leader lane of each row (sub == 0) holds its position, lhs and rhs.
-//   pass 1: exact FP64 activities. g == 1 rows are summed left to right and
-//           take the reference's exact row decision; g > 1 rows are combined
-//           by a shuffle tree and use the FP32 bound rule.
-//   pass 2: (g == 1, rare) the reference's sequential EPS-max.
-//   pass 3: candidates through the warp division queue.
+//   pass 1: exact FP64 activities. g == 1 rows are summed left to right,
+//           with the reference's sequential EPS-max of |a|(ub - lb) in the
+//           same loop, and take the reference's row test; g > 1 rows are
+//           combined by a shuffle tree and use the FP32 bound rule.
+//   pass 2: candidates through the warp division queue.
 __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int lane, bool exact, int len,
                                                 int cnt, double lhs, double rhs, int *change,
                                                 unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
@@ -261,40 +305,55 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
     const int cnt1 = exact ? cnt : 0;
     Acc s;
     acc_init(s);
-#pragma unroll 4
-    for (int i = 0; i < cnt1; i++) {
-        const int j = __ldg(col + 32 * i);
-        const double a = __ldg(val + 32 * i);
-        const double2 b = load_bnd(P, j);
-        acc_add<true>(s, a, b.x, b.y);
-    }
-    if (g > 1) acc_group_reduce(s, g);
     double mn = 0.0;
     int dec = 0;
-    if (leader) {
-        mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
-        if (g == 1) dec = row_decision(s.minf, s.maxf, s.U, s.L, mn);
-        else dec = u_filter_skips(s.minf, s.maxf, s.U, mn) ? 0 : 1;
-    }
-    if (__any_sync(kFull, dec == 2)) {
+    if (lg == 0) {
+        // one lane per row, elements in order: the reference's left-to-right
+        // sums and its sequential EPS-max of |a|(ub - lb) in the same loop, so
+        // the row test is the reference's own (canConsBeTightened)
         double m = 0.0;
-        const int len2 = dec == 2 ? len : 0;
-        for (int k = 0; k < len2; k++) {
-            const int j = __ldg(col + 32 * k);
-            const double a = __ldg(val + 32 * k);
+#pragma unroll 4
+        for (int i = 0; i < cnt1; i++) {
+            const int j = __ldg(col + 32 * i);
+            const double a = __ldg(val + 32 * i);
             const double2 b = load_bnd(P, j);
+            acc_add_terms(s, a, b.x, b.y);
             const double d = dmul(fabs(a), dsub(b.y, b.x));
             if (eps_gt_fast(d, m)) m = d;
         }
-        if (dec == 2) dec = reference_row_go(s.minf, s.maxf, m, mn) ? 1 : 0;
+        if (leader) {
+            mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
+            dec = reference_row_go(s.minf, s.maxf, m, mn) ? 1 : 0;
+        }
+    } else {
+#pragma unroll 4
+        for (int i = 0; i < cnt1; i++) {
+            const int j = __ldg(col + 32 * i);
+            const double a = __ldg(val + 32 * i);
+            const double2 b = load_bnd(P, j);
+            acc_add(s, a, b.x, b.y);
+        }
+        acc_group_reduce(s, g);
+        if (leader) {
+            mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
+            dec = u_filter_skips(s.minf, s.maxf, s.U, mn) ? 0 : 1;
+        }
+    }
+    {
+        const unsigned bx = __ballot_sync(kFull, leader);
+        if (lane == 0) ws.st_xrows += __popc(bx);
     }
     int tight = 0;
     const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && exact;
     if (row_go && leader) row_go[rl] = go ? 1 : 0;
+    {
+        const unsigned bg = __ballot_sync(kFull, go && sub == 0);
+        if (lane == 0) ws.st_go += __popc(bg);
+    }
     if (__any_sync(kFull, go)) {
         if (leader && dec == 1) ws.rc[rl] = make_rowc(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs);
         __syncwarp();
-        WarpQueue Q{ws.q, 0};
+        WarpQueue Q{ws.q, 0, 0};
         auto run = [&](unsigned code) {
             const int owner = (code >> 1) & 31;
             const int i = (int)(code >> 6);
@@ -321,6 +380,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
             queue_drain(Q, lane, false, run);
         }
         queue_drain(Q, lane, true, run);
+        if (lane == 0) ws.st_div += (unsigned long long)Q.pushed;
     }
     report_tight(tight, lane, change, tight_ctr);
 }
@@ -368,7 +428,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
             exact = !scr_skips(c, lhs, rhs);
         }
     }
-    count_work(P, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
+    count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
     if (P.defer_exact) {
         const unsigned bal = __ballot_sync(kFull, exact);
         if (!bal) return;
@@ -389,6 +449,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
 // first), 32/g rows per warp with their elements read from their own slices.
 __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, int *change, unsigned *tight_ctr,
                                                  WarpSmem &ws, int lane) {
+    stats_zero(ws, lane);
     for (int lg = 5; lg >= 0; lg--) {
         const int n = (int)*((volatile unsigned *)(P.xctr + 16 * par + lg));
         if (!n) continue;
@@ -420,6 +481,7 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             __syncwarp();
         }
     }
+    stats_flush(P, ws, lane);
 }
 
 // ---- split rows: one warp per tile ----------------------------------------
@@ -440,7 +502,7 @@ __device__ __forceinline__ void acc_shfl_reduce(Acc &s) {
 // element range [b, e) of one tile, from the row's complete activities held by
 // lane 0; the warp queues the divisions.
 __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int row, int b, int e, const Acc &s0,
-                                                     int lane, int *change, unsigned *tight_ctr, unsigned *qbuf) {
+                                                     int lane, int *change, unsigned *tight_ctr, WarpSmem &ws) {
     RowC c;
     int go = 0;
     if (lane == 0) {
@@ -462,7 +524,7 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
     c.nsur_dn = __shfl_sync(kFull, c.nsur_dn, 0);
     c.nsur_hi = __shfl_sync(kFull, c.nsur_hi, 0);
     int tight = 0;
-    WarpQueue Q{qbuf, 0};
+    WarpQueue Q{ws.q, 0, 0};
     auto run = [&](unsigned code) {
         const int k = b + (int)(code >> 1);
         tight += apply_side(P, c, __ldg(P.lcol + k), __ldg(P.lval + k), (int)(code & 1u)) ? 1 : 0;
@@ -480,6 +542,7 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
         queue_drain(Q, lane, false, run);
     }
     queue_drain(Q, lane, true, run);
+    if (lane == 0) ws.st_div += (unsigned long long)Q.pushed;
     report_tight(tight, lane, change, tight_ctr);
 }
 
@@ -509,7 +572,7 @@ __device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int
         const int j = __ldg(P.lcol + k);
         const double a = __ldg(P.lval + k);
         const double2 bb = load_bnd(P, j);
-        acc_add<false>(s, a, bb.x, bb.y);
+        acc_add(s, a, bb.x, bb.y);
     }
     acc_shfl_reduce(s);
     return s;
@@ -520,7 +583,7 @@ __device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int
 // tiles of longer rows store their screen partial for the candidate phase
 // (returns true for those).
 __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int lane, int round, bool marked,
-                                              int *change, unsigned *tight_ctr, unsigned *qbuf) {
+                                              int *change, unsigned *tight_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
     if (marked && P.mark[P.n_srows + row] != round) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
@@ -538,11 +601,11 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
     int exact = 0;
     if (lane == 0) {
-        atomicAdd(&P.flags[0].nnz_proc, (unsigned long long)(e - b));
-        if (t == t0) atomicAdd(&P.flags[0].rows_proc, 1ULL);
+        ws.st_nnz += (unsigned long long)(e - b);
+        if (t == t0) ws.st_rows += 1ULL;
         if (single) {
             exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
-            if (exact) atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)(e - b));
+            if (exact) ws.st_exact += (unsigned long long)(e - b);
         } else {
             TileScr ts;
             ts.mn_lo = c.mn_lo; ts.mn_hi = c.mn_hi; ts.mx_lo = c.mx_lo; ts.mx_hi = c.mx_hi;
@@ -553,7 +616,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     if (!single) return true;
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const Acc s = tile_exact(P, b, e, lane);
-    split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, qbuf);
+    split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, ws);
     return false;
 }
 
@@ -563,7 +626,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
 // exact FP64 partial, and its first tile flags the row for the exact phase
 // (returns true when the tile computed its exact partial).
 __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane, int round, bool marked,
-                                           int *exact_ctr) {
+                                           int *exact_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
     if (marked && P.mark[P.n_srows + row] != round) return false;
     const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
@@ -586,7 +649,7 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
         TilePart tp;
         tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf; tp.U = s.U; tp.pad = 0;
         P.tile_part[t] = tp;
-        atomicAdd(&P.flags[0].nnz_exact, (unsigned long long)(e - b));
+        ws.st_exact += (unsigned long long)(e - b);
         if (t == t0) {
             P.row_exact[row] = round;
             atomicAdd(exact_ctr, 1);
@@ -598,7 +661,7 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
 // Exact phase, tile t of a multi-tile row flagged this round: the row's exact
 // partials combined in tile order, then the decision and this tile's candidates.
 __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane, int round, int *change,
-                                            unsigned *tight_ctr, unsigned *qbuf) {
+                                            unsigned *tight_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
     if (P.row_exact[row] != round) return;
     // lanes load 32 partials at a time; lane 0 folds them in tile order
@@ -616,12 +679,21 @@ __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane
             o.minf = __shfl_sync(kFull, p.minf, i);
             o.maxf = __shfl_sync(kFull, p.maxf, i);
             o.U = __shfl_sync(kFull, p.U, i);
-            o.L = 0.0f;
-            if (b + i == t0) s = o;
-            else acc_combine(s, o);
+            if (lane == 0) {
+                if (b + i == t0) s = o;
+                else acc_combine(s, o);
+            }
         }
     }
-    split_row_candidates(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, qbuf);
+    split_row_candidates(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, ws);
+}
+
+// Adds a thread's committed-change count to the round flags, one atomic per warp.
+__device__ __forceinline__ void flush_changed(const DevProblem &P, unsigned long long changed) {
+    const unsigned active = __activemask();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) changed += __shfl_down_sync(active, changed, off);
+    if ((threadIdx.x & 31) == __ffs(active) - 1 && changed) atomicAdd(&P.flags[0].changed_vars, changed);
 }
 
 // Commit changed variables nxt -> cur, apply the infeasibility rule, mark the
@@ -648,7 +720,7 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
                     P.mark[__ldg(P.var_pos + p)] = round + 1;
         }
     }
-    if (changed) atomicAdd(&P.flags[0].changed_vars, changed);
+    flush_changed(P, changed);
 }
 
 // ---- work distribution ----------------------------------------------------
@@ -662,31 +734,39 @@ __device__ __forceinline__ int warp_next(unsigned *ctr, int lane) {
 __device__ __forceinline__ void activity_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
                                                int *change, unsigned *tight_ctr, WarpSmem &ws, int lane,
                                                int par = 0) {
+    stats_zero(ws, lane);
+    WarpCursor cur;
+    cur.start(ctr, 1u, lane);
     for (;;) {
-        const int i = warp_next(ctr, lane);
+        const int i = cur.next(lane);
         if (i >= P.n_items) break;
         const int it = __ldg(P.items + i);
         if (it >= 0) sell_slice(P, it, lane, round, marked, change, tight_ctr, ws, par);
-        else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws.q);
+        else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws);
     }
+    stats_flush(P, ws, lane);
 }
 
 __device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
-                                                int *exact_ctr, int lane) {
+                                                int *exact_ctr, WarpSmem &ws, int lane) {
+    stats_zero(ws, lane);
     for (;;) {
         const int i = warp_next(ctr, lane);
         if (i >= P.n_mtiles) break;
-        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, exact_ctr);
+        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, exact_ctr, ws);
     }
+    stats_flush(P, ws, lane);
 }
 
 __device__ __forceinline__ void exact_phase(const DevProblem &P, int round, unsigned *ctr, int *change,
                                             unsigned *tight_ctr, WarpSmem &ws, int lane) {
+    stats_zero(ws, lane);
     for (;;) {
         const int i = warp_next(ctr, lane);
         if (i >= P.n_mtiles) break;
-        split_exact(P, __ldg(P.mtiles + i), lane, round, change, tight_ctr, ws.q);
+        split_exact(P, __ldg(P.mtiles + i), lane, round, change, tight_ctr, ws);
     }
+    stats_flush(P, ws, lane);
 }
 
 // Whether the activity phase of this round's parity queued exact rows.

@@ -36,6 +36,13 @@ class GDPError(RuntimeError):
     pass
 
 
+class MpsProblem(C.Structure):
+    _fields_ = [("n_cons", C.c_int), ("n_vars", C.c_int), ("nnz", C.c_int),
+                ("row_ptr", C.POINTER(C.c_int)), ("col", C.POINTER(C.c_int)),
+                ("val", C.POINTER(C.c_double)), ("lhs", C.POINTER(C.c_double)), ("rhs", C.POINTER(C.c_double)),
+                ("lb", C.POINTER(C.c_double)), ("ub", C.POINTER(C.c_double)), ("vartype", C.POINTER(C.c_int))]
+
+
 class TuneTrial(C.Structure):
     _fields_ = [("thread_row_max", C.c_int), ("split_tile", C.c_int), ("sync_type", C.c_int),
                 ("ctas_per_sm", C.c_int), ("rounds", C.c_int), ("pad_", C.c_int), ("ms", C.c_double)]
@@ -72,6 +79,9 @@ class Stats(C.Structure):
         ("rows_deferred", C.c_longlong),
         ("full_rounds", C.c_int),
         ("pad_", C.c_int),
+        ("divisions", C.c_longlong),
+        ("rows_exact", C.c_longlong),
+        ("rows_go", C.c_longlong),
     ]
 
     def as_dict(self) -> dict:
@@ -134,6 +144,10 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
                                                     C.POINTER(Options), C.POINTER(C.c_double),
                                                     C.POINTER(TuneTrial), C.c_int, C.POINTER(C.c_int)]
     lib.gdp_autotune.restype = C.c_int
+    lib.gdp_mps_parse.argtypes = [C.c_char_p, C.c_longlong, C.POINTER(MpsProblem)]
+    lib.gdp_mps_parse.restype = C.c_int
+    lib.gdp_mps_free.argtypes = [C.POINTER(MpsProblem)]
+    lib.gdp_mps_free.restype = None
     lib.gdp_context_trace.argtypes = [C.c_void_p, _P_DBL, _P_DBL, C.c_int, _P_F, _P_F, C.POINTER(C.c_int),
                                       C.POINTER(Stats)]
     for name in ("gdp_mlp_create", "gdp_mlp_destroy", "gdp_mlp_get_params", "gdp_mlp_set_params",
@@ -309,6 +323,30 @@ class Context:
         return st.as_dict()
 
 
+def parse_mps(text: bytes) -> MIP:
+    """gdp_mps_parse on MPS text: a MIP in the reference's CSR convention."""
+    lib = load_library()
+    out = MpsProblem()
+    _check(lib.gdp_mps_parse(text, len(text), C.byref(out)), "gdp_mps_parse")
+    try:
+        def arr(ptr, cnt, dt):
+            return np.ctypeslib.as_array(ptr, shape=(max(cnt, 1),))[:cnt].astype(dt, copy=True)
+        m, n, nnz = out.n_cons, out.n_vars, out.nnz
+        return MIP(arr(out.row_ptr, m + 1, np.int32), arr(out.col, nnz, np.int32), arr(out.val, nnz, np.float64),
+                   arr(out.lhs, m, np.float64), arr(out.rhs, m, np.float64), arr(out.lb, n, np.float64),
+                   arr(out.ub, n, np.float64), arr(out.vartype, n, np.int32))
+    finally:
+        lib.gdp_mps_free(C.byref(out))
+
+
+def read_mps(path) -> MIP:
+    """Reads an .mps or .mps.gz file."""
+    import gzip
+    p = os.fspath(path)
+    data = gzip.open(p, "rb").read() if p.endswith(".gz") else open(p, "rb").read()
+    return parse_mps(data)
+
+
 def autotune(mip: MIP, repeats: int = 2, max_rounds: int = 0, use_marking: int = -1):
     """gdp_autotune: the fastest (thread_row_max, split_tile, sync_type,
     ctas_per_sm) for `mip`. Returns (options dict, best ms, list of trials)."""
@@ -339,10 +377,18 @@ class Batch:
 
     @classmethod
     def instances(cls, mips, max_rounds: int = 0, thread_row_max: int = 0, split_tile: int = 0,
-                  use_marking: int = -1) -> "Batch":
+                  use_marking: int = -1, ctas_per_sm: int = 0, autotune: bool = False) -> "Batch":
+        """autotune: pick thread_row_max, split_tile and ctas_per_sm with
+        gdp_autotune on the largest member (its schedule applies to the batch loop)."""
         lib = load_library()
         ps = [m.normalized() for m in mips]
         k = len(ps)
+        tuned = None
+        if autotune and ps:
+            big = max(ps, key=lambda p: p.nnz)
+            tuned, _, _ = globals()["autotune"](big, repeats=1, max_rounds=max_rounds, use_marking=use_marking)
+            thread_row_max, split_tile = tuned["thread_row_max"], tuned["split_tile"]
+            ctas_per_sm = tuned["ctas_per_sm"]
         arr_i = lambda xs: (C.c_int * k)(*xs)
         col = (_P_INT * k)(*[_pi(p.col) for p in ps])
         rp = (_P_INT * k)(*[_pi(p.row_ptr) for p in ps])
@@ -351,13 +397,14 @@ class Batch:
         rhs = (_P_DBL * k)(*[_pd(p.rhs) for p in ps])
         vt = (_P_INT * k)(*[_pi(p.vartype) for p in ps])
         o = default_options(max_rounds=max_rounds, thread_row_max=thread_row_max, split_tile=split_tile,
-                            use_marking=use_marking)
+                            use_marking=use_marking, ctas_per_sm=ctas_per_sm)
         h = C.c_void_p()
         rc = lib.gdp_batch_create(k, arr_i([p.m for p in ps]), arr_i([p.n for p in ps]),
                                   arr_i([p.nnz for p in ps]), col, rp, val, lhs, rhs, vt, C.byref(o), C.byref(h))
         _check(rc, "gdp_batch_create")
         b = cls(h, lib, [p.n for p in ps], keep=ps)
         b.mips = ps
+        b.tuned = tuned
         return b
 
     @classmethod

@@ -63,6 +63,9 @@ typedef struct {
     long long rows_deferred; /* learned marking: marked rows the model left for a later round */
     int full_rounds;        /* learned marking: rounds that swept every row (incl. the certification) */
     int pad_;
+    long long divisions;    /* bound candidates computed (one FP64 division each), summed over rounds */
+    long long rows_exact;   /* rows up to split_tile non-zeros that went through the exact FP64 pass */
+    long long rows_go;      /* ... of which passed the row test (candidates computed) */
 } gdp_stats;
 
 /* Fills *opts with the defaults. */
@@ -218,6 +221,25 @@ GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *csr_col_ind
                          const double *ubs, const int *vartypes, const gdp_options *base, int repeats,
                          gdp_options *best, double *best_ms, gdp_tune_trial *trials, int max_trials,
                          int *n_trials);
+
+/* ---- MPS reader (no counterpart in the reference, which reads MPS through
+ * python-mip, fileReader/readerInterface.py:52-145) ---------------------------
+ * Parses free-format MPS text (decompress .gz first) into the reference's CSR
+ * convention: constraint rows in ROWS order (objective rows dropped), entries
+ * of a row in column order, lhs/rhs with infinite sides as +-inf, bounds
+ * (default [0, +inf); UP < 0 with an untouched lower bound 0 gives lb = -inf),
+ * RANGES per the MPS standard, SCIP variable types (integer from MARKER
+ * INTORG/INTEND blocks or LI/UI/BV bounds; integer with bounds [0, 1] is
+ * binary). The arrays are malloc'ed by the library; release them with
+ * gdp_mps_free. */
+typedef struct {
+    int n_cons, n_vars, nnz;
+    int *row_ptr, *col;
+    double *val, *lhs, *rhs, *lb, *ub;
+    int *vartype;
+} gdp_mps_problem;
+GDP_RETCODE gdp_mps_parse(const char *text, long long len, gdp_mps_problem *out);
+void gdp_mps_free(gdp_mps_problem *p);
 
 /* Propagation that allocates no memory, for callers that cannot call
  * cudaMalloc (e.g. a solver or framework whose device memory belongs to its

@@ -18,7 +18,7 @@ def _declared_symbols():
     for h in (ROOT / "include").glob("*.h"):
         text = h.read_text()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"^\s*(?:GDP_RETCODE|const char \*|int)\s+\*?(\w+)\s*\(", text, flags=re.M):
+        for m in re.finditer(r"^\s*(?:GDP_RETCODE|const char \*|int|void)\s+\*?(\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
