@@ -97,12 +97,22 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     // features (trace rounds and learned marked rounds)
     const bool logged = P.learned == 2 && !full;
     const bool select = P.learned == 1 && kind == kRoundLearned;
+    __nv_bfloat16 (*feat)[16] = reinterpret_cast<__nv_bfloat16 (*)[16]>(ws.q);
+    unsigned trace_idx = 0xffffffffu;
     if (logged || select) {
         if (leader0) {
             float v[16];
             row_features(P, r, round, len, lhs, rhs, v);
 #pragma unroll
-            for (int k = 0; k < 16; k++) L.feat[rl][k] = __float2bfloat16_rn(v[k]);
+            for (int k = 0; k < 16; k++) feat[rl][k] = __float2bfloat16_rn(v[k]);
+            if (logged) {  // trace rounds process every marked row: log its features now
+                trace_idx = atomicAdd(P.trace_n, 1u);
+                if (trace_idx < P.trace_cap) {
+#pragma unroll
+                    for (int k = 0; k < 16; k++)
+                        P.trace_x[(size_t)trace_idx * 16 + k] = __bfloat162float(feat[rl][k]);
+                }
+            }
         }
         __syncwarp();
     }
@@ -110,7 +120,7 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
         const int ntiles = ((32 >> lg) + 15) >> 4;
         for (int tile = 0; tile < ntiles; tile++) {
             unsigned a[4];
-            load_a_smem(&L.feat[tile * 16][0], lane, a);
+            load_a_smem(&feat[tile * 16][0], lane, a);
             float z0, z1;
             mlp_infer_tile(P.mlp, a, lane, z0, z1);
             if ((lane & 3) == 0) {
@@ -166,14 +176,7 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     __syncwarp();
     if (leader) {
         const bool tightened = L.tight[rl] > 0;
-        if (logged) {
-            const unsigned idx = atomicAdd(P.trace_n, 1u);
-            if (idx < P.trace_cap) {
-#pragma unroll
-                for (int k = 0; k < 16; k++) P.trace_x[(size_t)idx * 16 + k] = __bfloat162float(L.feat[rl][k]);
-                P.trace_y[idx] = tightened ? 1.f : 0.f;
-            }
-        }
+        if (logged && trace_idx < P.trace_cap) P.trace_y[trace_idx] = tightened ? 1.f : 0.f;
         const unsigned old = P.rinfo[r];
         const unsigned streak = tightened ? 0u : min(((old >> kRowInfoStreakShift) & 255u) + 1u, 255u);
         P.rinfo[r] = (unsigned)min(c.minf, 3) | ((unsigned)min(c.maxf, 3) << 2) | ((exact ? 1u : 0u) << 4) |

@@ -110,8 +110,9 @@ __device__ __forceinline__ int candidate_sides(const RowC &c, double a, double l
 
 // One candidate (side 0: upper, 1: lower) of variable j; applies it with an
 // FP64 atomic if EPS-better than the snapshot. Returns true if it tightened.
-__device__ __forceinline__ bool apply_side(const DevProblem &P, const RowC &c, int j, double a, int side) {
-    const double2 b = load_bnd(P, j);
+// b: the variable's round-start bounds (read-only during the round).
+__device__ __forceinline__ bool apply_side(const DevProblem &P, const RowC &c, int j, double a, double2 b,
+                                           int side) {
     const bool pos = gt0_bits(dbits(a));
     const bool cont = __ldg(P.is_cont + j) != 0;
     if (side == 0) {
@@ -139,10 +140,17 @@ __device__ __forceinline__ bool apply_side(const DevProblem &P, const RowC &c, i
 }
 
 // ---- warp division queue --------------------------------------------------
-// Items are 32-bit codes; the caller decodes them. push() appends each lane's
-// items (ballot + prefix), drain() runs full batches of 32.
+// A queued candidate side carries its variable and its position (element
+// index, owner lane, side), so draining it reloads the coefficient and the
+// bounds with two independent loads (no column -> bound chain). push()
+// appends each lane's sides (ballot + prefix), drain() runs batches of 32.
+struct QEntry {  // 8 bytes
+    int j;
+    unsigned code;  // bit 0: side (0 upper, 1 lower); bits 1..5: owner lane; bits 6..: element step
+};
+
 struct WarpQueue {
-    unsigned *q;
+    QEntry *q;
     int cnt;     // warp-uniform
     int pushed;  // warp-uniform: candidate sides queued (each one division)
 };
@@ -160,12 +168,12 @@ __device__ __forceinline__ void queue_drain(WarpQueue &Q, int lane, bool all, Ru
     }
 }
 
-__device__ __forceinline__ void queue_push(WarpQueue &Q, int lane, int sides, unsigned code_base) {
+__device__ __forceinline__ void queue_push(WarpQueue &Q, int lane, int sides, int j, unsigned code_base) {
     const unsigned bu = __ballot_sync(kFull, sides & 1);
     const unsigned bl = __ballot_sync(kFull, sides & 2);
     const unsigned lt = (1u << lane) - 1u;
-    if (sides & 1) Q.q[Q.cnt + __popc(bu & lt)] = code_base | 0u;
-    if (sides & 2) Q.q[Q.cnt + __popc(bu) + __popc(bl & lt)] = code_base | 1u;
+    if (sides & 1) Q.q[Q.cnt + __popc(bu & lt)] = QEntry{j, code_base};
+    if (sides & 2) Q.q[Q.cnt + __popc(bu) + __popc(bl & lt)] = QEntry{j, code_base | 1u};
     __syncwarp();
     Q.cnt += __popc(bu) + __popc(bl);
     Q.pushed += __popc(bu) + __popc(bl);
@@ -184,7 +192,7 @@ __device__ __forceinline__ void report_tight(int tight, int lane, int *change, u
 // ---- SELL-g rows: one warp per slice, g lanes per row ----------------------
 struct WarpSmem {
     RowC rc[32];
-    unsigned q[kQueueCap];
+    QEntry q[kQueueCap];
     long long base[32];  // deferred exact pass: first element of each lane
     // work statistics of this warp, written by lane 0 and flushed to the
     // round flags once per phase (not once per item: same-address atomics
@@ -231,9 +239,10 @@ struct WarpCursor {
     }
 };
 
-// Learned marking: features, scores and per-row outcomes of one slice.
+// Learned marking: scores and per-row outcomes of one slice (the features
+// of the slice's rows live in the warp's division-queue storage, which is
+// free until the exact pass).
 struct LearnSmem {
-    __nv_bfloat16 feat[32][16];
     float z[32];
     int tight[32];
     int go[32];
@@ -354,29 +363,37 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
         if (leader && dec == 1) ws.rc[rl] = make_rowc(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs);
         __syncwarp();
         WarpQueue Q{ws.q, 0, 0};
-        auto run = [&](unsigned code) {
-            const int owner = (code >> 1) & 31;
-            const int i = (int)(code >> 6);
-            const long long e = ws.base[owner] + 32LL * i;
-            const int j = __ldg(P.sell_col + e);
-            const double a = __ldg(P.sell_val + e);
-            if (apply_side(P, ws.rc[owner >> lg], j, a, (int)(code & 1u))) {
+        auto run = [&](const QEntry &q) {
+            const int owner = (q.code >> 1) & 31;
+            const int slot = owner >> lg;
+            const double a = __ldg(P.sell_val + ws.base[owner] + 32LL * (int)(q.code >> 6));
+            if (apply_side(P, ws.rc[slot], q.j, a, load_bnd(P, q.j), (int)(q.code & 1u))) {
                 tight++;
-                if (row_tight) atomicAdd(row_tight + (owner >> lg), 1);
+                if (row_tight) atomicAdd(row_tight + slot, 1);
             }
         };
         int maxcnt = go ? cnt : 0;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) maxcnt = max(maxcnt, __shfl_xor_sync(kFull, maxcnt, off));
+        // software pipeline: element i + 2's column and coefficient and
+        // element i + 1's bounds are in flight while element i is tested
+        const int ce = go ? cnt : 0;
+        int j1 = 0, j2 = 0;
+        double a1 = 0.0, a2 = 0.0;
+        double2 b1 = make_double2(0.0, 0.0);
+        if (ce > 0) { j1 = __ldg(col); a1 = __ldg(val); }
+        if (ce > 1) { j2 = __ldg(col + 32); a2 = __ldg(val + 32); }
+        if (ce > 0) b1 = load_bnd(P, j1);
         for (int i = 0; i < maxcnt; i++) {
-            int sides = 0;
-            if (go && i < cnt) {
-                const int j = __ldg(col + 32 * i);
-                const double a = __ldg(val + 32 * i);
-                const double2 b = load_bnd(P, j);
-                sides = candidate_sides(ws.rc[rl], a, b.x, b.y);
-            }
-            queue_push(Q, lane, sides, ((unsigned)i << 6) | ((unsigned)lane << 1));
+            const int j = j1;
+            const double a = a1;
+            const double2 b = b1;
+            j1 = j2;
+            a1 = a2;
+            if (i + 2 < ce) { j2 = __ldg(col + 32 * (i + 2)); a2 = __ldg(val + 32 * (i + 2)); }
+            if (i + 1 < ce) b1 = load_bnd(P, j1);
+            const int sides = i < ce ? candidate_sides(ws.rc[rl], a, b.x, b.y) : 0;
+            queue_push(Q, lane, sides, j, ((unsigned)i << 6) | ((unsigned)lane << 1));
             queue_drain(Q, lane, false, run);
         }
         queue_drain(Q, lane, true, run);
@@ -525,20 +542,29 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
     c.nsur_hi = __shfl_sync(kFull, c.nsur_hi, 0);
     int tight = 0;
     WarpQueue Q{ws.q, 0, 0};
-    auto run = [&](unsigned code) {
-        const int k = b + (int)(code >> 1);
-        tight += apply_side(P, c, __ldg(P.lcol + k), __ldg(P.lval + k), (int)(code & 1u)) ? 1 : 0;
+    auto run = [&](const QEntry &q) {
+        const double a = __ldg(P.lval + b + (int)(q.code >> 1));
+        tight += apply_side(P, c, q.j, a, load_bnd(P, q.j), (int)(q.code & 1u)) ? 1 : 0;
     };
+    // software pipeline as in sell_rows_exact: two steps of columns and
+    // coefficients, one step of bounds ahead
+    int j1 = 0, j2 = 0;
+    double a1 = 0.0, a2 = 0.0;
+    double2 b1 = make_double2(0.0, 0.0);
+    if (b + lane < e) { j1 = __ldg(P.lcol + b + lane); a1 = __ldg(P.lval + b + lane); }
+    if (b + 32 + lane < e) { j2 = __ldg(P.lcol + b + 32 + lane); a2 = __ldg(P.lval + b + 32 + lane); }
+    if (b + lane < e) b1 = load_bnd(P, j1);
     for (int k0 = b; k0 < e; k0 += 32) {
         const int k = k0 + lane;
-        int sides = 0;
-        if (k < e) {
-            const int j = __ldg(P.lcol + k);
-            const double a = __ldg(P.lval + k);
-            const double2 bb = load_bnd(P, j);
-            sides = candidate_sides(c, a, bb.x, bb.y);
-        }
-        queue_push(Q, lane, sides, (unsigned)(k - b) << 1);
+        const int j = j1;
+        const double a = a1;
+        const double2 bb = b1;
+        j1 = j2;
+        a1 = a2;
+        if (k + 64 < e) { j2 = __ldg(P.lcol + k + 64); a2 = __ldg(P.lval + k + 64); }
+        if (k + 32 < e) b1 = load_bnd(P, j1);
+        const int sides = k < e ? candidate_sides(c, a, bb.x, bb.y) : 0;
+        queue_push(Q, lane, sides, j, (unsigned)(k - b) << 1);
         queue_drain(Q, lane, false, run);
     }
     queue_drain(Q, lane, true, run);
