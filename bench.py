@@ -265,16 +265,19 @@ def run_batched(args, ws, rank, local):
     t0 = time.perf_counter()
     mip, mips = _batch_members(args)
     gen_s = time.perf_counter() - t0
+    # chains of up to 5,000 links take up to that many Jacobi rounds to reach
+    # their fixpoint: the chain workload's default cap lets every member certify
+    max_rounds = args.max_rounds or (10_000 if args.workload == "chains" else 0)
     t0 = time.perf_counter()
     if args.workload == "nodes":
-        ctx = gdp.Context(mip, sync_type=gdp.MEGAKERNEL)
+        ctx = gdp.Context(mip, sync_type=gdp.MEGAKERNEL, max_rounds=max_rounds)
         rlb, rub, rst = ctx.propagate()
         members = _node_bounds(mip, rlb, rub, args.members or 256, seed=5)
         batch = gdp.Batch.nodes(ctx, len(members[0]))
         plain_mips = [mip] * len(members[0])
         sizes = {"m": mip.m, "n": mip.n, "nnz": mip.nnz, "root_rounds": rst["rounds"]}
     else:
-        batch = gdp.Batch.instances(mips, autotune=args.autotune)
+        batch = gdp.Batch.instances(mips, autotune=args.autotune, max_rounds=max_rounds)
         members = ([m.lb for m in mips], [m.ub for m in mips])
         plain_mips = mips
         sizes = {"members": len(mips), "m_total": int(sum(m.m for m in mips)),
@@ -300,7 +303,7 @@ def run_batched(args, ws, rank, local):
         for k, pm in enumerate(plain_mips):
             key = id(pm)
             if key not in ctxs:
-                ctxs[key] = gdp.Context(pm, sync_type=gdp.MEGAKERNEL, use_marking=marking)
+                ctxs[key] = gdp.Context(pm, sync_type=gdp.MEGAKERNEL, use_marking=marking, max_rounds=max_rounds)
             c = ctxs[key]
             d_lb = torch.tensor(members[0][k], dtype=torch.float64, device="cuda")
             d_ub = torch.tensor(members[1][k], dtype=torch.float64, device="cuda")
@@ -321,7 +324,9 @@ def run_batched(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": BATCH_WORKLOADS[args.workload], **sizes, "scale": args.scale,
+                       "max_rounds": max_rounds or 100,
                        "batch_rounds": tot["rounds"], "infeasible_members": tot["infeasible"],
+                       "converged_members": int(sum(bool(s["converged"]) for s in sts)),
                        "rows_processed": tot["rows_processed"], "nnz_processed": tot["nnz_processed"],
                        "nnz_exact": tot["nnz_exact"], "graph": batch.uses_graph, "parallelism": "single",
                        "autotune": getattr(batch, "tuned", None)},

@@ -100,13 +100,14 @@ GDP_RETCODE Batch::init_nodes(Context *ctx, int n_nodes) {
         DevProblem &Q = units_h_[u];
         Q.bnd = (double2 *)arena_.alloc_bytes(sizeof(double2) * (size_t)n);
         Q.bnd_nxt = (double2 *)arena_.alloc_bytes(sizeof(double2) * (size_t)n);
+        Q.bnd32 = (float2 *)arena_.alloc_bytes(sizeof(float2) * (size_t)n);
         Q.chg = (unsigned *)arena_.alloc_bytes(sizeof(unsigned) * (size_t)std::max(S.n_chg_words, 1));
         Q.mark = (int *)arena_.alloc_bytes(sizeof(int) * (size_t)npos);
         Q.slice_stamp = (int *)arena_.alloc_bytes(sizeof(int) * (size_t)std::max(S.n_slices, 1));
         Q.tile_part = (TilePart *)arena_.alloc_bytes(sizeof(TilePart) * (size_t)std::max(S.n_tiles, 1));
         Q.tile_scr = (TileScr *)arena_.alloc_bytes(sizeof(TileScr) * (size_t)std::max(S.n_tiles, 1));
         Q.row_exact = (int *)arena_.alloc_bytes(sizeof(int) * (size_t)std::max(S.n_lrows, 1));
-        if (!Q.bnd || !Q.bnd_nxt || !Q.chg || !Q.mark || !Q.slice_stamp || !Q.tile_part || !Q.tile_scr ||
+        if (!Q.bnd || !Q.bnd_nxt || !Q.bnd32 || !Q.chg || !Q.mark || !Q.slice_stamp || !Q.tile_part || !Q.tile_scr ||
             !Q.row_exact) {
             set_error("device allocation failed (node state)");
             return GDP_ERROR;

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "gdp_context.h"
+#include "gdp_device.cuh"
 #include "gdp_learned.h"
 
 namespace gdp {
@@ -164,6 +165,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     sell_elems = slice_ptr[n_slices];
     std::vector<int> sell_col((size_t)std::max<long long>(sell_elems, 1), 0);
     std::vector<double> sell_val((size_t)std::max<long long>(sell_elems, 1), 0.0);
+    std::vector<float> sell_a32((size_t)std::max<long long>(sell_elems, 1), 0.0f);
     std::vector<int> srow_len(std::max(ns, 1));
     std::vector<double> srow_lhs(std::max(ns, 1)), srow_rhs(std::max(ns, 1));
 #pragma omp parallel for schedule(dynamic, 64)
@@ -178,6 +180,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
                 const long long e = slice_ptr[s] + 32LL * (k >> lg) + (rl << lg) + (k & (g - 1));
                 sell_col[e] = col[row_ptr[i] + k];
                 sell_val[e] = val[row_ptr[i] + k];
+                sell_a32[e] = coef_screen(sell_val[e]);
             }
         }
     }
@@ -204,11 +207,13 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     const long long lnnz = lrow_ptr[n_lrows];
     std::vector<int> lcol((size_t)std::max<long long>(lnnz, 1));
     std::vector<double> lval((size_t)std::max<long long>(lnnz, 1));
+    std::vector<float> la32((size_t)std::max<long long>(lnnz, 1), 0.0f);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int r = 0; r < n_lrows; r++) {
         const int i = split_rows[r];
         std::memcpy(&lcol[lrow_ptr[r]], &col[row_ptr[i]], sizeof(int) * (size_t)len[i]);
         std::memcpy(&lval[lrow_ptr[r]], &val[row_ptr[i]], sizeof(double) * (size_t)len[i]);
+        for (int k = 0; k < len[i]; k++) la32[lrow_ptr[r] + k] = coef_screen(val[row_ptr[i] + k]);
     }
     // work items of the activity phase, heaviest first (slices: 32 x width non-zeros)
     std::vector<int> items;
@@ -246,6 +251,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.slice_lg, const int, slice_lg);
     GDP_UP(P.sell_col, const int, sell_col);
     GDP_UP(P.sell_val, const double, sell_val);
+    GDP_UP(P.sell_a32, const float, sell_a32);
     GDP_UP(P.srow_len, const int, srow_len);
     {
         std::vector<int> pos_slice(std::max(ns, 1), 0);
@@ -259,6 +265,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.n_tiles = n_tiles;
     GDP_UP(P.lcol, const int, lcol);
     GDP_UP(P.lval, const double, lval);
+    GDP_UP(P.la32, const float, la32);
     GDP_UP(P.lrow_lhs, const double, lrow_lhs);
     GDP_UP(P.lrow_rhs, const double, lrow_rhs);
     GDP_UP(P.lrow_tile0, const int, lrow_tile0);
@@ -298,6 +305,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);
     P.bnd = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
     P.bnd_nxt = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
+    P.bnd32 = (float2 *)arena.alloc_bytes(sizeof(float2) * (size_t)std::max(n, 1));
     P.chg = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * (size_t)std::max(n_words, 1));
     P.n_chg_words = n_words;
     P.flags = (RoundFlags *)arena.alloc_bytes(sizeof(RoundFlags) * 3);
@@ -306,7 +314,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.max_rounds = opts.max_rounds;
     d_lb = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     d_ub = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.xrow || !P.xctr || !P.mark || !P.bnd || !P.bnd_nxt || !P.chg || !P.flags || !P.barrier || !P.queue ||
+    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.xrow || !P.xctr || !P.mark || !P.bnd || !P.bnd_nxt || !P.bnd32 || !P.chg || !P.flags || !P.barrier || !P.queue ||
         !d_lb || !d_ub) {
         set_error("device allocation failed");
         return GDP_ERROR;

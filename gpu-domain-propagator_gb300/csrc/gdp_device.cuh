@@ -307,83 +307,131 @@ __device__ __forceinline__ MagEnc mag_enc(long long bits) {
     return e;
 }
 
-// Screen accumulator: [mn_lo, mn_hi] and [mx_lo, mx_hi] enclose the exact sums
-// of the finite activity terms (each term enclosed with directed rounding);
-// S >= sum of the terms' magnitudes bounds the FP64 summation error.
+// The screen reads FP32 copies of the data (4 B per coefficient, 8 B per
+// bound pair instead of 8 B and 16 B) that are made once: coefficients when
+// the layout is built, bounds when a variable changes. Each copy is the
+// round-to-nearest float, with these exceptions:
+//  * a bound the reference counts as infinite (lb <= -1e20, ub >= 1e20) is
+//    -inf / +inf, so the screen's infinity counts are the reference's;
+//  * a finite bound above 2^100 in magnitude is NaN;
+//  * a coefficient in (0, 1e-9] is NaN (the reference classifies it as
+//    non-positive but sums it as positive), one above 2^40 in magnitude is
+//    +-inf, and a non-zero one below 2^-60 in magnitude is NaN.
+// NaN or inf terms make the screen's sums, magnitude sum or U NaN or inf,
+// and every such row is left to the exact pass; the sign test a32 > 0 equals
+// the reference's EPSGT(a, 0) for every coefficient.
+constexpr float kF32Inf = __builtin_huge_valf();
+__host__ __device__ __forceinline__ float coef_screen(double a) {
+    const double m = a < 0 ? -a : a;
+    if (a > 0.0 && a <= kEps) return __builtin_nanf("");
+    if (m > 0x1p40) return a > 0 ? kF32Inf : -kF32Inf;
+    if (m != 0.0 && m < 0x1p-60) return __builtin_nanf("");
+    return (float)a;
+}
+constexpr long long kBits2p100 = 0x4630000000000000LL;  // 2^100
+__device__ __forceinline__ float2 bnd_screen(double2 b) {
+    const long long lb = dbits(b.x), ub = dbits(b.y);
+    float2 r;
+    r.x = neginf_bits(lb) ? -kF32Inf
+          : (lb & 0x7FFFFFFFFFFFFFFFLL) > kBits2p100 ? __int_as_float(0x7FC00000) : __double2float_rn(b.x);
+    r.y = posinf_bits(ub) ? kF32Inf
+          : (ub & 0x7FFFFFFFFFFFFFFFLL) > kBits2p100 ? __int_as_float(0x7FC00000) : __double2float_rn(b.y);
+    return r;
+}
+
+// max / min that return NaN when either operand is NaN (fmaxf drops it).
+__device__ __forceinline__ float fmax_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float fmin_nan(float a, float b) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+// Screen accumulator over the FP32 copies: mn / mx are round-to-nearest sums
+// of the finite activity terms t = fl(a32 * b32), S >= the sum of their
+// magnitudes (rounded upwards), U >= every |a| (ub - lb) up to a relative
+// 2^-20 (see scr_u_bound), minf / maxf the reference's infinity counts.
+//
+// Error bound of the sums (Higham, Accuracy and Stability of Numerical
+// Algorithms, 2nd ed., 3.1 and 4.2): each copy carries a relative error of
+// at most u = 2^-24 and the product one more, so |t - a b| <= gamma_3 |t| /
+// (1 - gamma_3); any summation order of n terms adds at most gamma_{n-1}
+// sum |t|; the FP64 sums the exact pass computes (any order) are within
+// gamma_n^(64) sum |a b| of the real sum. Together, for n <= 2^16,
+// |minact_FP64 - mn| <= (n + 4) u (1 + 2^-6) S, and for n <= 2^20 with the
+// factor 1.125; values below 2^-126 contribute absolute errors under 2^-80
+// in total (|a32| <= 2^40). Rows longer than 2^20 are never skipped.
 struct Scr {
-    float mn_lo, mn_hi, mx_lo, mx_hi, S, U;
+    float mn, mx, S, U;
     int minf, maxf;
 };
 __device__ __forceinline__ void scr_init(Scr &c) {
-    c.mn_lo = 0.0f; c.mn_hi = 0.0f; c.mx_lo = 0.0f; c.mx_hi = 0.0f; c.S = 0.0f; c.U = 0.0f;
+    c.mn = 0.0f; c.mx = 0.0f; c.S = 0.0f; c.U = 0.0f;
     c.minf = 0; c.maxf = 0;
 }
-__device__ __forceinline__ void scr_add(Scr &c, long long ab, long long lbb, long long ubb) {
-    const bool pos = gt_eps_bits(ab);
-    const bool lneg = neginf_bits(lbb), upos = posinf_bits(ubb);
-    const bool min_inf = pos ? lneg : upos;
-    const bool max_inf = pos ? upos : lneg;
-    c.minf += min_inf;
-    c.maxf += max_inf;
-    const MagEnc A = mag_enc(ab), L = mag_enc(lbb), Ub = mag_enc(ubb);
-    const bool lsg = lbb < 0, usg = ubb < 0, asg = ab < 0;
-    // U' >= delta_up(a, lb, ub): every operand rounded no closer to zero
-    const float ub_hi = usg ? -Ub.dn : Ub.up, lb_lo = lsg ? -L.up : L.dn;
-    c.U = fmaxf(c.U, __fmul_rn(A.up, __fsub_rn(ub_hi, lb_lo)));
-    const bool gt0 = gt0_bits(ab);
-    // min term a * (gt0 ? lb : ub), max term a * (gt0 ? ub : lb)
-    const MagEnc bmin = gt0 ? L : Ub, bmax = gt0 ? Ub : L;
-    const bool smin = asg != (gt0 ? lsg : usg), smax = asg != (gt0 ? usg : lsg);
-    if (!min_inf) {
-        const float lo = __fmul_rd(A.dn, bmin.dn), hi = __fmul_ru(A.up, bmin.up);
-        c.mn_lo = __fadd_rd(c.mn_lo, smin ? -hi : lo);
-        c.mn_hi = __fadd_ru(c.mn_hi, smin ? -lo : hi);
-        c.S = __fadd_ru(c.S, hi);
-    }
-    if (!max_inf) {
-        const float lo = __fmul_rd(A.dn, bmax.dn), hi = __fmul_ru(A.up, bmax.up);
-        c.mx_lo = __fadd_rd(c.mx_lo, smax ? -hi : lo);
-        c.mx_hi = __fadd_ru(c.mx_hi, smax ? -lo : hi);
-        c.S = __fadd_ru(c.S, hi);
-    }
+// One element: coefficient copy a, bound copies b = (lb, ub).
+__device__ __forceinline__ void scr_add(Scr &c, float a, float2 b) {
+    const bool pos = a > 0.0f;
+    const float bmin = pos ? b.x : b.y, bmax = pos ? b.y : b.x;
+    const bool imin = fabsf(bmin) == kF32Inf, imax = fabsf(bmax) == kF32Inf;
+    c.minf += imin;
+    c.maxf += imax;
+    const float tmin = imin ? 0.0f : __fmul_rn(a, bmin);
+    const float tmax = imax ? 0.0f : __fmul_rn(a, bmax);
+    c.mn = __fadd_rn(c.mn, tmin);
+    c.mx = __fadd_rn(c.mx, tmax);
+    c.S = __fadd_ru(c.S, __fadd_ru(fabsf(tmin), fabsf(tmax)));
+    // |a| (ub - lb) <= |a32| (fl(ub32 - lb32) + 2^-21 fl(|ub32| + |lb32|)) up
+    // to a relative 2^-21: the copies' errors are at most 2^-24 of |ub|, |lb|
+    const float d = __fsub_rn(b.y, b.x), w = __fadd_rn(fabsf(b.y), fabsf(b.x));
+    c.U = fmax_nan(c.U, __fmul_rn(fabsf(a), __fmaf_rn(w, 0x1p-21f, d)));
 }
 __device__ __forceinline__ void scr_combine(Scr &a, const Scr &b) {
-    a.mn_lo = __fadd_rd(a.mn_lo, b.mn_lo);
-    a.mn_hi = __fadd_ru(a.mn_hi, b.mn_hi);
-    a.mx_lo = __fadd_rd(a.mx_lo, b.mx_lo);
-    a.mx_hi = __fadd_ru(a.mx_hi, b.mx_hi);
+    a.mn = __fadd_rn(a.mn, b.mn);
+    a.mx = __fadd_rn(a.mx, b.mx);
     a.S = __fadd_ru(a.S, b.S);
-    a.U = fmaxf(a.U, b.U);
+    a.U = fmax_nan(a.U, b.U);
     a.minf += b.minf;
     a.maxf += b.maxf;
 }
 // Largest float not above 1e20 (the infinity threshold).
 constexpr float kInfF32Dn = 0x1.5af1d6p+66f;
-// True when the row filter certainly skips the row (u_filter_skips, and the
-// reference's test, whose sequential maxactdelta m satisfies m <= M <= U for the
-// true maximum M of |a|(ub - lb)): the FP64 activities of any summation order lie in
-// [lo - E, hi + E] with E = 2^-20 S (the rounding error of n <= 2^31 FP64
-// additions is below n 2^-53 S), and FP64 rounding of rhs - minact and
-// maxact - lhs is monotone, so min(rhs - minact, maxact - lhs) >= the
-// directed-rounded lower end computed here.
-__device__ __forceinline__ void scr_slack(const Scr &c, double lhs, double rhs, float &mn_lo, float &mn_hi) {
-    const float E = __fmul_ru(c.S, 9.5367431640625e-7f);
+// Upper bound of the row filter's U (delta_up of every element) and of the
+// reference's sequential maxactdelta: the accumulated U widened by 2^-20
+// relative plus 2^-80 absolute (bounds below 2^-126).
+__device__ __forceinline__ float scr_u_bound(const Scr &c) { return __fmaf_ru(c.U, kUMargin, 0x1p-80f); }
+// Enclosure [mn_lo, mn_hi] of min(rhs - minact, maxact - lhs) as the exact
+// pass computes it in FP64 for a row of n elements: the activities lie within
+// E of mn / mx, and FP64 rounding of the differences is monotone.
+__device__ __forceinline__ void scr_slack(const Scr &c, int n, double lhs, double rhs, float &mn_lo,
+                                          float &mn_hi) {
+    const float k = n <= (1 << 20) ? __fmul_ru((float)(n + 4), n <= (1 << 16) ? 0x1.04p-24f : 0x1.2p-24f)
+                                   : kF32Inf;
+    const float E = __fmaf_ru(c.S, k, 0x1p-80f);
     const MagEnc R = mag_enc(dbits(rhs)), Lh = mag_enc(dbits(lhs));
     const bool rsg = dbits(rhs) < 0, lsg = dbits(lhs) < 0;
     const float rhs_dn = rsg ? -R.up : R.dn, rhs_up = rsg ? -R.dn : R.up;
     const float lhs_dn = lsg ? -Lh.up : Lh.dn, lhs_up = lsg ? -Lh.dn : Lh.up;
-    const float s_lo = __fsub_rd(rhs_dn, __fadd_ru(c.mn_hi, E));
-    const float s_hi = __fsub_ru(rhs_up, __fsub_rd(c.mn_lo, E));
-    const float t_lo = __fsub_rd(__fsub_rd(c.mx_lo, E), lhs_up);
-    const float t_hi = __fsub_ru(__fadd_ru(c.mx_hi, E), lhs_dn);
-    mn_lo = fminf(s_lo, t_lo);
-    mn_hi = fminf(s_hi, t_hi);
+    const float s_lo = __fsub_rd(rhs_dn, __fadd_ru(c.mn, E));
+    const float s_hi = __fsub_ru(rhs_up, __fsub_rd(c.mn, E));
+    const float t_lo = __fsub_rd(__fsub_rd(c.mx, E), lhs_up);
+    const float t_hi = __fsub_ru(__fadd_ru(c.mx, E), lhs_dn);
+    mn_lo = fmin_nan(s_lo, t_lo);
+    mn_hi = fminf(s_hi, t_hi);  // min(s, t) <= either upper end
 }
-__device__ __forceinline__ bool scr_skips(const Scr &c, double lhs, double rhs) {
+// True when the row filter certainly skips the row: u_filter_skips (the
+// exact pass's rule for rows summed by several lanes) and the reference's
+// test (its sequential maxactdelta is at most the largest |a| (ub - lb) up to
+// FP64 rounding) both skip it.
+__device__ __forceinline__ bool scr_skips(const Scr &c, int n, double lhs, double rhs) {
     if (c.minf > 1 && c.maxf > 1) return true;
     float mn_lo, mn_hi;
-    scr_slack(c, lhs, rhs, mn_lo, mn_hi);
-    return mn_hi < kInfF32Dn && __fmul_rn(c.U, kUMargin) <= mn_lo;
+    scr_slack(c, n, lhs, rhs, mn_lo, mn_hi);
+    return mn_hi < kInfF32Dn && __fmul_ru(scr_u_bound(c), kUMargin) <= mn_lo;
 }
 
 // The project's infeasibility rule (the reference detects none).

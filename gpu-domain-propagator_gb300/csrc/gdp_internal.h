@@ -13,6 +13,9 @@
 //  * bounds: interleaved (lb, ub) pairs, current (read-only during a round) and
 //    next (receives the FP64 min/max atomics); a bitmap records the variables
 //    changed in the round.
+//  * FP32 screen copies of the coefficients (sell_a32, la32) and of the
+//    current bounds (bnd32): the screen streams 8 B per non-zero and gathers
+//    8 B per bound pair; the FP64 arrays are read only by the exact pass.
 //  * marking: per row position the round in which it must be processed next,
 //    and the positions of every variable's rows (CSC of positions).
 #pragma once
@@ -34,7 +37,7 @@ struct TilePart {
 
 // FP32 screen partial of a split-row tile (see Scr in gdp_device.cuh).
 struct TileScr {
-    float mn_lo, mn_hi, mx_lo, mx_hi, S, U;
+    float mn, mx, S, U;
     int minf, maxf;
 };
 
@@ -77,12 +80,14 @@ struct DevProblem {
     const int *slice_lg;         // n_slices: log2 of the lanes per row (SELL-g)
     const int *sell_col;
     const double *sell_val;
+    const float *sell_a32;       // FP32 screen copies of sell_val (coef_screen)
     const int *srow_len;         // n_srows
     const double *srow_lhs, *srow_rhs;
     // split rows
     int n_lrows, n_tiles;
     const int *lcol;
     const double *lval;
+    const float *la32;      // FP32 screen copies of lval
     const double *lrow_lhs, *lrow_rhs;
     const int *lrow_tile0;  // n_lrows + 1: tiles of split row r are [lrow_tile0[r], lrow_tile0[r+1])
     const int *tile_row;    // n_tiles
@@ -138,6 +143,7 @@ struct DevProblem {
     // bounds
     double2 *bnd;          // current (lb, ub); read-only while a round runs
     double2 *bnd_nxt;      // next: FP64 min/max atomics
+    float2 *bnd32;         // FP32 screen copies of bnd (bnd_screen), refreshed with it
     const unsigned char *is_cont;
     unsigned *chg;         // changed-variable bitmap, n_chg_words words
     int n_chg_words;

@@ -57,9 +57,9 @@ __device__ __forceinline__ void row_features(const DevProblem &P, int p, int rou
 }
 
 // Screen statistics kept for the row's next features.
-__device__ __forceinline__ float2 screen_stats(const Scr &c, double lhs, double rhs) {
+__device__ __forceinline__ float2 screen_stats(const Scr &c, int n, double lhs, double rhs) {
     float mn_lo, mn_hi;
-    scr_slack(c, lhs, rhs, mn_lo, mn_hi);
+    scr_slack(c, n, lhs, rhs, mn_lo, mn_hi);
     float2 r;
     if (!(mn_hi < kInfF32Dn) || !(mn_lo > -kInfF32Dn)) {
         r.x = 1.f;
@@ -149,21 +149,20 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     scr_init(c);
     {
         const int *col = P.sell_col + base;
-        const double *val = P.sell_val + base;
+        const float *val = P.sell_a32 + base;
 #pragma unroll 4
         for (int i = 0; i < cnt; i++) {
             const int j = __ldcs(col + 32 * i);
-            const double a = __ldcs(val + 32 * i);
-            const double2 b = load_bnd(P, j);
-            scr_add(c, dbits(a), dbits(b.x), dbits(b.y));
+            const float a = __ldcs(val + 32 * i);
+            scr_add(c, a, load_bnd32(P, j));
         }
     }
     if (g > 1) scr_group_reduce(c, g);
     bool exact = false;
     float2 st = make_float2(0.f, 0.f);
     if (leader) {
-        exact = !scr_skips(c, lhs, rhs);
-        st = screen_stats(c, lhs, rhs);
+        exact = !scr_skips(c, len, lhs, rhs);
+        st = screen_stats(c, len, lhs, rhs);
     }
     count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
@@ -220,6 +219,7 @@ __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round,
             bits &= bits - 1;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
+            P.bnd32[j] = bnd_screen(b);
             if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);

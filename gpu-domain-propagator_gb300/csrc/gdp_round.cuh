@@ -45,6 +45,7 @@ __device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
 // Bounds are written by the finalize phase of the same megakernel launch, so
 // they are read with coherent loads (never the read-only path).
 __device__ __forceinline__ double2 load_bnd(const DevProblem &P, int j) { return P.bnd[j]; }
+__device__ __forceinline__ float2 load_bnd32(const DevProblem &P, int j) { return P.bnd32[j]; }
 
 // Row constants of tightenVariable (src/propagation_methods.cuh:223-276), with
 // float thresholds that decide most per-element EPS tests without FP64:
@@ -265,10 +266,8 @@ __device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
 __device__ __forceinline__ void scr_group_reduce(Scr &c, int g) {
     for (int off = g >> 1; off > 0; off >>= 1) {
         Scr o;
-        o.mn_lo = __shfl_down_sync(kFull, c.mn_lo, off);
-        o.mn_hi = __shfl_down_sync(kFull, c.mn_hi, off);
-        o.mx_lo = __shfl_down_sync(kFull, c.mx_lo, off);
-        o.mx_hi = __shfl_down_sync(kFull, c.mx_hi, off);
+        o.mn = __shfl_down_sync(kFull, c.mn, off);
+        o.mx = __shfl_down_sync(kFull, c.mx, off);
         o.S = __shfl_down_sync(kFull, c.S, off);
         o.U = __shfl_down_sync(kFull, c.U, off);
         o.minf = __shfl_down_sync(kFull, c.minf, off);
@@ -428,21 +427,20 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     double lhs = 0.0, rhs = 0.0;
     {
         const int *col = P.sell_col + base;
-        const double *val = P.sell_val + base;
+        const float *val = P.sell_a32 + base;
         Scr c;
         scr_init(c);
 #pragma unroll 4
         for (int i = 0; i < cnt; i++) {
             const int j = __ldcs(col + 32 * i);
-            const double a = __ldcs(val + 32 * i);
-            const double2 b = load_bnd(P, j);
-            scr_add(c, dbits(a), dbits(b.x), dbits(b.y));
+            const float a = __ldcs(val + 32 * i);
+            scr_add(c, a, load_bnd32(P, j));
         }
         if (g > 1) scr_group_reduce(c, g);
         if (leader) {
             lhs = __ldg(P.srow_lhs + r);
             rhs = __ldg(P.srow_rhs + r);
-            exact = !scr_skips(c, lhs, rhs);
+            exact = !scr_skips(c, len, lhs, rhs);
         }
     }
     count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
@@ -576,10 +574,8 @@ __device__ __forceinline__ void scr_shfl_reduce(Scr &c) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         Scr o;
-        o.mn_lo = __shfl_down_sync(kFull, c.mn_lo, off);
-        o.mn_hi = __shfl_down_sync(kFull, c.mn_hi, off);
-        o.mx_lo = __shfl_down_sync(kFull, c.mx_lo, off);
-        o.mx_hi = __shfl_down_sync(kFull, c.mx_hi, off);
+        o.mn = __shfl_down_sync(kFull, c.mn, off);
+        o.mx = __shfl_down_sync(kFull, c.mx, off);
         o.S = __shfl_down_sync(kFull, c.S, off);
         o.U = __shfl_down_sync(kFull, c.U, off);
         o.minf = __shfl_down_sync(kFull, c.minf, off);
@@ -618,9 +614,8 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
 #pragma unroll 4
     for (int k = b + lane; k < e; k += 32) {
         const int j = __ldcs(P.lcol + k);
-        const double a = __ldcs(P.lval + k);
-        const double2 bb = load_bnd(P, j);
-        scr_add(c, dbits(a), dbits(bb.x), dbits(bb.y));
+        const float a = __ldcs(P.la32 + k);
+        scr_add(c, a, load_bnd32(P, j));
     }
     scr_shfl_reduce(c);
     const int t0 = __ldg(P.lrow_tile0 + row);
@@ -630,12 +625,11 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
         ws.st_nnz += (unsigned long long)(e - b);
         if (t == t0) ws.st_rows += 1ULL;
         if (single) {
-            exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+            exact = !scr_skips(c, e - b, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
             if (exact) ws.st_exact += (unsigned long long)(e - b);
         } else {
             TileScr ts;
-            ts.mn_lo = c.mn_lo; ts.mn_hi = c.mn_hi; ts.mx_lo = c.mx_lo; ts.mx_hi = c.mx_hi;
-            ts.S = c.S; ts.U = c.U; ts.minf = c.minf; ts.maxf = c.maxf;
+            ts.mn = c.mn; ts.mx = c.mx; ts.S = c.S; ts.U = c.U; ts.minf = c.minf; ts.maxf = c.maxf;
             P.tile_scr[t] = ts;
         }
     }
@@ -661,13 +655,15 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
     for (int u = t0 + lane; u < t1; u += 32) {
         const TileScr p = P.tile_scr[u];
         Scr o;
-        o.mn_lo = p.mn_lo; o.mn_hi = p.mn_hi; o.mx_lo = p.mx_lo; o.mx_hi = p.mx_hi;
-        o.S = p.S; o.U = p.U; o.minf = p.minf; o.maxf = p.maxf;
+        o.mn = p.mn; o.mx = p.mx; o.S = p.S; o.U = p.U; o.minf = p.minf; o.maxf = p.maxf;
         scr_combine(c, o);
     }
     scr_shfl_reduce(c);
     int exact = 0;
-    if (lane == 0) exact = !scr_skips(c, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+    if (lane == 0) {
+        const int n_row = __ldg(P.tile_end + t1 - 1) - __ldg(P.tile_begin + t0);
+        exact = !scr_skips(c, n_row, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+    }
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
     const Acc s = tile_exact(P, b, e, lane);
@@ -737,6 +733,7 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
             bits &= bits - 1;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
+            P.bnd32[j] = bnd_screen(b);
             if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);
