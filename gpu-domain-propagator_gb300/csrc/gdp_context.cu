@@ -165,7 +165,6 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     sell_elems = slice_ptr[n_slices];
     std::vector<int> sell_col((size_t)std::max<long long>(sell_elems, 1), 0);
     std::vector<double> sell_val((size_t)std::max<long long>(sell_elems, 1), 0.0);
-    std::vector<float> sell_a32((size_t)std::max<long long>(sell_elems, 1), 0.0f);
     std::vector<int> srow_len(std::max(ns, 1));
     std::vector<double> srow_lhs(std::max(ns, 1)), srow_rhs(std::max(ns, 1));
 #pragma omp parallel for schedule(dynamic, 64)
@@ -180,7 +179,6 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
                 const long long e = slice_ptr[s] + 32LL * (k >> lg) + (rl << lg) + (k & (g - 1));
                 sell_col[e] = col[row_ptr[i] + k];
                 sell_val[e] = val[row_ptr[i] + k];
-                sell_a32[e] = coef_screen(sell_val[e]);
             }
         }
     }
@@ -207,13 +205,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     const long long lnnz = lrow_ptr[n_lrows];
     std::vector<int> lcol((size_t)std::max<long long>(lnnz, 1));
     std::vector<double> lval((size_t)std::max<long long>(lnnz, 1));
-    std::vector<float> la32((size_t)std::max<long long>(lnnz, 1), 0.0f);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int r = 0; r < n_lrows; r++) {
         const int i = split_rows[r];
         std::memcpy(&lcol[lrow_ptr[r]], &col[row_ptr[i]], sizeof(int) * (size_t)len[i]);
         std::memcpy(&lval[lrow_ptr[r]], &val[row_ptr[i]], sizeof(double) * (size_t)len[i]);
-        for (int k = 0; k < len[i]; k++) la32[lrow_ptr[r] + k] = coef_screen(val[row_ptr[i] + k]);
     }
     // work items of the activity phase, heaviest first (slices: 32 x width non-zeros)
     std::vector<int> items;
@@ -251,8 +247,34 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.slice_lg, const int, slice_lg);
     GDP_UP(P.sell_col, const int, sell_col);
     GDP_UP(P.sell_val, const double, sell_val);
-    GDP_UP(P.sell_a32, const float, sell_a32);
+    {  // FP32 screen copies, made on the device from the uploaded values
+        float *a32 = (float *)arena.alloc_bytes(sizeof(float) * sell_val.size());
+        if (!a32 || launch_coef_screen(P.sell_val, a32, (long long)sell_val.size(), 8 * n_sms, stream) != 0) {
+            set_error("device allocation/launch failed for sell_a32");
+            return GDP_ERROR;
+        }
+        P.sell_a32 = a32;
+    }
     GDP_UP(P.srow_len, const int, srow_len);
+    {  // row-contiguous copy (positions in SELL order) for the deferred exact pass
+        std::vector<int> xptr(std::max(ns, 1), 0);
+        long long acc = 0;
+        for (int p = 0; p < ns; p++) {
+            xptr[p] = (int)acc;
+            acc += len[order[p]];
+        }
+        std::vector<int> xcol((size_t)std::max<long long>(acc, 1));
+        std::vector<double> xval((size_t)std::max<long long>(acc, 1));
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (int p = 0; p < ns; p++) {
+            const int i = order[p];
+            std::memcpy(&xcol[xptr[p]], &col[row_ptr[i]], sizeof(int) * (size_t)len[i]);
+            std::memcpy(&xval[xptr[p]], &val[row_ptr[i]], sizeof(double) * (size_t)len[i]);
+        }
+        GDP_UP(P.xptr, const int, xptr);
+        GDP_UP(P.xcol, const int, xcol);
+        GDP_UP(P.xval, const double, xval);
+    }
     {
         std::vector<int> pos_slice(std::max(ns, 1), 0);
         for (int s = 0; s < n_slices; s++)
@@ -265,7 +287,14 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.n_tiles = n_tiles;
     GDP_UP(P.lcol, const int, lcol);
     GDP_UP(P.lval, const double, lval);
-    GDP_UP(P.la32, const float, la32);
+    {
+        float *a32 = (float *)arena.alloc_bytes(sizeof(float) * lval.size());
+        if (!a32 || launch_coef_screen(P.lval, a32, (long long)lval.size(), 8 * n_sms, stream) != 0) {
+            set_error("device allocation/launch failed for la32");
+            return GDP_ERROR;
+        }
+        P.la32 = a32;
+    }
     GDP_UP(P.lrow_lhs, const double, lrow_lhs);
     GDP_UP(P.lrow_rhs, const double, lrow_rhs);
     GDP_UP(P.lrow_tile0, const int, lrow_tile0);
@@ -299,7 +328,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     for (int c = 0; c < 6; c++) { P.cls_begin[c] = 0; P.cls_end[c] = 0; }
     for (int sl = n_slices - 1; sl >= 0; sl--) P.cls_begin[slice_lg[sl]] = slice_row0[sl];
     for (int sl = 0; sl < n_slices; sl++) P.cls_end[slice_lg[sl]] = slice_row0[sl + 1];
-    P.xrow = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
+    P.xrow = (XRow *)arena.alloc_bytes(sizeof(XRow) * (size_t)std::max(ns, 1));
     P.xctr = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 32);
     P.row_exact = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
     P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);

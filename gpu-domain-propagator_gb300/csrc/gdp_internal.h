@@ -13,6 +13,9 @@
 //  * bounds: interleaved (lb, ub) pairs, current (read-only during a round) and
 //    next (receives the FP64 min/max atomics); a bitmap records the variables
 //    changed in the round.
+//  * a row-contiguous copy of the SELL rows (xcol, xval): the deferred exact
+//    pass reads rows that came from many slices, one row per lane (or group),
+//    so it wants each row's elements next to each other.
 //  * FP32 screen copies of the coefficients (sell_a32, la32) and of the
 //    current bounds (bnd32): the screen streams 8 B per non-zero and gathers
 //    8 B per bound pair; the FP64 arrays are read only by the exact pass.
@@ -33,6 +36,14 @@ struct TilePart {
     int minf, maxf;
     float U;  // FP32 upper bound of max |a|(ub - lb)
     int pad;
+};
+
+// A row queued for the deferred exact pass: the index of its first element
+// in the row-contiguous copy, its position and its length, so that the pass
+// starts its element loads without looking the row up.
+struct XRow {
+    long long base;
+    int pos, len;
 };
 
 // FP32 screen partial of a split-row tile (see Scr in gdp_device.cuh).
@@ -82,6 +93,11 @@ struct DevProblem {
     const double *sell_val;
     const float *sell_a32;       // FP32 screen copies of sell_val (coef_screen)
     const int *srow_len;         // n_srows
+    // row-contiguous copy of the SELL rows for the deferred exact pass: the
+    // elements of position p at xptr[p] .. xptr[p] + srow_len[p] - 1
+    const int *xptr;             // n_srows
+    const int *xcol;
+    const double *xval;
     const double *srow_lhs, *srow_rhs;
     // split rows
     int n_lrows, n_tiles;
@@ -116,7 +132,7 @@ struct DevProblem {
     // are exactly that range, slices being sorted by g).
     int defer_exact;
     int cls_begin[6], cls_end[6];
-    int *xrow;             // n_srows
+    XRow *xrow;            // n_srows
     unsigned *xctr;        // [parity * 16 + lg]: queue tails, [parity * 16 + 8 + lg]: pull counters
     // learned marking (SELL rows; null when no model is attached). learned:
     // 1 = rounds process the marked rows the model selects, 2 = trace (every
@@ -157,6 +173,7 @@ constexpr int kWarpsPerCta = 8;
 constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
 // Launch helpers (gdp_round.cu). All return the cudaError_t of the launch.
+int launch_coef_screen(const double *v, float *out, long long n, int blocks, cudaStream_t s);
 int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_interleave(const DevProblem &P, const double *lb, const double *ub, int blocks, cudaStream_t s);
 int launch_deinterleave(const DevProblem &P, double *lb, double *ub, int blocks, cudaStream_t s);

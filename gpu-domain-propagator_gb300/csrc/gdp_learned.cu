@@ -170,7 +170,7 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     if (__any_sync(kFull, exact)) {
         ws.base[lane] = base;
         __syncwarp();
-        sell_rows_exact(P, lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws, L.tight, L.go);
+        sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws, L.tight, L.go);
     }
     __syncwarp();
     if (leader) {

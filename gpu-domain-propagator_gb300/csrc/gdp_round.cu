@@ -66,6 +66,12 @@ __global__ void k_condition(DevProblem P, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// FP32 screen copies of coefficient values (coef_screen).
+__global__ void __launch_bounds__(256) k_coef_screen(const double *v, float *out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = coef_screen(v[i]);
+}
+
 __global__ void __launch_bounds__(256) k_check_bounds(DevProblem P) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < P.n; j += gridDim.x * blockDim.x) {
         const double2 b = P.bnd[j];
@@ -159,6 +165,11 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
 }  // namespace
 
 // ---- launchers ------------------------------------------------------------
+int launch_coef_screen(const double *v, float *out, long long n, int blocks, cudaStream_t s) {
+    k_coef_screen<<<blocks, 256, 0, s>>>(v, out, n);
+    return (int)cudaGetLastError();
+}
+
 int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s) {
     if (P.n == 0) return 0;
     k_check_bounds<<<blocks, 256, 0, s>>>(P);

@@ -291,16 +291,29 @@ __device__ __forceinline__ void count_work(WarpSmem &ws, int lane, int rows, int
     }
 }
 
+// Where the exact pass finds a row's elements: step i of lane l at
+// col[ws.base[l] + stride i] -- stride 32 in the SELL slices (a warp that
+// screened the slice), stride g in the row-contiguous copy (the deferred
+// pass, whose rows come from different slices: a lane's successive elements
+// then share sectors instead of sitting 128 B / 256 B apart).
+struct ElemView {
+    const int *col;
+    const double *val;
+    int stride;
+};
+__device__ __forceinline__ ElemView sell_view(const DevProblem &P) { return ElemView{P.sell_col, P.sell_val, 32}; }
+
 // Exact pass of up to 32/g SELL-g rows held by one warp, g lanes per row:
 // lane l serves row l >> lg (active if `exact`), its elements at
-// ws.base[l] + 32 i for i < cnt (element sub + g i of the row, sub = l & (g-1)).
+// ws.base[l] + stride i for i < cnt (element sub + g i of the row, sub = l & (g-1)).
 // The leader lane of each row (sub == 0) holds its position, lhs and rhs.
 //   pass 1: exact FP64 activities. g == 1 rows are summed left to right,
 //           with the reference's sequential EPS-max of |a|(ub - lb) in the
 //           same loop, and take the reference's row test; g > 1 rows are
 //           combined by a shuffle tree and use the FP32 bound rule.
 //   pass 2: candidates through the warp division queue.
-__device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int lane, bool exact, int len,
+__device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemView ev, int lg, int lane,
+                                                bool exact, int len,
                                                 int cnt, double lhs, double rhs, int *change,
                                                 unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
                                                 int *row_go = nullptr) {
@@ -308,8 +321,9 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
     const int rl = lane >> lg, sub = lane & (g - 1);
     const bool leader = exact && sub == 0;
     const long long base = ws.base[lane];
-    const int *col = P.sell_col + base;
-    const double *val = P.sell_val + base;
+    const int *col = ev.col + base;
+    const double *val = ev.val + base;
+    const int st = ev.stride;
     const int cnt1 = exact ? cnt : 0;
     Acc s;
     acc_init(s);
@@ -322,8 +336,8 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
         double m = 0.0;
 #pragma unroll 4
         for (int i = 0; i < cnt1; i++) {
-            const int j = __ldg(col + 32 * i);
-            const double a = __ldg(val + 32 * i);
+            const int j = __ldg(col + st * i);
+            const double a = __ldg(val + st * i);
             const double2 b = load_bnd(P, j);
             acc_add_terms(s, a, b.x, b.y);
             const double d = dmul(fabs(a), dsub(b.y, b.x));
@@ -336,8 +350,8 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
     } else {
 #pragma unroll 4
         for (int i = 0; i < cnt1; i++) {
-            const int j = __ldg(col + 32 * i);
-            const double a = __ldg(val + 32 * i);
+            const int j = __ldg(col + st * i);
+            const double a = __ldg(val + st * i);
             const double2 b = load_bnd(P, j);
             acc_add(s, a, b.x, b.y);
         }
@@ -365,7 +379,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
         auto run = [&](const QEntry &q) {
             const int owner = (q.code >> 1) & 31;
             const int slot = owner >> lg;
-            const double a = __ldg(P.sell_val + ws.base[owner] + 32LL * (int)(q.code >> 6));
+            const double a = __ldg(ev.val + ws.base[owner] + (long long)st * (int)(q.code >> 6));
             if (apply_side(P, ws.rc[slot], q.j, a, load_bnd(P, q.j), (int)(q.code & 1u))) {
                 tight++;
                 if (row_tight) atomicAdd(row_tight + slot, 1);
@@ -381,7 +395,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
         double a1 = 0.0, a2 = 0.0;
         double2 b1 = make_double2(0.0, 0.0);
         if (ce > 0) { j1 = __ldg(col); a1 = __ldg(val); }
-        if (ce > 1) { j2 = __ldg(col + 32); a2 = __ldg(val + 32); }
+        if (ce > 1) { j2 = __ldg(col + st); a2 = __ldg(val + st); }
         if (ce > 0) b1 = load_bnd(P, j1);
         for (int i = 0; i < maxcnt; i++) {
             const int j = j1;
@@ -389,7 +403,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, int lg, int
             const double2 b = b1;
             j1 = j2;
             a1 = a2;
-            if (i + 2 < ce) { j2 = __ldg(col + 32 * (i + 2)); a2 = __ldg(val + 32 * (i + 2)); }
+            if (i + 2 < ce) { j2 = __ldg(col + st * (i + 2)); a2 = __ldg(val + st * (i + 2)); }
             if (i + 1 < ce) b1 = load_bnd(P, j1);
             const int sides = i < ce ? candidate_sides(ws.rc[rl], a, b.x, b.y) : 0;
             queue_push(Q, lane, sides, j, ((unsigned)i << 6) | ((unsigned)lane << 1));
@@ -421,6 +435,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;  // my elements
     const long long base = __ldg(P.slice_ptr + slice) + lane;
     const bool leader = act && sub == 0;
+    const int xbase = (leader && P.defer_exact) ? __ldg(P.xptr + r) : 0;  // used at the end
 
     // FP32 screen
     bool exact = false;
@@ -450,18 +465,99 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         unsigned first = 0;
         if (lane == 0) first = atomicAdd(P.xctr + 16 * par + lg, (unsigned)__popc(bal));
         first = __shfl_sync(kFull, first, 0);
-        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = r;
+        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len};
         return;
     }
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
     if (!__any_sync(kFull, exact)) return;
     ws.base[lane] = base;
     __syncwarp();
-    sell_rows_exact(P, lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws);
+    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws);
+}
+
+// K slices of one-lane rows (g = 1) screened together in the deferred-exact
+// mode: lane l screens row l of each slice, so the K rows' column, coefficient
+// and bound loads are in flight at the same time (a slice of short rows holds
+// only 64..128 non-zeros: alone, its chain of dependent loads leaves the warp
+// waiting), and the exact rows of all K slices are queued with one counter
+// update. Decisions and queue contents equal those of K sell_slice calls.
+constexpr int kScreenGroup = 2;
+template <int K>
+__device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&sl)[K], int lane, int round,
+                                               bool marked, WarpSmem &ws, int par) {
+    int r[K], len[K];
+    long long base[K];
+    double lhs[K], rhs[K];
+    bool act[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int row0 = __ldg(P.slice_row0 + sl[k]);
+        r[k] = row0 + lane;
+        act[k] = lane < __ldg(P.slice_row0 + sl[k] + 1) - row0;
+        base[k] = __ldg(P.slice_ptr + sl[k]) + lane;
+    }
+    if (marked) {
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (act[k]) act[k] = P.mark[r[k]] == round;
+    }
+    int mx = 0, xbase[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        len[k] = act[k] ? __ldg(P.srow_len + r[k]) : 0;
+        xbase[k] = act[k] ? __ldg(P.xptr + r[k]) : 0;
+        mx = max(mx, len[k]);
+    }
+    Scr c[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) scr_init(c[k]);
+#pragma unroll 2
+    for (int i = 0; i < mx; i++) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if (i < len[k]) {
+                const int j = __ldcs(P.sell_col + base[k] + 32 * i);
+                const float a = __ldcs(P.sell_a32 + base[k] + 32 * i);
+                scr_add(c[k], a, load_bnd32(P, j));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        lhs[k] = 0.0;
+        rhs[k] = 0.0;
+        if (act[k]) {
+            lhs[k] = __ldg(P.srow_lhs + r[k]);
+            rhs[k] = __ldg(P.srow_rhs + r[k]);
+        }
+    }
+    bool exact[K];
+    int rows = 0, nnz = 0, nnz_exact = 0, total = 0;
+    unsigned bal[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        exact[k] = act[k] && !scr_skips(c[k], len[k], lhs[k], rhs[k]);
+        rows += act[k] ? 1 : 0;
+        nnz += len[k];
+        nnz_exact += exact[k] ? len[k] : 0;
+        bal[k] = __ballot_sync(kFull, exact[k]);
+        total += __popc(bal[k]);
+    }
+    count_work(ws, lane, rows, nnz, nnz_exact);
+    if (!total) return;
+    unsigned first = 0;
+    if (lane == 0) first = atomicAdd(P.xctr + 16 * par, (unsigned)total);
+    first = __shfl_sync(kFull, first, 0) + (unsigned)P.cls_begin[0];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k]};
+        first += __popc(bal[k]);
+    }
 }
 
 // Exact-rows phase: the rows the screen queued, class by class (widest rows
-// first), 32/g rows per warp with their elements read from their own slices.
+// first), 32/g rows per warp with their elements read from the row-contiguous copy.
 __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, int *change, unsigned *tight_ctr,
                                                  WarpSmem &ws, int lane) {
     stats_zero(ws, lane);
@@ -480,10 +576,10 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             long long base = 0;
             double lhs = 0.0, rhs = 0.0;
             if (exact) {
-                const int p = P.xrow[P.cls_begin[lg] + k];
-                const int s = __ldg(P.pos_slice + p);
-                base = __ldg(P.slice_ptr + s) + ((long long)(p - __ldg(P.slice_row0 + s)) << lg) + sub;
-                len = __ldg(P.srow_len + p);
+                const XRow x = P.xrow[P.cls_begin[lg] + k];
+                const int p = x.pos;
+                base = x.base + sub;
+                len = x.len;
                 cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
                 if (sub == 0) {
                     lhs = __ldg(P.srow_lhs + p);
@@ -492,7 +588,8 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             }
             ws.base[lane] = base;
             __syncwarp();
-            sell_rows_exact(P, lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws);
+            sell_rows_exact(P, ElemView{P.xcol, P.xval, g}, lg, lane, exact, len, cnt, lhs, rhs, change,
+                            tight_ctr, ws);
             __syncwarp();
         }
     }
@@ -754,18 +851,43 @@ __device__ __forceinline__ int warp_next(unsigned *ctr, int lane) {
     return (int)__shfl_sync(kFull, v, 0);
 }
 
+__device__ __forceinline__ void activity_item(const DevProblem &P, int it, int lane, int round, bool marked,
+                                              int *change, unsigned *tight_ctr, WarpSmem &ws, int par) {
+    if (it >= 0) sell_slice(P, it, lane, round, marked, change, tight_ctr, ws, par);
+    else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws);
+}
+
+// Items are claimed kScreenGroup at a time; a claim of one-lane-row slices
+// (the light end of the heaviest-first order) is screened as a group when
+// exact rows are deferred, other claims item by item.
 __device__ __forceinline__ void activity_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
                                                int *change, unsigned *tight_ctr, WarpSmem &ws, int lane,
                                                int par = 0) {
     stats_zero(ws, lane);
+    constexpr int K = kScreenGroup;
     WarpCursor cur;
-    cur.start(ctr, 1u, lane);
+    cur.start(ctr, (unsigned)K, lane);
     for (;;) {
         const int i = cur.next(lane);
         if (i >= P.n_items) break;
-        const int it = __ldg(P.items + i);
-        if (it >= 0) sell_slice(P, it, lane, round, marked, change, tight_ctr, ws, par);
-        else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws);
+        int it[K];
+        bool group = P.defer_exact && i + K <= P.n_items;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            it[k] = i + k < P.n_items ? __ldg(P.items + i + k) : -1;
+            group = group && it[k] >= 0;
+        }
+        if (group) {
+#pragma unroll
+            for (int k = 0; k < K; k++) group = group && __ldg(P.slice_lg + it[k]) == 0;
+        }
+        if (group) {
+            sell_slices_g1<K>(P, it, lane, round, marked, ws, par);
+        } else {
+#pragma unroll 1
+            for (int k = 0; k < K && i + k < P.n_items; k++)
+                activity_item(P, it[k], lane, round, marked, change, tight_ctr, ws, par);
+        }
     }
     stats_flush(P, ws, lane);
 }

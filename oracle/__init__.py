@@ -32,7 +32,7 @@ _P_DBL = C.POINTER(C.c_double)
 class _Result(C.Structure):
     _fields_ = [("rounds", C.c_int), ("converged", C.c_int), ("infeasible", C.c_int),
                 ("infeasible_var", C.c_int), ("candidates", C.c_longlong), ("rows_processed", C.c_longlong),
-                ("nnz_processed", C.c_longlong)]
+                ("nnz_processed", C.c_longlong), ("rows_go", C.c_longlong)]
 
 
 class _Acts(C.Structure):
@@ -51,6 +51,7 @@ class Result:
     seconds: float
     rows_processed: int = 0
     nnz_processed: int = 0
+    rows_go: int = 0  # GPU mode: processed rows of at most split_tile non-zeros that passed their row test
 
 
 _o = None
@@ -150,7 +151,7 @@ def propagate(mip, schedule: int = JACOBI, max_rounds: int = 0, nthreads: int = 
     if rc != 0:
         raise ValueError(f"oracle rejected the input ({rc})")
     return Result(lbo, ubo, res.rounds, bool(res.converged), bool(res.infeasible), res.infeasible_var, dt,
-                  res.rows_processed, res.nnz_processed)
+                  res.rows_processed, res.nnz_processed, res.rows_go)
 
 
 def ref_propagate(mip, schedule: int = JACOBI, max_rounds: int = 0, lb=None, ub=None) -> Result:

@@ -290,7 +290,7 @@ int gdpo_gpu_row_go(double minact, double maxact, int minf, int maxf, float U, d
 static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, const double *lb, const double *ub,
                       const int *vartype, double *lb_out, double *ub_out,
-                      unsigned char *var_changed);
+                      unsigned char *var_changed, int *go);
 
 /* Rows up to thread_row_max non-zeros: the GPU's FP32 bound only pre-filters,
  * an exact second pass takes the reference's decision, so these rows follow
@@ -298,11 +298,12 @@ static int jacobi_row(int row, const int *col, const int *row_ptr, const double 
 static int jacobi_row_gpu(int row, const int *col, const int *row_ptr, const double *val, const double *lhs,
                           const double *rhs, const double *lb, const double *ub, const int *vartype,
                           double *lb_out, double *ub_out, unsigned char *var_changed, int thread_row_max,
-                          int tile) {
+                          int tile, int *go) {
     if (row_ptr[row + 1] - row_ptr[row] <= thread_row_max)
-        return jacobi_row(row, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, var_changed);
+        return jacobi_row(row, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, var_changed, go);
     const gacc a = gpu_row_acts(row, col, row_ptr, val, lb, ub, thread_row_max, tile);
-    if (!gdpo_gpu_row_go(a.minact, a.maxact, a.minf, a.maxf, a.U, lhs[row], rhs[row])) return 0;
+    *go = gdpo_gpu_row_go(a.minact, a.maxact, a.minf, a.maxf, a.U, lhs[row], rhs[row]);
+    if (!*go) return 0;
     int any = 0;
     for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
         const int j = col[k];
@@ -359,12 +360,12 @@ static inline void atomic_min_d(double *addr, double v) {
 static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, const double *lb, const double *ub,
                       const int *vartype, double *lb_out, double *ub_out,
-                      unsigned char *var_changed) {
+                      unsigned char *var_changed, int *go) {
     const gdpo_acts a = gdpo_activities(row, col, row_ptr, val, lb, ub);
     int any = 0;
-    if (!gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[row],
-                                    rhs[row], a.maxactdelta))
-        return 0;
+    *go = gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[row], rhs[row],
+                                     a.maxactdelta);
+    if (!*go) return 0;
     for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
         const int j = col[k];
         int lt, ut;
@@ -392,7 +393,8 @@ int gdpo_jacobi_round(int m, int n, const int *col, const int *row_ptr, const do
 #endif
     for (int i = 0; i < m; i++) {
         if (mark && !mark[i]) continue;
-        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL);
+        int go;
+        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL, &go);
         if (t && tight_row) tight_row[i] = 1;
         change |= t;
     }
@@ -473,7 +475,7 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
     while (r.rounds < max_rounds && change && !r.infeasible) {
         r.rounds++;
         change = 0;
-        long long rows = 0, nz = 0, cands = 0;
+        long long rows = 0, nz = 0, cands = 0, go_rows = 0;
         for (int i = 0; i < m; i++)
             if (mark[i]) { rows++; nz += row_ptr[i + 1] - row_ptr[i]; }
         if (schedule == GDPO_SCHED_SEQUENTIAL) {
@@ -500,16 +502,20 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
             memcpy(lb_snap, lb, sizeof(double) * (size_t)n);
             memcpy(ub_snap, ub, sizeof(double) * (size_t)n);
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads > 0 ? nthreads : 1) reduction(| : change)
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads > 0 ? nthreads : 1) \
+        reduction(| : change) reduction(+ : go_rows)
 #endif
             for (int i = 0; i < m; i++) {
                 if (!mark[i]) continue;
-                if (gpu_mode)
+                int go = 0;
+                if (gpu_mode) {
                     change |= jacobi_row_gpu(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
-                                             ub, var_changed, split_len, split_tile);
-                else
+                                             ub, var_changed, split_len, split_tile, &go);
+                    if (go && row_ptr[i + 1] - row_ptr[i] <= split_tile) go_rows++;
+                } else {
                     change |= jacobi_row(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
-                                         ub, var_changed);
+                                         ub, var_changed, &go);
+                }
             }
         }
         /* marking for the next round: reference src/propagation_methods.cu:3-13 */
@@ -526,6 +532,7 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
         }
         r.rows_processed += rows;
         r.nnz_processed += nz;
+        r.rows_go += go_rows;
         r.candidates += cands;
     }
     r.converged = !change || r.infeasible;

@@ -39,6 +39,8 @@ typedef struct {
     long long candidates;  /* bound tightenings found (summed over rounds) */
     long long rows_processed; /* marked rows processed (summed over rounds) */
     long long nnz_processed;  /* their non-zeros */
+    long long rows_go;        /* GPU mode: processed rows of at most split_tile non-zeros that passed
+                                 their row test (summed over rounds) */
 } gdpo_result;
 
 /* --- reference math, one function each (known-answer tests call these) --- */

@@ -42,6 +42,10 @@ def check_vs_oracle(mip, sync=gdp.CPU_LOOP, max_rounds=0, trm=TRM, tile=TILE, ma
         # always-on marking processes exactly the rows the oracle's marking processes
         assert st["rows_processed"] == ref.rows_processed
         assert st["nnz_processed"] == ref.nnz_processed
+        # every row test decided like the oracle's, whether the FP32 screen,
+        # the screen's bounds of max |a|(ub - lb) or the sequential EPS-max
+        # decided it on the GPU
+        assert st["rows_go"] == ref.rows_go
     return st
 
 
@@ -129,6 +133,20 @@ def test_power_law_small_tiles_and_threshold():
     mip = gdpgen.random_mip(1, seed=5, m=30_000, n=20_000, len_max=3000, dense_len=8000, n_dense_rows=3)
     check_vs_oracle(mip, gdp.MEGAKERNEL, trm=64, tile=512)
     check_vs_oracle(mip, gdp.CPU_LOOP, trm=256, tile=1024)
+
+
+@pytest.mark.parametrize("sync", [gdp.CPU_LOOP, gdp.MEGAKERNEL])
+def test_row_tests_decided_like_oracle(sync):
+    """Rows at or near equality (the largest |a|(ub - lb) within EPS of the
+    slack) are where the screen's bounds cannot decide the reference's row
+    test: with marking on every round, the GPU passes exactly the rows the
+    oracle passes, round by round, on power-law, chain and cover instances."""
+    mips = [gdpgen.random_mip(1, seed=7, m=40_000, n=30_000, len_max=2000, dense_len=5000, n_dense_rows=2),
+            gdpgen.chains(8000, chain_max=300, seed=5, frac_int_vars=1.0),
+            gdpgen.cover_knapsack(20_000, 2_000, 16_000, 2_000, seed=2)]
+    for mip in mips:
+        st = check_vs_oracle(mip, sync, max_rounds=2000, marking=2)
+        assert st["rows_go"] > 0
 
 
 def test_chains_many_rounds():
