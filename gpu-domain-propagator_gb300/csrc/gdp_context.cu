@@ -274,6 +274,12 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         GDP_UP(P.xptr, const int, xptr);
         GDP_UP(P.xcol, const int, xcol);
         GDP_UP(P.xval, const double, xval);
+        float *a32 = (float *)arena.alloc_bytes(sizeof(float) * xval.size());
+        if (!a32 || launch_coef_screen(P.xval, a32, (long long)xval.size(), 8 * n_sms, stream) != 0) {
+            set_error("device allocation/launch failed for xa32");
+            return GDP_ERROR;
+        }
+        P.xa32 = a32;
     }
     {
         std::vector<int> pos_slice(std::max(ns, 1), 0);

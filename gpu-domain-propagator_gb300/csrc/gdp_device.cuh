@@ -319,13 +319,14 @@ __device__ __forceinline__ MagEnc mag_enc(long long bits) {
 //    +-inf, and a non-zero one below 2^-60 in magnitude is NaN.
 // NaN or inf terms make the screen's sums, magnitude sum or U NaN or inf,
 // and every such row is left to the exact pass; the sign test a32 > 0 equals
-// the reference's EPSGT(a, 0) for every coefficient.
+// the reference's EPSGT(a, 0) for every coefficient, and a NaN copy keeps the
+// coefficient's sign (so the sign bit tells a > 0, as in candidate_sides).
 constexpr float kF32Inf = __builtin_huge_valf();
 __host__ __device__ __forceinline__ float coef_screen(double a) {
     const double m = a < 0 ? -a : a;
     if (a > 0.0 && a <= kEps) return __builtin_nanf("");
     if (m > 0x1p40) return a > 0 ? kF32Inf : -kF32Inf;
-    if (m != 0.0 && m < 0x1p-60) return __builtin_nanf("");
+    if (m != 0.0 && m < 0x1p-60) return a > 0 ? __builtin_nanf("") : -__builtin_nanf("");
     return (float)a;
 }
 constexpr long long kBits2p100 = 0x4630000000000000LL;  // 2^100
@@ -423,6 +424,23 @@ __device__ __forceinline__ void scr_slack(const Scr &c, int n, double lhs, doubl
     mn_lo = fmin_nan(s_lo, t_lo);
     mn_hi = fminf(s_hi, t_hi);  // min(s, t) <= either upper end
 }
+// FP32 enclosure lo <= fl(|a| fl(ub - lb)) <= hi of one element from the
+// screen copies (the copies' errors as in scr_add, widened by 2^-20 relative
+// and 2^-80 absolute, which also covers the two FP64 roundings). A bound coded
+// +-inf is at least 1e20 in magnitude, so the lower end uses +-kInfF32Dn in its
+// place; NaN copies leave both ends NaN, and the comparisons then stay open.
+__device__ __forceinline__ DeltaBox delta_box32(float a, float2 b) {
+    const float aa = fabsf(a);
+    const float d = __fsub_rn(b.y, b.x), w = __fadd_rn(fabsf(b.y), fabsf(b.x));
+    DeltaBox r;
+    r.hi = __fmaf_ru(__fmul_rn(aa, __fmaf_rn(w, 0x1p-21f, d)), kUMargin, 0x1p-80f);
+    const float ubl = fmin_nan(b.y, kInfF32Dn), lbh = fmax_nan(b.x, -kInfF32Dn);
+    const float dl = __fsub_rn(ubl, lbh), wl = __fadd_rn(fabsf(ubl), fabsf(lbh));
+    r.lo = __fmaf_rd(__fmul_rn(fmin_nan(aa, 0x1p40f), __fmaf_rn(wl, -0x1p-21f, dl)), 0.99999904632568359375f,
+                     -0x1p-80f);
+    return r;
+}
+
 // True when the row filter certainly skips the row: u_filter_skips (the
 // exact pass's rule for rows summed by several lanes) and the reference's
 // test (its sequential maxactdelta is at most the largest |a| (ub - lb) up to

@@ -98,6 +98,7 @@ struct DevProblem {
     const int *xptr;             // n_srows
     const int *xcol;
     const double *xval;
+    const float *xa32;           // screen copies of xval
     const double *srow_lhs, *srow_rhs;
     // split rows
     int n_lrows, n_tiles;

@@ -109,6 +109,26 @@ __device__ __forceinline__ int candidate_sides(const RowC &c, double a, double l
     return (u_ok ? 1 : 0) | (l_ok ? 2 : 0);
 }
 
+// candidate_sides from the screen copies of the coefficient and the bounds.
+// Returns 4 when the FP32 box leaves a side test open; the caller then decides
+// with the FP64 values (candidate_sides). Signs and infinity tests are exact on
+// the copies: the sign bit of a32 is a's, and -inf / +inf copies are exactly
+// the bounds the reference counts as infinite.
+__device__ __forceinline__ int candidate_sides32(const RowC &c, float a, float2 b) {
+    const DeltaBox box = delta_box32(a, b);
+    const int rs = (c.ok & 1) ? side_test(box, c.slack_dn, c.slack_hi) : 0;
+    const int ls = (c.ok & 2) ? side_test(box, c.nsur_dn, c.nsur_hi) : 0;
+    if (rs == 2 || ls == 2) return 4;
+    const bool pos = __float_as_int(a) > 0;
+    const bool u_side = pos ? rs : ls;
+    const bool l_side = pos ? ls : rs;
+    const int nu = pos ? c.minf : c.maxf;
+    const int nl = pos ? c.maxf : c.minf;
+    const bool u_ok = u_side && (nu == 0 || (nu == 1 && b.x == -kF32Inf));
+    const bool l_ok = l_side && (nl == 0 || (nl == 1 && b.y == kF32Inf));
+    return (u_ok ? 1 : 0) | (l_ok ? 2 : 0);
+}
+
 // One candidate (side 0: upper, 1: lower) of variable j; applies it with an
 // FP64 atomic if EPS-better than the snapshot. Returns true if it tightened.
 // b: the variable's round-start bounds (read-only during the round).
@@ -247,6 +267,7 @@ struct LearnSmem {
     float z[32];
     int tight[32];
     int go[32];
+    unsigned long long marked;  // marked SELL rows met by this warp in the current phase
 };
 
 // Combines the partial accumulators of a group of g lanes (g a power of two,
@@ -299,9 +320,12 @@ __device__ __forceinline__ void count_work(WarpSmem &ws, int lane, int rows, int
 struct ElemView {
     const int *col;
     const double *val;
+    const float *a32;  // screen copies of val (the candidate tests read these)
     int stride;
 };
-__device__ __forceinline__ ElemView sell_view(const DevProblem &P) { return ElemView{P.sell_col, P.sell_val, 32}; }
+__device__ __forceinline__ ElemView sell_view(const DevProblem &P) {
+    return ElemView{P.sell_col, P.sell_val, P.sell_a32, 32};
+}
 
 // Exact pass of up to 32/g SELL-g rows held by one warp, g lanes per row:
 // lane l serves row l >> lg (active if `exact`), its elements at
@@ -388,24 +412,31 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
         int maxcnt = go ? cnt : 0;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) maxcnt = max(maxcnt, __shfl_xor_sync(kFull, maxcnt, off));
-        // software pipeline: element i + 2's column and coefficient and
-        // element i + 1's bounds are in flight while element i is tested
+        // software pipeline over the screen copies: element i + 2's column
+        // and coefficient and element i + 1's bounds are in flight while
+        // element i is tested; the FP64 values are read only for tests the
+        // FP32 box leaves open
+        const float *a32 = ev.a32 + base;
         const int ce = go ? cnt : 0;
         int j1 = 0, j2 = 0;
-        double a1 = 0.0, a2 = 0.0;
-        double2 b1 = make_double2(0.0, 0.0);
-        if (ce > 0) { j1 = __ldg(col); a1 = __ldg(val); }
-        if (ce > 1) { j2 = __ldg(col + st); a2 = __ldg(val + st); }
-        if (ce > 0) b1 = load_bnd(P, j1);
+        float a1 = 0.0f, a2 = 0.0f;
+        float2 b1 = make_float2(0.0f, 0.0f);
+        if (ce > 0) { j1 = __ldg(col); a1 = __ldg(a32); }
+        if (ce > 1) { j2 = __ldg(col + st); a2 = __ldg(a32 + st); }
+        if (ce > 0) b1 = load_bnd32(P, j1);
         for (int i = 0; i < maxcnt; i++) {
             const int j = j1;
-            const double a = a1;
-            const double2 b = b1;
+            const float a = a1;
+            const float2 b = b1;
             j1 = j2;
             a1 = a2;
-            if (i + 2 < ce) { j2 = __ldg(col + st * (i + 2)); a2 = __ldg(val + st * (i + 2)); }
-            if (i + 1 < ce) b1 = load_bnd(P, j1);
-            const int sides = i < ce ? candidate_sides(ws.rc[rl], a, b.x, b.y) : 0;
+            if (i + 2 < ce) { j2 = __ldg(col + st * (i + 2)); a2 = __ldg(a32 + st * (i + 2)); }
+            if (i + 1 < ce) b1 = load_bnd32(P, j1);
+            int sides = i < ce ? candidate_sides32(ws.rc[rl], a, b) : 0;
+            if (sides & 4) {
+                const double2 bd = load_bnd(P, j);
+                sides = candidate_sides(ws.rc[rl], __ldg(val + st * i), bd.x, bd.y);
+            }
             queue_push(Q, lane, sides, j, ((unsigned)i << 6) | ((unsigned)lane << 1));
             queue_drain(Q, lane, false, run);
         }
@@ -588,7 +619,7 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             }
             ws.base[lane] = base;
             __syncwarp();
-            sell_rows_exact(P, ElemView{P.xcol, P.xval, g}, lg, lane, exact, len, cnt, lhs, rhs, change,
+            sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, change,
                             tight_ctr, ws);
             __syncwarp();
         }
@@ -644,21 +675,25 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
     // software pipeline as in sell_rows_exact: two steps of columns and
     // coefficients, one step of bounds ahead
     int j1 = 0, j2 = 0;
-    double a1 = 0.0, a2 = 0.0;
-    double2 b1 = make_double2(0.0, 0.0);
-    if (b + lane < e) { j1 = __ldg(P.lcol + b + lane); a1 = __ldg(P.lval + b + lane); }
-    if (b + 32 + lane < e) { j2 = __ldg(P.lcol + b + 32 + lane); a2 = __ldg(P.lval + b + 32 + lane); }
-    if (b + lane < e) b1 = load_bnd(P, j1);
+    float a1 = 0.0f, a2 = 0.0f;
+    float2 b1 = make_float2(0.0f, 0.0f);
+    if (b + lane < e) { j1 = __ldg(P.lcol + b + lane); a1 = __ldg(P.la32 + b + lane); }
+    if (b + 32 + lane < e) { j2 = __ldg(P.lcol + b + 32 + lane); a2 = __ldg(P.la32 + b + 32 + lane); }
+    if (b + lane < e) b1 = load_bnd32(P, j1);
     for (int k0 = b; k0 < e; k0 += 32) {
         const int k = k0 + lane;
         const int j = j1;
-        const double a = a1;
-        const double2 bb = b1;
+        const float a = a1;
+        const float2 bb = b1;
         j1 = j2;
         a1 = a2;
-        if (k + 64 < e) { j2 = __ldg(P.lcol + k + 64); a2 = __ldg(P.lval + k + 64); }
-        if (k + 32 < e) b1 = load_bnd(P, j1);
-        const int sides = k < e ? candidate_sides(c, a, bb.x, bb.y) : 0;
+        if (k + 64 < e) { j2 = __ldg(P.lcol + k + 64); a2 = __ldg(P.la32 + k + 64); }
+        if (k + 32 < e) b1 = load_bnd32(P, j1);
+        int sides = k < e ? candidate_sides32(c, a, bb) : 0;
+        if (sides & 4) {
+            const double2 bd = load_bnd(P, j);
+            sides = candidate_sides(c, __ldg(P.lval + k), bd.x, bd.y);
+        }
         queue_push(Q, lane, sides, j, (unsigned)(k - b) << 1);
         queue_drain(Q, lane, false, run);
     }
