@@ -9,9 +9,11 @@
 //            marked row shorter than learn_min_len (the rest stay marked, their
 //            features ageing, so several markings of an unproductive row
 //            coalesce into one later processing);
-//   FLUSH    every marked row -- after a LEARNED round that changed nothing;
-//   FULL     every row -- the first round and after a FLUSH round that
-//            changed nothing (with use_marking == 0, every round).
+//   FLUSH    every marked row -- after a LEARNED round that changed nothing
+//            and met fewer marked rows than an eighth of all rows;
+//   FULL     every row -- the first round, after a FLUSH round that changed
+//            nothing, and after a LEARNED round that changed nothing with
+//            more marked rows than that (with use_marking == 0, every round).
 // Unlike the plain adaptive schedule, a round with many tightenings is not
 // followed by a full sweep: the marks are always pushed, so that rows the
 // model deferred are not swept along.
@@ -86,6 +88,10 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     const int rl = lane >> lg, sub = lane & (g - 1);
     const int r = row0 + rl;
     bool act = rl < nrows && (full || P.dirty[r] != 0);
+    {
+        const unsigned mk = __ballot_sync(kFull, act && sub == 0);
+        if (lane == 0) L.marked += __popc(mk);
+    }
     if (!__any_sync(kFull, act)) return;
     const int len = act ? __ldg(P.srow_len + r) : 0;
     const bool leader0 = act && sub == 0;
@@ -190,8 +196,10 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
 
 __device__ __forceinline__ void learned_activity_phase(const DevProblem &P, int round, int kind, unsigned *ctr,
                                                        int *change, unsigned *tight_ctr, WarpSmem &ws,
-                                                       LearnSmem &L, int lane) {
+                                                       LearnSmem &L, int lane, unsigned long long *marked_ctr) {
     stats_zero(ws, lane);
+    if (lane == 0) L.marked = 0;
+    __syncwarp();
     WarpCursor cur;
     cur.start(ctr, 1u, lane);
     for (;;) {
@@ -202,6 +210,7 @@ __device__ __forceinline__ void learned_activity_phase(const DevProblem &P, int 
         else split_partial(P, -it - 1, lane, round, kind != kRoundFull, change, tight_ctr, ws);
     }
     stats_flush(P, ws, lane);
+    if (lane == 0 && L.marked) atomicAdd(marked_ctr, L.marked);
 }
 
 // Commit changed variables; mark their rows for the next round: SELL rows
@@ -256,12 +265,14 @@ __global__ void __launch_bounds__(kCtaThreads, 2) k_megakernel_learned(DevProble
             int *exact = &P.flags[1 + par].exact;
             unsigned *q = P.queue + 4 * par;
             const bool full = kind == kRoundFull;
-            learned_activity_phase(P, round, kind, q + 0, change, tight, mine, L, lane);
+            learned_activity_phase(P, round, kind, q + 0, change, tight, mine, L, lane,
+                                   &P.flags[1 + par].rows_deferred);
             if (!grid_barrier(P.barrier, err)) return;
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 P.flags[1 + (par ^ 1)].change = 0;
                 P.flags[1 + (par ^ 1)].tight = 0u;
                 P.flags[1 + (par ^ 1)].exact = 0;
+                P.flags[1 + (par ^ 1)].rows_deferred = 0ULL;  // this kernel's per-round marked-row count
                 P.queue[4 * (par ^ 1) + 0] = 0u;
                 P.queue[4 * (par ^ 1) + 1] = 0u;
                 P.queue[4 * (par ^ 1) + 2] = 0u;
@@ -278,7 +289,17 @@ __global__ void __launch_bounds__(kCtaThreads, 2) k_megakernel_learned(DevProble
             const unsigned t = *((volatile unsigned *)tight);
             const bool certified = full && t == 0;
             int next;
-            if (t == 0) next = kind == kRoundLearned ? kRoundFlush : kRoundFull;
+            // a LEARNED round that changed nothing is followed by a FLUSH of the
+            // deferred rows -- or directly by the certifying FULL round when
+            // the marked rows were at least an eighth of all rows (a full
+            // sweep then costs little more than the flush, and one of the two
+            // is saved when nothing is left to tighten)
+            const unsigned long long marked =
+                    *((volatile unsigned long long *)&P.flags[1 + par].rows_deferred);
+            if (t == 0)
+                next = kind == kRoundLearned ? (marked * 8ULL >= (unsigned long long)P.n_srows ? kRoundFull
+                                                                                              : kRoundFlush)
+                                             : kRoundFull;
             else next = P.use_marking == 0 ? kRoundFull : kRoundLearned;
             learned_finalize(P, round, !certified && next != kRoundFull && round < P.max_rounds,
                              blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
