@@ -135,11 +135,24 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         if (len[i] <= Ls) sell_rows.push_back(i);
         else split_rows.push_back(i);
     }
-    // by lanes per row (widest first), then length (longest first), stable
-    std::stable_sort(sell_rows.begin(), sell_rows.end(), [&](int a, int b) {
-        const int ga = lanes_of(len[a]), gb = lanes_of(len[b]);
-        return ga != gb ? ga > gb : len[a] > len[b];
-    });
+    // by lanes per row (widest first), then length (longest first), stable:
+    // lanes_of never decreases with the length, so this is a counting sort by
+    // length, longest first (O(m), no comparisons)
+    {
+        int lmax = 0;
+        for (int i : sell_rows) lmax = std::max(lmax, len[i]);
+        std::vector<int> start((size_t)lmax + 2, 0);
+        for (int i : sell_rows) start[len[i]]++;
+        int acc = 0;
+        for (int L = lmax; L >= 0; L--) {
+            const int c = start[L];
+            start[L] = acc;
+            acc += c;
+        }
+        std::vector<int> sorted(sell_rows.size());
+        for (int i : sell_rows) sorted[start[len[i]]++] = i;
+        sell_rows.swap(sorted);
+    }
     std::stable_sort(split_rows.begin(), split_rows.end(), [&](int a, int b) { return len[a] > len[b]; });
     const int ns = (int)sell_rows.size();
     const std::vector<int> &order = sell_rows;  // row position -> original row
@@ -163,24 +176,20 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     n_slices = (int)slice_lg.size();
     if (slice_lg.empty()) slice_lg.push_back(0);
     sell_elems = slice_ptr[n_slices];
-    std::vector<int> sell_col((size_t)std::max<long long>(sell_elems, 1), 0);
-    std::vector<double> sell_val((size_t)std::max<long long>(sell_elems, 1), 0.0);
-    std::vector<int> srow_len(std::max(ns, 1));
+    // per row position: length, sides, first element of the row-contiguous copy
+    std::vector<int> srow_len(std::max(ns, 1)), xptr(std::max(ns, 1), 0);
     std::vector<double> srow_lhs(std::max(ns, 1)), srow_rhs(std::max(ns, 1));
-#pragma omp parallel for schedule(dynamic, 64)
-    for (int s = 0; s < n_slices; s++) {
-        const int lg = slice_lg[s], g = 1 << lg;
-        for (int p = slice_row0[s]; p < slice_row0[s + 1]; p++) {
-            const int i = order[p], rl = p - slice_row0[s];
-            srow_len[p] = len[i];
-            srow_lhs[p] = lhs[i];
-            srow_rhs[p] = rhs[i];
-            for (int k = 0; k < len[i]; k++) {
-                const long long e = slice_ptr[s] + 32LL * (k >> lg) + (rl << lg) + (k & (g - 1));
-                sell_col[e] = col[row_ptr[i] + k];
-                sell_val[e] = val[row_ptr[i] + k];
-            }
-        }
+#pragma omp parallel for schedule(static)
+    for (int p = 0; p < ns; p++) {
+        const int i = order[p];
+        srow_len[p] = len[i];
+        srow_lhs[p] = lhs[i];
+        srow_rhs[p] = rhs[i];
+    }
+    long long x_elems = 0;
+    for (int p = 0; p < ns; p++) {
+        xptr[p] = (int)x_elems;
+        x_elems += srow_len[p];
     }
     // split rows: CSR-contiguous, warp tiles of split_tile non-zeros
     n_lrows = (int)split_rows.size();
@@ -203,14 +212,6 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     lrow_tile0[n_lrows] = (int)tile_row.size();
     n_tiles = (int)tile_row.size();
     const long long lnnz = lrow_ptr[n_lrows];
-    std::vector<int> lcol((size_t)std::max<long long>(lnnz, 1));
-    std::vector<double> lval((size_t)std::max<long long>(lnnz, 1));
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int r = 0; r < n_lrows; r++) {
-        const int i = split_rows[r];
-        std::memcpy(&lcol[lrow_ptr[r]], &col[row_ptr[i]], sizeof(int) * (size_t)len[i]);
-        std::memcpy(&lval[lrow_ptr[r]], &val[row_ptr[i]], sizeof(double) * (size_t)len[i]);
-    }
     // work items of the activity phase, heaviest first (slices: 32 x width non-zeros)
     std::vector<int> items;
     items.reserve((size_t)n_slices + n_tiles);
@@ -245,42 +246,8 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.slice_ptr, const long long, slice_ptr);
     GDP_UP(P.slice_row0, const int, slice_row0);
     GDP_UP(P.slice_lg, const int, slice_lg);
-    GDP_UP(P.sell_col, const int, sell_col);
-    GDP_UP(P.sell_val, const double, sell_val);
-    {  // FP32 screen copies, made on the device from the uploaded values
-        float *a32 = (float *)arena.alloc_bytes(sizeof(float) * sell_val.size());
-        if (!a32 || launch_coef_screen(P.sell_val, a32, (long long)sell_val.size(), 8 * n_sms, stream) != 0) {
-            set_error("device allocation/launch failed for sell_a32");
-            return GDP_ERROR;
-        }
-        P.sell_a32 = a32;
-    }
     GDP_UP(P.srow_len, const int, srow_len);
-    {  // row-contiguous copy (positions in SELL order) for the deferred exact pass
-        std::vector<int> xptr(std::max(ns, 1), 0);
-        long long acc = 0;
-        for (int p = 0; p < ns; p++) {
-            xptr[p] = (int)acc;
-            acc += len[order[p]];
-        }
-        std::vector<int> xcol((size_t)std::max<long long>(acc, 1));
-        std::vector<double> xval((size_t)std::max<long long>(acc, 1));
-#pragma omp parallel for schedule(dynamic, 1024)
-        for (int p = 0; p < ns; p++) {
-            const int i = order[p];
-            std::memcpy(&xcol[xptr[p]], &col[row_ptr[i]], sizeof(int) * (size_t)len[i]);
-            std::memcpy(&xval[xptr[p]], &val[row_ptr[i]], sizeof(double) * (size_t)len[i]);
-        }
-        GDP_UP(P.xptr, const int, xptr);
-        GDP_UP(P.xcol, const int, xcol);
-        GDP_UP(P.xval, const double, xval);
-        float *a32 = (float *)arena.alloc_bytes(sizeof(float) * xval.size());
-        if (!a32 || launch_coef_screen(P.xval, a32, (long long)xval.size(), 8 * n_sms, stream) != 0) {
-            set_error("device allocation/launch failed for xa32");
-            return GDP_ERROR;
-        }
-        P.xa32 = a32;
-    }
+    GDP_UP(P.xptr, const int, xptr);
     {
         std::vector<int> pos_slice(std::max(ns, 1), 0);
         for (int s = 0; s < n_slices; s++)
@@ -291,15 +258,64 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.srow_rhs, const double, srow_rhs);
     P.n_lrows = n_lrows;
     P.n_tiles = n_tiles;
-    GDP_UP(P.lcol, const int, lcol);
-    GDP_UP(P.lval, const double, lval);
-    {
-        float *a32 = (float *)arena.alloc_bytes(sizeof(float) * lval.size());
-        if (!a32 || launch_coef_screen(P.lval, a32, (long long)lval.size(), 8 * n_sms, stream) != 0) {
-            set_error("device allocation/launch failed for la32");
+    {  // element arrays: the raw CSR goes up once and the device places every
+       // element (SELL slots, row-contiguous copy, split rows), then the FP32
+       // screen copies of the three coefficient arrays
+        const size_t n_sell = (size_t)std::max<long long>(sell_elems, 1);
+        const size_t n_x = (size_t)std::max<long long>(x_elems, 1);
+        const size_t n_l = (size_t)std::max<long long>(lnnz, 1);
+        int *sc = (int *)arena.alloc_bytes(sizeof(int) * n_sell);
+        double *sv = (double *)arena.alloc_bytes(sizeof(double) * n_sell);
+        int *xc = (int *)arena.alloc_bytes(sizeof(int) * n_x);
+        double *xv = (double *)arena.alloc_bytes(sizeof(double) * n_x);
+        int *lc = (int *)arena.alloc_bytes(sizeof(int) * n_l);
+        double *lv = (double *)arena.alloc_bytes(sizeof(double) * n_l);
+        float *sa = (float *)arena.alloc_bytes(sizeof(float) * n_sell);
+        float *xa = (float *)arena.alloc_bytes(sizeof(float) * n_x);
+        float *la = (float *)arena.alloc_bytes(sizeof(float) * n_l);
+        if (!sc || !sv || !xc || !xv || !lc || !lv || !sa || !xa || !la) {
+            set_error("device allocation failed (layout element arrays)");
             return GDP_ERROR;
         }
-        P.la32 = a32;
+        GDP_CUDA(cudaMemsetAsync(sc, 0, sizeof(int) * n_sell, stream));  // padding slots
+        GDP_CUDA(cudaMemsetAsync(sv, 0, sizeof(double) * n_sell, stream));
+        Arena tmp;  // raw CSR and the row maps, freed when the build is done
+        const size_t nz = (size_t)std::max(nnz, 1);
+        int *dcol = (int *)tmp.alloc_bytes(sizeof(int) * nz);
+        double *dval = (double *)tmp.alloc_bytes(sizeof(double) * nz);
+        int *drp = (int *)tmp.alloc_bytes(sizeof(int) * ((size_t)m + 1));
+        int *dord = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
+        int *dspl = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
+        long long *dlrp = (long long *)tmp.alloc_bytes(sizeof(long long) * ((size_t)n_lrows + 1));
+        if (!dcol || !dval || !drp || !dord || !dspl || !dlrp) {
+            set_error("device allocation failed (raw CSR)");
+            return GDP_ERROR;
+        }
+        if (nnz) {
+            GDP_CUDA(cudaMemcpyAsync(dcol, col, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, stream));
+            GDP_CUDA(cudaMemcpyAsync(dval, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, stream));
+        }
+        GDP_CUDA(cudaMemcpyAsync(drp, row_ptr, sizeof(int) * ((size_t)m + 1), cudaMemcpyHostToDevice, stream));
+        if (ns) GDP_CUDA(cudaMemcpyAsync(dord, order.data(), sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, stream));
+        if (n_lrows)
+            GDP_CUDA(cudaMemcpyAsync(dspl, split_rows.data(), sizeof(int) * (size_t)n_lrows, cudaMemcpyHostToDevice,
+                                     stream));
+        GDP_CUDA(cudaMemcpyAsync(dlrp, lrow_ptr.data(), sizeof(long long) * ((size_t)n_lrows + 1),
+                                 cudaMemcpyHostToDevice, stream));
+        LayoutBuild L;
+        L.col = dcol; L.row_ptr = drp; L.val = dval;
+        L.n_srows = ns; L.order = dord; L.pos_slice = P.pos_slice; L.slice_row0 = P.slice_row0;
+        L.slice_lg = P.slice_lg; L.xptr = P.xptr; L.slice_ptr = P.slice_ptr;
+        L.sell_col = sc; L.xcol = xc; L.sell_val = sv; L.xval = xv;
+        L.n_lrows = n_lrows; L.split_rows = dspl; L.lrow_ptr = dlrp; L.lcol = lc; L.lval = lv;
+        GDP_CUDA(build_layout_elements(L, 8 * n_sms, stream));
+        GDP_CUDA(launch_coef_screen(sv, sa, (long long)n_sell, 8 * n_sms, stream));
+        GDP_CUDA(launch_coef_screen(xv, xa, (long long)n_x, 8 * n_sms, stream));
+        GDP_CUDA(launch_coef_screen(lv, la, (long long)n_l, 8 * n_sms, stream));
+        GDP_CUDA(cudaStreamSynchronize(stream));  // before the raw CSR is freed
+        P.sell_col = sc; P.sell_val = sv; P.sell_a32 = sa;
+        P.xcol = xc; P.xval = xv; P.xa32 = xa;
+        P.lcol = lc; P.lval = lv; P.la32 = la;
     }
     GDP_UP(P.lrow_lhs, const double, lrow_lhs);
     GDP_UP(P.lrow_rhs, const double, lrow_rhs);

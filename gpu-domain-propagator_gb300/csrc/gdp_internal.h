@@ -187,6 +187,23 @@ int launch_finalize(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_t s);
 int launch_megakernel(const DevProblem &P, int grid, cudaStream_t s);
 int phase_occupancy(int *act_blocks_per_sm, int *cand_blocks_per_sm, int *mega_blocks_per_sm);
+// gdp_layout.cu: element arrays of the layout from the raw CSR (all device pointers)
+struct LayoutBuild {
+    const int *col, *row_ptr;  // raw CSR
+    const double *val;
+    int n_srows;
+    const int *order;          // row position -> row
+    const int *pos_slice, *slice_row0, *slice_lg, *xptr;
+    const long long *slice_ptr;
+    int *sell_col, *xcol;
+    double *sell_val, *xval;
+    int n_lrows;
+    const int *split_rows;     // split-row slot -> row
+    const long long *lrow_ptr;
+    int *lcol;
+    double *lval;
+};
+int build_layout_elements(const LayoutBuild &L, int blocks, cudaStream_t s);
 // gdp_layout.cu: variable -> row-position index for marking (scratch: n + 2 + (n+1)/1024 ints)
 int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s);
 

@@ -1,4 +1,5 @@
-// gdp_layout.cu -- device-side construction of the marking index: for every
+// gdp_layout.cu -- device-side construction of the layout's element arrays
+// from the raw CSR (below), and of the marking index: for every
 // variable, the row positions (SELL slot or split-row slot) of the rows it
 // appears in. This is the transpose (CSR -> CSC pattern) that the reference
 // computes with cuSPARSE csr2csc on every call (src/kernels/util_kernels.cuh:92-229)
@@ -111,6 +112,54 @@ int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *sc
     e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n1, s);
     if (e != cudaSuccess) return (int)e;
     k_fill_cols<<<blocks, 256, 0, s>>>(P, var_ptr, cnt, var_pos);
+    return (int)cudaGetLastError();
+}
+
+// ---- element arrays from the raw CSR -----------------------------------------
+// The host decides the layout (row order, slices, split-row tiles: O(m) work)
+// and uploads the CSR once; these kernels place every element: SELL slot and
+// row-contiguous copy (warp per row position), split-row arrays (block per
+// split row). Padding slots of the SELL arrays stay as cleared before.
+namespace {
+__global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < L.n_srows; p += nwarps) {
+        const int i = L.order[p];
+        const int s = L.pos_slice[p];
+        const int lg = L.slice_lg[s], g = 1 << lg;
+        const int rl = p - L.slice_row0[s];
+        const long long base = L.slice_ptr[s] + ((long long)rl << lg);
+        const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
+        const long long xb = L.xptr[p];
+        for (int k = lane; k < len; k += 32) {
+            const int c = L.col[b + k];
+            const double v = L.val[b + k];
+            const long long e = base + 32LL * (k >> lg) + (k & (g - 1));
+            L.sell_col[e] = c;
+            L.sell_val[e] = v;
+            L.xcol[xb + k] = c;
+            L.xval[xb + k] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_build_split(LayoutBuild L) {
+    for (int r = blockIdx.x; r < L.n_lrows; r += gridDim.x) {
+        const int i = L.split_rows[r];
+        const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
+        const long long o = L.lrow_ptr[r];
+        for (int k = threadIdx.x; k < len; k += blockDim.x) {
+            L.lcol[o + k] = L.col[b + k];
+            L.lval[o + k] = L.val[b + k];
+        }
+    }
+}
+}  // namespace
+
+int build_layout_elements(const LayoutBuild &L, int blocks, cudaStream_t s) {
+    if (L.n_srows > 0) k_build_sell<<<blocks, 256, 0, s>>>(L);
+    if (L.n_lrows > 0) k_build_split<<<blocks, 256, 0, s>>>(L);
     return (int)cudaGetLastError();
 }
 
