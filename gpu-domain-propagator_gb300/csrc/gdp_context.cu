@@ -17,6 +17,10 @@
 #include <string>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include "gdp_context.h"
 #include "gdp_device.cuh"
 #include "gdp_learned.h"
@@ -128,53 +132,121 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         return g;
     };
     std::vector<int> len(m);
-    for (int i = 0; i < m; i++) len[i] = row_ptr[i + 1] - row_ptr[i];
-    std::vector<int> sell_rows, split_rows;
+    int lmax = 0;  // longest SELL row
+#pragma omp parallel for reduction(max : lmax) schedule(static)
     for (int i = 0; i < m; i++) {
-        if (len[i] == 0) continue;
-        if (len[i] <= Ls) sell_rows.push_back(i);
-        else split_rows.push_back(i);
+        len[i] = row_ptr[i + 1] - row_ptr[i];
+        if (len[i] <= Ls) lmax = std::max(lmax, len[i]);
     }
-    // by lanes per row (widest first), then length (longest first), stable:
-    // lanes_of never decreases with the length, so this is a counting sort by
-    // length, longest first (O(m), no comparisons)
+    // SELL rows (1..Ls non-zeros) by lanes per row (widest first), then length
+    // (longest first), stable: lanes_of never decreases with the length, so
+    // this is a counting sort by length, longest first -- run in parallel over
+    // contiguous row chunks (per-chunk histograms keep it stable). Split rows
+    // (longer than Ls) are collected in row order and sorted by length.
+    std::vector<int> sell_rows, split_rows;
     {
-        int lmax = 0;
-        for (int i : sell_rows) lmax = std::max(lmax, len[i]);
-        std::vector<int> start((size_t)lmax + 2, 0);
-        for (int i : sell_rows) start[len[i]]++;
-        int acc = 0;
-        for (int L = lmax; L >= 0; L--) {
-            const int c = start[L];
-            start[L] = acc;
-            acc += c;
+#ifdef _OPENMP
+        const int nt = lmax <= (1 << 16) ? std::max(1, std::min(omp_get_max_threads(), 64)) : 1;
+#else
+        const int nt = 1;
+#endif
+        const size_t W = (size_t)lmax + 1;  // keys 0..lmax (0: empty rows, skipped)
+        std::vector<int> hist((size_t)nt * W, 0);
+        std::vector<int> nsplit(nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            const int i0 = (int)((long long)m * t / nt), i1 = (int)((long long)m * (t + 1) / nt);
+            int *h = &hist[(size_t)t * W];
+            for (int i = i0; i < i1; i++) {
+                if (len[i] > Ls) nsplit[t + 1]++;
+                else h[len[i]]++;
+            }
         }
-        std::vector<int> sorted(sell_rows.size());
-        for (int i : sell_rows) sorted[start[len[i]]++] = i;
-        sell_rows.swap(sorted);
+        // offsets: longer rows first; within a length, chunks in row order
+        int acc = 0;
+        for (int L = lmax; L >= 1; L--)
+            for (int t = 0; t < nt; t++) {
+                const int c = hist[(size_t)t * W + L];
+                hist[(size_t)t * W + L] = acc;
+                acc += c;
+            }
+        for (int t = 0; t < nt; t++) nsplit[t + 1] += nsplit[t];
+        sell_rows.resize(acc);
+        split_rows.resize(nsplit[nt]);
+#pragma omp parallel num_threads(nt)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            const int i0 = (int)((long long)m * t / nt), i1 = (int)((long long)m * (t + 1) / nt);
+            int *h = &hist[(size_t)t * W];
+            int sp = nsplit[t];
+            for (int i = i0; i < i1; i++) {
+                if (len[i] > Ls) split_rows[sp++] = i;
+                else if (len[i] > 0) sell_rows[h[len[i]]++] = i;
+            }
+        }
     }
     std::stable_sort(split_rows.begin(), split_rows.end(), [&](int a, int b) { return len[a] > len[b]; });
     const int ns = (int)sell_rows.size();
     const std::vector<int> &order = sell_rows;  // row position -> original row
 
     n_srows = ns;
-    std::vector<long long> slice_ptr(1, 0);
-    std::vector<int> slice_row0(1, 0), slice_lg;
-    for (int p = 0; p < ns;) {
-        const int g = lanes_of(len[order[p]]);
-        int lg = 0;
-        while ((1 << lg) < g) lg++;
-        int q = p;
-        const int per = 32 / g;
-        while (q < ns && q - p < per && lanes_of(len[order[q]]) == g) q++;
-        const long long width = (len[order[p]] + g - 1) / g;
-        slice_ptr.push_back(slice_ptr.back() + 32LL * width);
-        slice_row0.push_back(q);
-        slice_lg.push_back(lg);
-        p = q;
+    // slices: the rows of one lanes-per-row class are consecutive positions;
+    // a class of g lanes is cut into slices of 32 / g rows, each as wide as
+    // its first (longest) row
+    std::vector<long long> slice_ptr;
+    std::vector<int> slice_row0, slice_lg;
+    {
+        int cls_lo[6], cls_hi[6], cls_first[6];
+        for (int c = 0; c < 6; c++) { cls_lo[c] = 0; cls_hi[c] = 0; }
+        for (int p = 0; p < ns;) {  // class boundaries: binary search on the sorted lengths
+            const int g = lanes_of(len[order[p]]);
+            int lg = 0;
+            while ((1 << lg) < g) lg++;
+            int lo = p, hi = ns;  // first position of a smaller class
+            while (lo < hi) {
+                const int mid = lo + (hi - lo) / 2;
+                if (lanes_of(len[order[mid]]) == g) lo = mid + 1;
+                else hi = mid;
+            }
+            cls_lo[lg] = p;
+            cls_hi[lg] = lo;
+            p = lo;
+        }
+        int nsl = 0;
+        for (int lg = 5; lg >= 0; lg--) {
+            cls_first[lg] = nsl;
+            const int per = 32 >> lg;
+            nsl += (cls_hi[lg] - cls_lo[lg] + per - 1) / per;
+        }
+        slice_row0.resize((size_t)nsl + 1);
+        slice_lg.resize((size_t)std::max(nsl, 1), 0);
+        slice_ptr.resize((size_t)nsl + 1);
+        std::vector<long long> width((size_t)std::max(nsl, 1), 0);
+        for (int lg = 5; lg >= 0; lg--) {
+            const int per = 32 >> lg, g = 1 << lg, c0 = cls_lo[lg], c1 = cls_hi[lg];
+            const int k_n = (c1 - c0 + per - 1) / per;
+#pragma omp parallel for schedule(static)
+            for (int k = 0; k < k_n; k++) {
+                const int s = cls_first[lg] + k, r0 = c0 + k * per;
+                slice_row0[s] = r0;
+                slice_lg[s] = lg;
+                width[s] = (len[order[r0]] + g - 1) / g;
+            }
+        }
+        slice_row0[nsl] = ns;
+        slice_ptr[0] = 0;
+        for (int s = 0; s < nsl; s++) slice_ptr[s + 1] = slice_ptr[s] + 32LL * width[s];
+        n_slices = nsl;
     }
-    n_slices = (int)slice_lg.size();
-    if (slice_lg.empty()) slice_lg.push_back(0);
     sell_elems = slice_ptr[n_slices];
     // per row position: length, sides, first element of the row-contiguous copy
     std::vector<int> srow_len(std::max(ns, 1)), xptr(std::max(ns, 1), 0);
@@ -218,13 +290,28 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     {
         std::vector<std::pair<long long, int>> cost;
         cost.reserve((size_t)n_slices + n_tiles);
+        long long wmax = 0;
         for (int s = 0; s < n_slices; s++) cost.emplace_back(slice_ptr[s + 1] - slice_ptr[s], s);
         for (int t = 0; t < n_tiles; t++) cost.emplace_back((long long)(tile_end[t] - tile_begin[t]), -t - 1);
-        std::stable_sort(cost.begin(), cost.end(),
-                         [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
-                             return a.first > b.first;
-                         });
-        for (auto &c : cost) items.push_back(c.second);
+        for (auto &c : cost) wmax = std::max(wmax, c.first);
+        if (wmax <= (1 << 20)) {  // stable counting sort, heaviest first
+            std::vector<int> start((size_t)wmax + 2, 0);
+            for (auto &c : cost) start[c.first]++;
+            int acc = 0;
+            for (long long w = wmax; w >= 0; w--) {
+                const int k = start[w];
+                start[w] = acc;
+                acc += k;
+            }
+            items.resize(cost.size());
+            for (auto &c : cost) items[start[c.first]++] = c.second;
+        } else {
+            std::stable_sort(cost.begin(), cost.end(),
+                             [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
+                                 return a.first > b.first;
+                             });
+            for (auto &c : cost) items.push_back(c.second);
+        }
     }
     // ---- upload ----
     auto up = [&](const void *src, size_t bytes) -> void * {
@@ -250,6 +337,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.xptr, const int, xptr);
     {
         std::vector<int> pos_slice(std::max(ns, 1), 0);
+#pragma omp parallel for schedule(static)
         for (int s = 0; s < n_slices; s++)
             for (int p = slice_row0[s]; p < slice_row0[s + 1]; p++) pos_slice[p] = s;
         GDP_UP(P.pos_slice, const int, pos_slice);
@@ -338,6 +426,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // adaptive marking: mark when a round tightened fewer bounds than 1/16 of the variables
     P.mark_threshold = (unsigned)std::max(1, n / 16);
     std::vector<unsigned char> is_cont(std::max(n, 1), 0);
+#pragma omp parallel for schedule(static)
     for (int j = 0; j < n; j++) is_cont[j] = vartype[j] == GDP_CONTINUOUS ? 1 : 0;
     GDP_UP(P.is_cont, const unsigned char, is_cont);
 #undef GDP_UP
