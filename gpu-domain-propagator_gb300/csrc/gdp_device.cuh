@@ -190,13 +190,6 @@ __device__ __forceinline__ float f32_dn(long long b) {
     const unsigned long long mag = (unsigned long long)b & 0x7FFFFFFFFFFFFFFFULL;
     return b < 0 ? -f32_mag(mag, true) : f32_mag(mag, false);
 }
-// FP32 upper bound of |a| (ub - lb) up to two round-to-nearest float errors
-// (covered by the row test's 1 + 2^-20 margin).
-__device__ __forceinline__ float delta_up(long long ab, long long lbb, long long ubb) {
-    const float au = f32_mag((unsigned long long)ab & 0x7FFFFFFFFFFFFFFFULL, true);
-    const float d = __fsub_rn(f32_up(ubb), f32_dn(lbb));
-    return __fmul_rn(au, d);
-}
 constexpr float kUMargin = 1.00000095367431640625f;  // 1 + 2^-20
 
 // Sign-aware FP32 enclosure lo <= |a| (ub - lb) <= hi of one element, each end
@@ -220,8 +213,9 @@ __device__ __forceinline__ DeltaBox delta_box(long long ab, long long lbb, long 
 }
 
 // Activity accumulator: the reference's computeActivities terms with integer
-// classification (no FP64 compares), and an FP32 upper bound U of the maximum
-// of |a| (ub - lb) (used by the row test of rows summed by several lanes).
+// classification (no FP64 compares); U carries the row's FP32 bound of the
+// maximum of |a| (ub - lb) (from the screen, see scr_u_bound), which the row
+// test of rows summed by several lanes uses.
 struct Acc {
     double minact, maxact;
     int minf, maxf;
@@ -243,11 +237,6 @@ __device__ __forceinline__ void acc_add_terms(Acc &s, double a, double lb, doubl
     if (!min_inf) s.minact = dadd(s.minact, dmul(a, gt0 ? lb : ub));
     if (!max_inf) s.maxact = dadd(s.maxact, dmul(a, gt0 ? ub : lb));
 }
-// Terms, infinity counts and the FP32 bound U.
-__device__ __forceinline__ void acc_add(Acc &s, double a, double lb, double ub) {
-    acc_add_terms(s, a, lb, ub);
-    s.U = fmaxf(s.U, delta_up(dbits(a), dbits(lb), dbits(ub)));
-}
 __device__ __forceinline__ void acc_combine(Acc &a, const Acc &b) {
     a.minact = dadd(a.minact, b.minact);
     a.maxact = dadd(a.maxact, b.maxact);
@@ -261,11 +250,13 @@ __device__ __forceinline__ double row_min_slack(double minact, double maxact, do
     const double s = dsub(rhs, minact), t = dsub(maxact, lhs);
     return (t < s) ? t : s;
 }
-// The FP32 row filter: true if no variable of the row can be tightened
-// (U bounds the reference's maxactdelta from above).
+// The row filter of rows summed by several lanes: true if no variable of the
+// row can be tightened. U (scr_u_bound of the row's screen) bounds every
+// FP64 |a| (ub - lb) from above, so U <= mn leaves no candidate for which
+// EPSGT(|a| (ub - lb), slack) holds: skipping such a row changes nothing.
 __device__ __forceinline__ bool u_filter_skips(int minf, int maxf, float U, double mn) {
     if (minf > 1 && maxf > 1) return true;
-    return mn < kInf && (double)__fmul_rn(U, kUMargin) <= mn;
+    return mn < kInf && (double)U <= mn;
 }
 // The reference's decision from its sequential maxactdelta (canConsBeTightened).
 __device__ __forceinline__ bool reference_row_go(int minf, int maxf, double maxactdelta, double mn) {
@@ -401,9 +392,10 @@ __device__ __forceinline__ void scr_combine(Scr &a, const Scr &b) {
 }
 // Largest float not above 1e20 (the infinity threshold).
 constexpr float kInfF32Dn = 0x1.5af1d6p+66f;
-// Upper bound of the row filter's U (delta_up of every element) and of the
-// reference's sequential maxactdelta: the accumulated U widened by 2^-20
-// relative plus 2^-80 absolute (bounds below 2^-126).
+// Upper bound of every FP64 |a| (ub - lb) of the row (each fl(|a| fl(ub - lb)),
+// and so of the reference's sequential maxactdelta), the row filter's U: the
+// accumulated U widened by 2^-20 relative plus 2^-80 absolute (bounds below
+// 2^-126).
 __device__ __forceinline__ float scr_u_bound(const Scr &c) { return __fmaf_ru(c.U, kUMargin, 0x1p-80f); }
 // Enclosure [mn_lo, mn_hi] of min(rhs - minact, maxact - lhs) as the exact
 // pass computes it in FP64 for a row of n elements: the activities lie within

@@ -34,7 +34,7 @@ namespace gdp {
 struct TilePart {
     double minact, maxact;
     int minf, maxf;
-    float U;  // FP32 upper bound of max |a|(ub - lb)
+    float U;  // the row's FP32 bound of max |a|(ub - lb) (from its screen)
     int pad;
 };
 
@@ -44,6 +44,8 @@ struct TilePart {
 struct XRow {
     long long base;
     int pos, len;
+    float u_hi;  // rows summed by several lanes: the screen's bound of max |a| (ub - lb)
+    int pad;
 };
 
 // FP32 screen partial of a split-row tile (see Scr in gdp_device.cuh).

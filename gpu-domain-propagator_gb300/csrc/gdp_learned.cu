@@ -166,9 +166,11 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     if (g > 1) scr_group_reduce(c, g);
     bool exact = false;
     float2 st = make_float2(0.f, 0.f);
+    float u_hi = 0.0f;
     if (leader) {
         exact = !scr_skips(c, len, lhs, rhs);
         st = screen_stats(c, len, lhs, rhs);
+        u_hi = scr_u_bound(c);
     }
     count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
@@ -176,7 +178,8 @@ __device__ __forceinline__ void sell_slice_learned(const DevProblem &P, int slic
     if (__any_sync(kFull, exact)) {
         ws.base[lane] = base;
         __syncwarp();
-        sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws, L.tight, L.go);
+        sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, u_hi, change, tight_ctr, ws, L.tight,
+                        L.go);
     }
     __syncwarp();
     if (leader) {

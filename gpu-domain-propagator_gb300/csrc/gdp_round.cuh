@@ -338,7 +338,7 @@ __device__ __forceinline__ ElemView sell_view(const DevProblem &P) {
 //   pass 2: candidates through the warp division queue.
 __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemView ev, int lg, int lane,
                                                 bool exact, int len,
-                                                int cnt, double lhs, double rhs, int *change,
+                                                int cnt, double lhs, double rhs, float u_hi, int *change,
                                                 unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
                                                 int *row_go = nullptr) {
     const int g = 1 << lg;
@@ -377,12 +377,12 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
             const int j = __ldg(col + st * i);
             const double a = __ldg(val + st * i);
             const double2 b = load_bnd(P, j);
-            acc_add(s, a, b.x, b.y);
+            acc_add_terms(s, a, b.x, b.y);
         }
         acc_group_reduce(s, g);
         if (leader) {
             mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
-            dec = u_filter_skips(s.minf, s.maxf, s.U, mn) ? 0 : 1;
+            dec = u_filter_skips(s.minf, s.maxf, u_hi, mn) ? 0 : 1;
         }
     }
     {
@@ -471,6 +471,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     // FP32 screen
     bool exact = false;
     double lhs = 0.0, rhs = 0.0;
+    float u_hi = 0.0f;  // the row's bound of max |a| (ub - lb), leaders
     {
         const int *col = P.sell_col + base;
         const float *val = P.sell_a32 + base;
@@ -487,6 +488,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
             lhs = __ldg(P.srow_lhs + r);
             rhs = __ldg(P.srow_rhs + r);
             exact = !scr_skips(c, len, lhs, rhs);
+            u_hi = scr_u_bound(c);
         }
     }
     count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
@@ -496,14 +498,14 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         unsigned first = 0;
         if (lane == 0) first = atomicAdd(P.xctr + 16 * par + lg, (unsigned)__popc(bal));
         first = __shfl_sync(kFull, first, 0);
-        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len};
+        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len, u_hi, 0};
         return;
     }
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
     if (!__any_sync(kFull, exact)) return;
     ws.base[lane] = base;
     __syncwarp();
-    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, change, tight_ctr, ws);
+    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, u_hi, change, tight_ctr, ws);
 }
 
 // K slices of one-lane rows (g = 1) screened together in the deferred-exact
@@ -582,7 +584,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k]};
+        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k], 0.0f, 0};
         first += __popc(bal[k]);
     }
 }
@@ -606,11 +608,13 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             int len = 0, cnt = 0;
             long long base = 0;
             double lhs = 0.0, rhs = 0.0;
+            float u_hi = 0.0f;
             if (exact) {
                 const XRow x = P.xrow[P.cls_begin[lg] + k];
                 const int p = x.pos;
                 base = x.base + sub;
                 len = x.len;
+                u_hi = x.u_hi;
                 cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
                 if (sub == 0) {
                     lhs = __ldg(P.srow_lhs + p);
@@ -619,8 +623,8 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             }
             ws.base[lane] = base;
             __syncwarp();
-            sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, change,
-                            tight_ctr, ws);
+            sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, u_hi,
+                            change, tight_ctr, ws);
             __syncwarp();
         }
     }
@@ -726,7 +730,7 @@ __device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int
         const int j = __ldg(P.lcol + k);
         const double a = __ldg(P.lval + k);
         const double2 bb = load_bnd(P, j);
-        acc_add(s, a, bb.x, bb.y);
+        acc_add_terms(s, a, bb.x, bb.y);
     }
     acc_shfl_reduce(s);
     return s;
@@ -767,7 +771,8 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     }
     if (!single) return true;
     if (!__shfl_sync(kFull, exact, 0)) return false;
-    const Acc s = tile_exact(P, b, e, lane);
+    Acc s = tile_exact(P, b, e, lane);
+    s.U = scr_u_bound(c);  // lane 0 decides with it
     split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, ws);
     return false;
 }
@@ -800,8 +805,11 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
     const Acc s = tile_exact(P, b, e, lane);
     if (lane == 0) {
+        // every tile of the row carries the row's bound of max |a| (ub - lb)
         TilePart tp;
-        tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf; tp.U = s.U; tp.pad = 0;
+        tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf;
+        tp.U = scr_u_bound(c);
+        tp.pad = 0;
         P.tile_part[t] = tp;
         ws.st_exact += (unsigned long long)(e - b);
         if (t == t0) {

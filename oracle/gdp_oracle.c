@@ -165,8 +165,10 @@ static inline void atomic_min_d(double *addr, double v);
  *     shuffle tree combines the group; longer rows are summed per warp tile
  *     of split_tile non-zeros (lane l sums elements l, l+32, ... of the tile,
  *     shuffle tree over 32 lanes), tile partials combined in tile order.
- * U is computed from the doubles by integer rounding to float (outward) and
- * two round-to-nearest float operations, identically here and on the GPU. */
+ * U is the GPU screen's bound of max |a| (ub - lb): the maximum, NaN
+ * propagating, of |a32| * fma(|ub32| + |lb32|, 2^-21, ub32 - lb32) over the
+ * round-to-nearest float copies of the coefficients and bounds (screen_coef,
+ * screen_bound), evaluated in float exactly like the GPU. */
 typedef struct {
     double minact, maxact;
     int minf, maxf;
@@ -176,31 +178,41 @@ typedef struct {
 static inline uint64_t dbits(double x) { uint64_t b; memcpy(&b, &x, 8); return b; }
 static inline float fbits(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
 
-/* magnitude bits of a double -> float magnitude rounded up (up=1) or down */
-static inline float f32_mag(uint64_t mag, int up) {
-    const int e = (int)(mag >> 52);
-    if (e == 2047) return (mag & 0xFFFFFFFFFFFFFULL) ? fbits(0x7FC00000u) : fbits(0x7F800000u);
-    const int fe = e - 1023 + 127;
-    if (fe >= 255) return up ? fbits(0x7F800000u) : fbits(0x7F7FFFFFu);
-    if (fe <= 0) return (up && mag) ? fbits(0x00800000u) : 0.0f;
-    const uint64_t man = mag & 0xFFFFFFFFFFFFFULL;
-    uint32_t fb = ((uint32_t)fe << 23) | (uint32_t)(man >> 29);
-    if (up && (man & 0x1FFFFFFFULL)) fb += 1u;
-    return fbits(fb);
+/* FP32 copies the GPU screen reads: coefficients in (0, 1e-9] -> NaN, above
+ * 2^40 in magnitude -> +-inf, non-zero below 2^-60 -> NaN with a's sign;
+ * bounds counted as infinite (lb <= -1e20, ub >= 1e20) -> -inf / +inf, finite
+ * bounds above 2^100 in magnitude -> NaN; all else round-to-nearest. */
+static inline float screen_coef(double a) {
+    const double m = fabs(a);
+    if (a > 0.0 && a <= O_EPS) return NAN;
+    if (m > 0x1p40) return a > 0 ? INFINITY : -INFINITY;
+    if (m != 0.0 && m < 0x1p-60) return a > 0 ? NAN : -NAN;
+    return (float)a;
 }
-/* float >= x (rounded toward +inf) and float <= x (toward -inf) */
-static inline float f32_up(double x) {
-    const uint64_t b = dbits(x), mag = b & 0x7FFFFFFFFFFFFFFFULL;
-    return (b >> 63) ? -f32_mag(mag, 0) : f32_mag(mag, 1);
+static inline float screen_bound(double x, int upper) {
+    if (upper ? x >= O_INF : x <= -O_INF) return upper ? INFINITY : -INFINITY;
+    if (fabs(x) > 0x1p100 || isnan(x)) return NAN;
+    return (float)x;
 }
-static inline float f32_dn(double x) {
-    const uint64_t b = dbits(x), mag = b & 0x7FFFFFFFFFFFFFFFULL;
-    return (b >> 63) ? -f32_mag(mag, 1) : f32_mag(mag, 0);
+static inline float max_nan(float a, float b) { return (isnan(a) || isnan(b)) ? NAN : (a > b ? a : b); }
+static inline float screen_delta(double coeff, double l, double u) {
+    const float a = screen_coef(coeff), l32 = screen_bound(l, 0), u32 = screen_bound(u, 1);
+    const float d = u32 - l32, w = fabsf(u32) + fabsf(l32);
+    return fabsf(a) * fmaf(w, 0x1p-21f, d);
 }
-static inline float delta_up(double coeff, double l, double u) {
-    const float au = f32_mag(dbits(coeff) & 0x7FFFFFFFFFFFFFFFULL, 1);
-    const float d = f32_up(u) - f32_dn(l);
-    return au * d;
+/* float(U * (1 + 2^-20) + 2^-80) rounded upwards (the GPU's __fmaf_ru), from
+ * exact double arithmetic: U * (1 + 2^-20) has at most 45 significant bits. */
+static inline float ru_float(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = nextafterf(f, INFINITY);
+    return f;
+}
+static inline float u_bound(float U) {
+    if (isnan(U)) return U;
+    const double y = (double)U * (1.0 + 0x1p-20);
+    if (y < 0x1p-27) return ru_float(y + 0x1p-80); /* exact in double */
+    const float fy = ru_float(y);
+    return ((double)fy - y >= 0x1p-80) ? fy : nextafterf(fy, INFINITY);
 }
 
 static inline void gacc_init(gacc *s) { s->minact = 0.0; s->maxact = 0.0; s->minf = 0; s->maxf = 0; s->U = 0.0f; }
@@ -214,7 +226,7 @@ static inline void gacc_add(gacc *s, double coeff, double l, double u) {
     s->maxf += max_inf;
     if (!min_inf) s->minact = s->minact + (coeff > 0 ? coeff * l : coeff * u);
     if (!max_inf) s->maxact = s->maxact + (coeff > 0 ? coeff * u : coeff * l);
-    s->U = fmaxf(s->U, delta_up(coeff, l, u));
+    s->U = max_nan(s->U, screen_delta(coeff, l, u));
 }
 
 static inline void gacc_combine(gacc *a, const gacc *b) {
@@ -222,7 +234,7 @@ static inline void gacc_combine(gacc *a, const gacc *b) {
     a->maxact = a->maxact + b->maxact;
     a->minf += b->minf;
     a->maxf += b->maxf;
-    a->U = fmaxf(a->U, b->U);
+    a->U = max_nan(a->U, b->U);
 }
 
 static gacc gacc_tile(int b, int e, const int *col, const double *val, const double *lb, const double *ub) {
@@ -282,8 +294,8 @@ int gdpo_gpu_row_go(double minact, double maxact, int minf, int maxf, float U, d
     if (minf > 1 && maxf > 1) return 0;
     const double s = rhs - minact, t = maxact - lhs;
     const double mn = (t < s) ? t : s;
-    const float Um = U * 1.00000095367431640625f; /* 1 + 2^-20 */
-    if (mn < O_INF && (double)Um <= mn) return 0;
+    const float Ub = u_bound(U);
+    if (mn < O_INF && (double)Ub <= mn) return 0;
     return 1;
 }
 
