@@ -30,7 +30,7 @@
 #include <chrono>
 #include <cstring>
 
-#include "gdp_round.cuh"
+#include "gdp_learned.cuh"
 
 namespace gdp {
 
@@ -76,6 +76,24 @@ __device__ __forceinline__ void queue_position(const BatchDev &B, const DevProbl
     } else {
         const int row = p - Pu.n_srows;
         for (int t = __ldg(Pu.lrow_tile0 + row); t < __ldg(Pu.lrow_tile0 + row + 1); t++) push_entry(B, par, u, -t - 1);
+    }
+}
+
+// Learned units: variable j of unit u changed; its SELL rows turn dirty and
+// their slices are queued for round `stamp`, its split rows are marked and
+// their tiles queued (as in learned_mark_position).
+__device__ __forceinline__ void mark_var_rows_learned(const BatchDev &B, const DevProblem &Pu, int u, int j,
+                                                      int stamp) {
+    for (int k = __ldg(Pu.var_ptr + j); k < __ldg(Pu.var_ptr + j + 1); k++) {
+        const int p = __ldg(Pu.var_pos + k);
+        if (p < Pu.n_srows) {
+            atomicAdd(Pu.dcount + p, 1);
+            if (Pu.dirty[p] == 0) atomicCAS(Pu.dirty + p, 0, stamp);
+            const int s = __ldg(Pu.pos_slice + p);
+            if (atomicExch(Pu.slice_stamp + s, stamp) != stamp) push_entry(B, stamp & 1, u, s);
+        } else if (atomicExch(Pu.mark + p, stamp) != stamp) {
+            queue_position(B, Pu, u, p, stamp);
+        }
     }
 }
 
@@ -129,11 +147,32 @@ __device__ void build_full_sweep_list(const BatchDev &B, Pred &&pred) {
     }
 }
 
+// The kind of round r + 1 of learned unit Pu after round r.
+__device__ __forceinline__ int unit_next_kind(const DevProblem &Pu, int r) {
+    const RoundFlags &fr = Pu.flags[1 + (r & 1)];
+    return learned_next_kind(fr.kind, fr.tight, fr.rows_deferred, Pu.n_srows, Pu.use_marking);
+}
+// A learned unit is finished after round r when it turned infeasible or a
+// FULL round changed nothing (its certification).
+__device__ __forceinline__ bool unit_certified(const DevProblem &Pu, int r) {
+    const RoundFlags &fr = Pu.flags[1 + (r & 1)];
+    return fr.kind == kRoundFull && fr.tight == 0u;
+}
+
 // Round bookkeeping of unit u after round r (every phase of r is complete).
 __device__ __forceinline__ void close_round(const BatchDev &B, int u, int r) {
     RoundFlags &f0 = B.units[u].flags[0];
     if (f0.done) return;
     f0.rounds = r;
+    if (B.units[u].learned == 1) {
+        const bool cert = unit_certified(B.units[u], r);
+        if (B.units[u].flags[1 + (r & 1)].kind == kRoundFull) f0.full_rounds += 1;
+        if (f0.infeasible || cert || r >= B.max_rounds) {
+            f0.done = 1;
+            f0.change = (f0.infeasible || cert) ? B.units[u].flags[1 + (r & 1)].change : 1;
+        }
+        return;
+    }
     const int ch = B.units[u].flags[1 + (r & 1)].change;
     if (f0.infeasible) {
         f0.done = 1;
@@ -161,21 +200,28 @@ namespace {
 //   F  commit changed variables of every unit; mark and queue rows for r + 1
 //      (units staying on marked rounds), full-sweep list for r + 1.
 // After F every CTA reads the same next-round work size and leaves together.
-__global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
+// kLearned: units with a model (learned == 1) run learned rounds (gdp_learned.cu)
+// -- each unit its own sequence of FULL / LEARNED / FLUSH rounds, the kind of
+// round r in flags[1 + (r & 1)].kind; a slice whose marked rows the model
+// deferred is queued again for the next round, and a unit ends only with a FULL
+// round that changes nothing, exactly as in its single-problem learned run.
+template <bool kLearned>
+__global__ void __launch_bounds__(kCtaThreads, kLearned ? 2 : 3) k_batch_loop(BatchDev B) {
     __shared__ WarpSmem ws[kWarpsPerCta];
+    __shared__ LearnSmem ls[kLearned ? kWarpsPerCta : 1];
     const int lane = threadIdx.x & 31;
     WarpSmem &mine = ws[threadIdx.x >> 5];
+    LearnSmem &L = ls[kLearned ? (threadIdx.x >> 5) : 0];
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = gridDim.x * blockDim.x;
     int last = 0;
     for (int r = 1; r <= B.max_rounds; r++) {
         const int par = r & 1;
         unsigned *ctr = B.ctr + 4 * par;
         // close round r - 1 for every unit (its flags are final); the entry
-        // queue of round r - 1 (parity par ^ 1) is free again: round r's F
-        // phase, behind barrier A, fills it for round r + 1
+        // queue of round r - 1 (parity par ^ 1) was emptied in its phase B and
+        // fills for round r + 1 (phase A: slices with deferred rows, phase F)
         if (r > 1)
             for (int u = gtid; u < B.n_units; u += gthreads) close_round(B, u, r - 1);
-        if (gtid == 0) B.tail[par ^ 1] = 0u;
         // ---- A
         {
             const int nfs = *((volatile int *)B.n_fs);
@@ -203,7 +249,22 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
                 if (*((volatile int *)&Pu.flags[0].infeasible)) continue;
                 int *change = &Pu.flags[1 + par].change;
                 unsigned *tight = &Pu.flags[1 + par].tight;
-                if (it >= 0) {
+                if (kLearned && Pu.learned == 1) {
+                    const int kind = Pu.flags[1 + par].kind;
+                    if (it >= 0) {
+                        if (lane == 0) L.marked = 0;
+                        __syncwarp();
+                        const bool deferred = sell_slice_learned(Pu, it, lane, r, kind, change, tight, mine, L);
+                        if (lane == 0) {
+                            if (L.marked) atomicAdd(&Pu.flags[1 + par].rows_deferred, L.marked);
+                            if (deferred && r < B.max_rounds && atomicExch(Pu.slice_stamp + it, r + 1) != r + 1)
+                                push_entry(B, par ^ 1, u, it);
+                        }
+                    } else if (split_partial(Pu, -it - 1, lane, r, kind != kRoundFull, change, tight, mine) &&
+                               lane == 0) {
+                        push_tile(B.cq, B.tail + 2, B.cap_tiles, B.error, u, -it - 1);
+                    }
+                } else if (it >= 0) {
                     sell_slice(Pu, it, lane, r, marked, change, tight, mine);
                 } else if (split_partial(Pu, -it - 1, lane, r, marked, change, tight, mine) && lane == 0) {
                     push_tile(B.cq, B.tail + 2, B.cap_tiles, B.error, u, -it - 1);
@@ -216,10 +277,12 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
         if (gtid == 0) {
             unsigned *nctr = B.ctr + 4 * (par ^ 1);
             nctr[0] = 0u; nctr[1] = 0u; nctr[2] = 0u;
+            B.tail[par] = 0u;  // round r's entry queue is consumed; it fills again in round r + 1
         }
         for (int u = gtid; u < B.n_units; u += gthreads) {
             RoundFlags &fn = B.units[u].flags[1 + (par ^ 1)];
             fn.change = 0; fn.tight = 0u; fn.exact = 0;
+            fn.rows_deferred = 0ULL;  // learned units: marked rows met in the round
         }
         const int n_cq = (int)min(*((volatile unsigned *)(B.tail + 2)), B.cap_tiles);
         if (n_cq) {
@@ -255,6 +318,9 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
             if (more)
                 build_full_sweep_list(B, [&](int u) {
                     const DevProblem &Pu = B.units[u];
+                    if (kLearned && Pu.learned == 1)
+                        return !Pu.flags[0].done && !Pu.flags[0].infeasible && !unit_certified(Pu, r) &&
+                               unit_next_kind(Pu, r) == kRoundFull;
                     return !Pu.flags[0].done && Pu.flags[1 + par].change && !unit_next_marked(Pu, r);
                 });
             else if (threadIdx.x == 0) {
@@ -262,7 +328,23 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
                 B.fs_prefix[0] = 0;
             }
             if (threadIdx.x == 0) { B.tail[2] = 0u; B.tail[3] = 0u; }
+            if (kLearned) {  // learned units that need round r + 1 even without queued work
+                __shared__ int s_pend;
+                if (threadIdx.x == 0) s_pend = 0;
+                __syncthreads();
+                for (int u = threadIdx.x; u < B.n_units; u += blockDim.x) {
+                    const DevProblem &Pu = B.units[u];
+                    if (Pu.learned == 1 && more && !Pu.flags[0].done && !Pu.flags[0].infeasible &&
+                        !unit_certified(Pu, r))
+                        atomicAdd(&s_pend, 1);
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) B.n_pending[0] = s_pend;
+            }
         }
+        if (kLearned)
+            for (int u = gtid; u < B.n_units; u += gthreads)
+                if (B.units[u].learned == 1) B.units[u].flags[1 + (par ^ 1)].kind = unit_next_kind(B.units[u], r);
         for (int w = gtid; w < B.total_words; w += gthreads) {
             const int u = find_unit(B.wbase, B.n_units, w);
             const DevProblem &Pu = B.units[u];
@@ -271,7 +353,9 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
             if (!bits) continue;
             Pu.chg[wl] = 0u;
             atomicAdd(&Pu.flags[0].changed_vars, (unsigned long long)__popc(bits));  // per word, per unit
-            const bool push = more && unit_next_marked(Pu, r);
+            const bool lrn = kLearned && Pu.learned == 1;
+            const bool push = more && (lrn ? (!unit_certified(Pu, r) && unit_next_kind(Pu, r) != kRoundFull)
+                                           : unit_next_marked(Pu, r));
             while (bits) {
                 const int j = wl * 32 + __ffs(bits) - 1;
                 bits &= bits - 1;
@@ -282,7 +366,10 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
                     Pu.flags[0].infeasible = 1;
                     atomicMin(&Pu.flags[0].infeasible_var, j);
                 }
-                if (push) mark_var_rows(B, Pu, u, j, r + 1);
+                if (push) {
+                    if (lrn) mark_var_rows_learned(B, Pu, u, j, r + 1);
+                    else mark_var_rows(B, Pu, u, j, r + 1);
+                }
             }
         }
         if (!grid_barrier(B.barrier, B.error)) return;
@@ -290,7 +377,8 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
         const int nfs = *((volatile int *)B.n_fs);
         const int next = *((volatile int *)(B.fs_prefix + nfs)) +
                          (int)min(*((volatile unsigned *)(B.tail + (par ^ 1))), B.cap_entries);
-        if (!more || next == 0) break;
+        const int pending = kLearned ? *((volatile int *)B.n_pending) : 0;
+        if (!more || (next == 0 && pending == 0)) break;
     }
     for (int u = gtid; u < B.n_units; u += gthreads) close_round(B, u, last);
     if (gtid == 0) B.rounds_out[0] = last;
@@ -321,6 +409,15 @@ __global__ void __launch_bounds__(256) k_batch_init(BatchDev B, const double *lb
         Pu.slice_stamp[s] = 0;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < Pu.n_lrows; r += gridDim.x * blockDim.x)
         Pu.row_exact[r] = 0;
+    if (Pu.learned == 1)
+        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Pu.n_srows; p += gridDim.x * blockDim.x) {
+            Pu.dirty[p] = 0;
+            Pu.dcount[p] = 0;
+            Pu.last_proc[p] = 0;
+            Pu.last_tight[p] = 0;
+            Pu.rstat[p] = make_float2(0.f, 0.f);
+            Pu.rinfo[p] = 0u;
+        }
 }
 
 // Round-1 marks of units started from a certified fixpoint `ref` of their
@@ -362,13 +459,14 @@ __global__ void __launch_bounds__(256) k_batch_fini(BatchDev B, double *lb, doub
 }  // namespace
 
 // ---- launchers --------------------------------------------------------------
-int batch_occupancy(int *blocks_per_sm) {
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_loop, kCtaThreads, 0);
+int batch_occupancy(int *blocks_per_sm, bool learned) {
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            blocks_per_sm, learned ? k_batch_loop<true> : k_batch_loop<false>, kCtaThreads, 0);
 }
 
 int launch_batch(const BatchDev &B, int grid, const double *lb, const double *ub, double *lb_out,
                  double *ub_out, const long long *var_base, int max_unit_n, const double2 *ref,
-                 const int *seed_mode, cudaStream_t s) {
+                 const int *seed_mode, bool learned, cudaStream_t s) {
     const dim3 vgrid((unsigned)std::max(1, std::min((max_unit_n + 255) / 256, 64)), (unsigned)B.n_units);
     k_batch_init<<<vgrid, 256, 0, s>>>(B, lb, ub, var_base);
     cudaError_t e = cudaGetLastError();
@@ -381,7 +479,8 @@ int launch_batch(const BatchDev &B, int grid, const double *lb, const double *ub
     if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
     BatchDev Bc = B;
     void *args[] = {&Bc};
-    e = cudaLaunchCooperativeKernel((const void *)k_batch_loop, dim3(grid), dim3(kCtaThreads), args, 0, s);
+    e = cudaLaunchCooperativeKernel(learned ? (const void *)k_batch_loop<true> : (const void *)k_batch_loop<false>,
+                                    dim3(grid), dim3(kCtaThreads), args, 0, s);
     if (e != cudaSuccess) return (int)e;
     k_batch_fini<<<vgrid, 256, 0, s>>>(B, lb_out, ub_out, var_base);
     return (int)cudaGetLastError();

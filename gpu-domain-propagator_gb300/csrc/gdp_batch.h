@@ -27,12 +27,13 @@ struct BatchDev {
     unsigned *barrier;    // {count, generation}
     int *error;
     int *rounds_out;
+    int *n_pending;       // learned units that need the next round (learned batches)
 };
 
 int launch_batch(const BatchDev &B, int grid, const double *lb, const double *ub, double *lb_out,
                  double *ub_out, const long long *var_base, int max_unit_n, const double2 *ref,
-                 const int *seed_mode, cudaStream_t s);
-int batch_occupancy(int *blocks_per_sm);
+                 const int *seed_mode, bool learned, cudaStream_t s);
+int batch_occupancy(int *blocks_per_sm, bool learned);
 
 class Batch {
 public:
@@ -46,6 +47,8 @@ public:
     GDP_RETCODE init_nodes(Context *ctx, int n_nodes);
     // lbs[k], ubs[k]: member k's bounds (host, in/out).
     GDP_RETCODE propagate(double *const *lbs, double *const *ubs, gdp_stats *member_stats, gdp_stats *total);
+    // Instance batches: learned row marking for every member (m == nullptr: off).
+    GDP_RETCODE set_model(const Mlp *m, float threshold, int min_len);
 
     int n_units = 0;
     bool nodes = false;
@@ -56,11 +59,14 @@ public:
 
 private:
     GDP_RETCODE finish_init(int device, int ctas_per_sm);
+    GDP_RETCODE size_grid();
     GDP_RETCODE enqueue(cudaStream_t s);
 
     std::vector<std::unique_ptr<Context>> inst_;  // instances (units in heaviest-first order)
     Context *base_ = nullptr;                     // nodes
     std::vector<int> member_of_unit_;             // unit -> member index of the caller
+    bool learned_ = false;                        // members run learned rounds (set_model)
+    int device_ = 0, ctas_per_sm_ = 0;
     std::vector<DevProblem> units_h_;
     std::vector<long long> var_base_;             // unit -> first variable in the staging buffers
     long long total_vars_ = 0;

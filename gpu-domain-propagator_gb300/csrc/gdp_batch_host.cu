@@ -177,9 +177,10 @@ GDP_RETCODE Batch::finish_init(int device, int ctas_per_sm) {
     B_.n_fs = (int *)dev(sizeof(int));
     B_.barrier = (unsigned *)dev(sizeof(unsigned) * 2);
     // error and rounds_out adjacent: one copy reads both
-    int *misc = (int *)dev(sizeof(int) * 2);
+    int *misc = (int *)dev(sizeof(int) * 3);
     B_.error = misc;
     B_.rounds_out = misc + 1;
+    B_.n_pending = misc + 2;
     d_lb_ = (double *)dev(sizeof(double) * (size_t)total_vars_);
     d_ub_ = (double *)dev(sizeof(double) * (size_t)total_vars_);
     d_var_base_ = (long long *)dev(sizeof(long long) * (size_t)(n_units + 1));
@@ -195,12 +196,54 @@ GDP_RETCODE Batch::finish_init(int device, int ctas_per_sm) {
                               cudaMemcpyHostToDevice, stream_));
     GDP_BCUDA(cudaMemcpyAsync(d_var_base_, var_base_.data(), sizeof(long long) * (size_t)(n_units + 1),
                               cudaMemcpyHostToDevice, stream_));
-    int bps = 0, sms = 0;
-    GDP_BCUDA((cudaError_t)batch_occupancy(&bps));
-    GDP_BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    if (ctas_per_sm > 0) bps = std::min(bps, ctas_per_sm);
-    grid = std::max(1, bps) * sms;
+    device_ = device;
+    ctas_per_sm_ = ctas_per_sm;
+    if (size_grid() != GDP_OKAY) return GDP_ERROR;
     GDP_BCUDA(cudaStreamSynchronize(stream_));
+    return GDP_OKAY;
+}
+
+// Cooperative grid of the batch loop instantiation in use.
+GDP_RETCODE Batch::size_grid() {
+    int bps = 0, sms = 0;
+    GDP_BCUDA((cudaError_t)batch_occupancy(&bps, learned_));
+    GDP_BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+    if (ctas_per_sm_ > 0) bps = std::min(bps, ctas_per_sm_);
+    grid = std::max(1, bps) * sms;
+    return GDP_OKAY;
+}
+
+GDP_RETCODE Batch::set_model(const Mlp *m, float threshold, int min_len) {
+    if (nodes) {
+        set_error("learned marking in a batch needs instance members");
+        return GDP_ERROR;
+    }
+    GDP_BCUDA(cudaStreamSynchronize(stream_));
+    for (int u = 0; u < n_units; u++) {
+        if (inst_[u]->set_model(m, threshold, min_len) != GDP_OKAY) return GDP_ERROR;
+        const DevProblem &S = inst_[u]->P;
+        DevProblem &Q = units_h_[u];
+        Q.learned = S.learned;
+        Q.tau = S.tau;
+        Q.learn_min_len = S.learn_min_len;
+        Q.mlp = S.mlp;
+        Q.dirty = S.dirty;
+        Q.dcount = S.dcount;
+        Q.last_proc = S.last_proc;
+        Q.last_tight = S.last_tight;
+        Q.rstat = S.rstat;
+        Q.rinfo = S.rinfo;
+        Q.trace_n = S.trace_n;
+    }
+    learned_ = m != nullptr;
+    GDP_BCUDA(cudaMemcpyAsync(B_.units, units_h_.data(), sizeof(DevProblem) * (size_t)n_units,
+                              cudaMemcpyHostToDevice, stream_));
+    GDP_BCUDA(cudaStreamSynchronize(stream_));
+    if (size_grid() != GDP_OKAY) return GDP_ERROR;
+    // the captured graph holds the other loop instantiation and grid: capture again
+    if (graph_exec_) { cudaGraphExecDestroy(graph_exec_); graph_exec_ = nullptr; }
+    if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+    graph_failed_ = false;
     return GDP_OKAY;
 }
 
@@ -217,11 +260,11 @@ GDP_RETCODE Batch::enqueue(cudaStream_t s) {
     GDP_BCUDA(cudaMemsetAsync(B_.ctr, 0, sizeof(unsigned) * 8, s));
     GDP_BCUDA(cudaMemsetAsync(B_.tail, 0, sizeof(unsigned) * 4, s));
     GDP_BCUDA(cudaMemsetAsync(B_.barrier, 0, sizeof(unsigned) * 2, s));
-    GDP_BCUDA(cudaMemsetAsync(B_.error, 0, sizeof(int) * 2, s));
+    GDP_BCUDA(cudaMemsetAsync(B_.error, 0, sizeof(int) * 3, s));
     // external records: inside a stream capture they become graph event nodes
     GDP_BCUDA(cudaEventRecordWithFlags(ev0_, s, cudaEventRecordExternal));
     GDP_BCUDA((cudaError_t)launch_batch(B_, grid, d_lb_, d_ub_, d_lb_, d_ub_, d_var_base_, max_unit_n_, ref_,
-                                        d_seed_mode_, s));
+                                        d_seed_mode_, learned_, s));
     GDP_BCUDA(cudaEventRecordWithFlags(ev1_, s, cudaEventRecordExternal));
     if (vbytes) {
         GDP_BCUDA(cudaMemcpyAsync(h_lb_, d_lb_, vbytes, cudaMemcpyDeviceToHost, s));
@@ -316,6 +359,8 @@ GDP_RETCODE Batch::propagate(double *const *lbs, double *const *ubs, gdp_stats *
         st.rows_processed = (long long)f.rows_proc;
         st.nnz_processed = (long long)f.nnz_proc;
         st.nnz_exact = (long long)f.nnz_exact;
+        st.rows_deferred = (long long)f.rows_deferred;
+        st.full_rounds = f.full_rounds;
         st.bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc +
                                36.0 * (double)(var_base_[u + 1] - var_base_[u]) * (double)f.rounds;
         st.device_ms = ms;
@@ -328,6 +373,8 @@ GDP_RETCODE Batch::propagate(double *const *lbs, double *const *ubs, gdp_stats *
         tot.rows_processed += st.rows_processed;
         tot.nnz_processed += st.nnz_processed;
         tot.nnz_exact += st.nnz_exact;
+        tot.rows_deferred += st.rows_deferred;
+        tot.full_rounds = std::max(tot.full_rounds, st.full_rounds);
         tot.bytes_algorithmic += st.bytes_algorithmic;
     }
     tot.kernel_launches = 5;

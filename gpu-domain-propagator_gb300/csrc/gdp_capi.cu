@@ -163,6 +163,13 @@ GDP_RETCODE gdp_context_set_model(gdp_context *ctx, const gdp_mlp *model, float 
     });
 }
 
+GDP_RETCODE gdp_batch_set_model(gdp_batch *b, const gdp_mlp *model, float threshold, int min_len) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!b) { gdp::set_error("null batch"); return GDP_ERROR; }
+        return b->impl.set_model(model ? &model->impl : nullptr, threshold, min_len);
+    });
+}
+
 GDP_RETCODE gdp_context_trace(gdp_context *ctx, double *lbs, double *ubs, int capacity, float *features,
                               float *labels, int *n_samples, gdp_stats *stats) {
     return guarded([&]() -> GDP_RETCODE {

@@ -68,6 +68,7 @@ struct RoundFlags {
     unsigned tight;      // tightenings found in this round (decides the next round's mode)
     int exact;           // multi-tile rows of this round that need the exact pass
     int full_rounds;     // learned marking: rounds that swept every row
+    int kind;            // learned marking, batched engine: kind of the round ([1 + parity])
     unsigned long long changed_vars;  // committed variable changes, all rounds
     unsigned long long rows_proc;     // rows processed (screened), all rounds
     unsigned long long nnz_proc;      // their non-zeros

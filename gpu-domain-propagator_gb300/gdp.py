@@ -140,6 +140,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     lib.gdp_mlp_train.argtypes = [C.c_void_p, C.c_int, _P_F, _P_F, _P_F, C.c_int, C.c_int, C.c_float,
                                   C.c_ulonglong, _P_F]
     lib.gdp_context_set_model.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_int]
+    lib.gdp_batch_set_model.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_int]
     lib.gdp_autotune.argtypes = _LEGACY_ARGS[:8] + [_P_DBL, _P_DBL, _P_INT, C.POINTER(Options), C.c_int,
                                                     C.POINTER(Options), C.POINTER(C.c_double),
                                                     C.POINTER(TuneTrial), C.c_int, C.POINTER(C.c_int)]
@@ -152,7 +153,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
                                       C.POINTER(Stats)]
     for name in ("gdp_mlp_create", "gdp_mlp_destroy", "gdp_mlp_get_params", "gdp_mlp_set_params",
                  "gdp_mlp_forward", "gdp_mlp_gradient", "gdp_mlp_train", "gdp_context_set_model",
-                 "gdp_context_trace"):
+                 "gdp_context_trace", "gdp_batch_set_model"):
         getattr(lib, name).restype = C.c_int
     for name in ("gdp_default_options", "gdp_context_create", "gdp_context_destroy", "gdp_propagate",
                  "gdp_propagate_device", "gdp_context_set_options", "gdp_context_layout",
@@ -417,6 +418,14 @@ class Batch:
     @property
     def uses_graph(self) -> bool:
         return bool(self._lib.gdp_batch_uses_graph(self._h))
+
+    def set_model(self, model, threshold: float = 0.0, min_len: int = 8) -> None:
+        """Learned marking for every member of an instance batch (`model` an
+        Mlp, None turns it off): each member takes the rounds of its own
+        learned propagation (Context.set_model) inside the one launch."""
+        self._model = model
+        _check(self._lib.gdp_batch_set_model(self._h, model._h if model is not None else None, float(threshold),
+                                             int(min_len)), "gdp_batch_set_model")
 
     def propagate(self, lbs, ubs):
         """lbs, ubs: one array per member. Returns (lbs, ubs, member stats, total stats)."""

@@ -186,6 +186,14 @@ GDP_RETCODE gdp_mlp_train(gdp_mlp *m, int n, const float *x, const float *y, con
  * run as one persistent launch. */
 GDP_RETCODE gdp_context_set_model(gdp_context *ctx, const gdp_mlp *model, float threshold, int min_len);
 
+/* Learned row marking for every member of an instance batch (model NULL: off):
+ * each member runs the rounds gdp_context_set_model describes -- its own
+ * sequence of learned, flush and full rounds, ended by a full round that
+ * changes nothing -- inside the batch's one persistent launch, with the
+ * bounds, round count and verdict of its single-problem learned propagation.
+ * Node batches return GDP_ERROR. The model must outlive its use by b. */
+GDP_RETCODE gdp_batch_set_model(gdp_batch *b, const gdp_mlp *model, float threshold, int min_len);
+
 /* Trace propagation of ctx's problem from lbs/ubs (host, in/out) with exact
  * marking (every marked row processed): for each marked row of a marked round
  * the 16 features before processing go to features[16 * i ..] and the label

@@ -107,3 +107,44 @@ def test_train_on_traces_and_gain():
     # against the plain full sweep every round (the reference's schedule)
     assert lst["nnz_processed"] < 0.5 * full["nnz_processed"]
     print("full sweep", {k: full[k] for k in ("rounds", "rows_processed", "nnz_processed", "device_ms")})
+
+
+@pytest.mark.parametrize("threshold", [-1e30, 0.0, 1e30])
+def test_learned_batch_equals_single_learned(threshold):
+    """Learned marking inside an instance batch: every member takes exactly the
+    rounds of its own single-problem learned propagation -- bounds bit for bit,
+    round count, verdict, deferred rows and full rounds -- with an infeasible
+    member and members of different sizes in the one launch."""
+    mips = [gdpgen.chains(12_000 + 9_000 * s, chain_max=80, seed=60 + s, frac_int_vars=1.0) for s in range(3)]
+    mips.append(gdpgen.chains(15_000, chain_max=60, seed=64, infeasible=True, frac_int_vars=1.0))
+    mips.append(_cover(3))
+    model = gdp.Mlp(seed=5)
+    b = gdp.Batch.instances(mips, max_rounds=1000)
+    b.set_model(model, threshold, 8)
+    for _ in range(2):  # the second call replays the captured graph
+        lbs, ubs, sts, tot = b.propagate([m.lb for m in mips], [m.ub for m in mips])
+        for k, m in enumerate(mips):
+            lb, ub, st = _ctx(m, model, threshold, max_rounds=1000, min_len=8).propagate()
+            what = f"member {k}, threshold {threshold}"
+            assert sts[k]["rounds"] == st["rounds"], what
+            assert sts[k]["infeasible"] == st["infeasible"], what
+            assert sts[k]["converged"] == st["converged"], what
+            assert sts[k]["rows_deferred"] == st["rows_deferred"], what
+            assert sts[k]["full_rounds"] == st["full_rounds"], what
+            assert_bitexact(lbs[k], ubs[k], lb, ub, what=what)
+        assert tot["infeasible"] >= 1
+    if threshold > 1e29:
+        assert tot["rows_deferred"] > 0
+
+
+def test_learned_batch_model_off_equals_plain_batch():
+    mips = [gdpgen.chains(10_000, chain_max=50, seed=70 + s, frac_int_vars=1.0) for s in range(2)]
+    plain = gdp.Batch.instances(mips, max_rounds=1000)
+    r0 = plain.propagate([m.lb for m in mips], [m.ub for m in mips])
+    b = gdp.Batch.instances(mips, max_rounds=1000)
+    b.set_model(gdp.Mlp(seed=1), 0.0, 8)
+    b.set_model(None)
+    r1 = b.propagate([m.lb for m in mips], [m.ub for m in mips])
+    for k in range(len(mips)):
+        assert_bitexact(r0[0][k], r0[1][k], r1[0][k], r1[1][k])
+        assert r0[2][k]["rounds"] == r1[2][k]["rounds"]
