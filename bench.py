@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--train-seeds", type=int, default=200, help="cover: instances traced for training")
     ap.add_argument("--eval-seeds", type=int, default=50, help="cover: held-out instances evaluated")
     ap.add_argument("--train-scale", type=float, default=0.1, help="cover: size of the traced instances")
+    ap.add_argument("--learned", action="store_true",
+                    help="instances / chains: learned row marking in the batch (MLP trained on the GPU on "
+                         "traces of smaller instances of the same generator), timed beside the exact-marking batch")
     return ap.parse_args()
 
 
@@ -216,6 +219,10 @@ BATCH_WORKLOADS = {
     "instances": "64 power-law MIPs, m log-uniform in [1,000, 500,000], n=0.75m",
     "chains": "128 chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
               "[100,000, 1,000,000], 60% integer vars, 15% infinite bounds, 10% made infeasible",
+    "chains_learned": "128 chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
+                      "[100,000, 1,000,000], 60% integer vars, 15% infinite bounds, 10% made infeasible; "
+                      "learned marking (MLP 16-64-64-1, BF16, trained on the GPU on traces of 16 instances "
+                      "of one tenth the size) in the one persistent batch launch",
 }
 
 
@@ -267,7 +274,8 @@ def run_batched(args, ws, rank, local):
     gen_s = time.perf_counter() - t0
     # chains of up to 5,000 links take up to that many Jacobi rounds to reach
     # their fixpoint: the chain workload's default cap lets every member certify
-    max_rounds = args.max_rounds or (10_000 if args.workload == "chains" else 0)
+    # learned rounds defer rows and so take more rounds: room for them too
+    max_rounds = args.max_rounds or (10_000 if args.workload == "chains" else 1_000 if args.learned else 0)
     t0 = time.perf_counter()
     if args.workload == "nodes":
         ctx = gdp.Context(mip, sync_type=gdp.MEGAKERNEL, max_rounds=max_rounds)
@@ -283,6 +291,27 @@ def run_batched(args, ws, rank, local):
         sizes = {"members": len(mips), "m_total": int(sum(m.m for m in mips)),
                  "nnz_total": int(sum(m.nnz for m in mips))}
     build_s = time.perf_counter() - t0
+    learned_info = None
+    exact_batch_ms = None
+    if args.learned and args.workload != "nodes":
+        import marking
+        import gdpgen
+        # the exact-marking batch first (same members, same launch), then the model
+        for _ in range(args.warmup):
+            batch.propagate(*members)
+        exact_batch_ms = statistics.median(batch.propagate(*members)[3]["device_ms"] for _ in range(args.steps))
+        t1 = time.perf_counter()
+        rng = np.random.default_rng(77)
+        k_train = 16
+        tm = np.exp(rng.uniform(np.log(100_000 * args.scale), np.log(1_000_000 * args.scale), k_train)) * 0.1
+        train = (gdpgen.chains(int(m), chain_max=500, seed=9000 + i) for i, m in enumerate(tm))
+        x, y = marking.collect_traces(train, capacity=200_000, max_rounds=max_rounds)
+        model, tau, info = marking.train_marking_model(x, y, epochs=4, batch=8192, seed=1, recall=0.98, min_len=8)
+        batch.set_model(model, tau, 8)
+        learned_info = {"train_instances": k_train, "train_samples": info["samples"],
+                        "positive_rate": info["positive_rate"], "train_loss": info["loss"], "threshold": tau,
+                        "train_recall": info["recall"], "selected_rate": info["selected_rate"],
+                        "train_s": time.perf_counter() - t1}
     for _ in range(args.warmup):
         batch.propagate(*members)
     clocks = Clocks(local)
@@ -299,7 +328,7 @@ def run_batched(args, ws, rank, local):
     # plain: every member alone, device-resident bounds, CUDA-event time of its round loop
     def plain_total(marking):
         ctxs = {}
-        total, rounds, agree = 0.0, [], True
+        total, rounds, agree, n_same = 0.0, [], True, 0
         for k, pm in enumerate(plain_mips):
             key = id(pm)
             if key not in ctxs:
@@ -311,30 +340,51 @@ def run_batched(args, ws, rank, local):
             torch.cuda.synchronize()
             total += st["device_ms"]
             rounds.append(st["rounds"])
-            agree &= (st["rounds"] == sts[k]["rounds"] and bool(st["infeasible"]) == bool(sts[k]["infeasible"])
-                      and np.array_equal(d_lb.cpu().numpy().view(np.int64), blb[k].view(np.int64))
-                      and np.array_equal(d_ub.cpu().numpy().view(np.int64), bub[k].view(np.int64)))
+            plb, pub = d_lb.cpu().numpy(), d_ub.cpu().numpy()
+            if learned_info is None:
+                agree &= (st["rounds"] == sts[k]["rounds"] and bool(st["infeasible"]) == bool(sts[k]["infeasible"])
+                          and np.array_equal(plb.view(np.int64), blb[k].view(np.int64))
+                          and np.array_equal(pub.view(np.int64), bub[k].view(np.int64)))
+            else:
+                # learned rounds reach the same certified fixpoint in another
+                # order: the same verdict; integer bounds equal, continuous ones
+                # within 1e-8 relative / 1e-9 absolute (feasible members)
+                same = bool(st["infeasible"]) == bool(sts[k]["infeasible"])
+                if same and not st["infeasible"]:
+                    same = (np.allclose(plb, blb[k], rtol=1e-8, atol=1e-9, equal_nan=True)
+                            and np.allclose(pub, bub[k], rtol=1e-8, atol=1e-9, equal_nan=True))
+                agree &= same
+                n_same += int(same)
         for c in ctxs.values():
             c.close()
-        return total, rounds, agree
+        return total, rounds, agree, n_same
 
-    plain_full_ms, rounds_full, agree_full = plain_total(0)
-    plain_adapt_ms, _, agree_adapt = plain_total(1)
+    plain_full_ms, rounds_full, agree_full, same_full = plain_total(0)
+    plain_adapt_ms, _, agree_adapt, same_adapt = plain_total(1)
     line = {"metric": "ms-to-fixpoint", "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOADS[args.workload], **sizes, "scale": args.scale,
+            "config": {"workload": BATCH_WORKLOADS[args.workload + ("_learned" if learned_info and
+                                                                   args.workload == "chains" else "")],
+                       **sizes, "scale": args.scale,
                        "max_rounds": max_rounds or 100,
                        "batch_rounds": tot["rounds"], "infeasible_members": tot["infeasible"],
                        "converged_members": int(sum(bool(s["converged"]) for s in sts)),
                        "rows_processed": tot["rows_processed"], "nnz_processed": tot["nnz_processed"],
                        "nnz_exact": tot["nnz_exact"], "graph": batch.uses_graph, "parallelism": "single",
-                       "autotune": getattr(batch, "tuned", None)},
+                       "autotune": getattr(batch, "tuned", None),
+                       "learned": learned_info, "rows_deferred": tot["rows_deferred"]},
             "plain": {"full_sweep_ms": plain_full_ms, "adaptive_marking_ms": plain_adapt_ms,
                       "rounds_max": max(rounds_full), "rounds_sum": int(sum(rounds_full)),
-                      "bitexact_full_sweep": bool(agree_full), "bitexact_adaptive": bool(agree_adapt),
+                      **({"bitexact_full_sweep": bool(agree_full), "bitexact_adaptive": bool(agree_adapt)}
+                         if learned_info is None else
+                         {"same_fixpoint_members_full_sweep": f"{same_full}/{len(plain_mips)}",
+                          "same_fixpoint_members_adaptive": f"{same_adapt}/{len(plain_mips)}"}),
                       "speedup_vs_full_sweep": plain_full_ms / value,
-                      "speedup_vs_adaptive": plain_adapt_ms / value},
+                      "speedup_vs_adaptive": plain_adapt_ms / value,
+                      **({} if exact_batch_ms is None else
+                         {"exact_marking_batch_ms": exact_batch_ms,
+                          "speedup_vs_exact_marking_batch": exact_batch_ms / value})},
             "e2e": {"value": statistics.median(e2e_ms), "unit": "ms",
                     "h2d_bytes_per_step": int(16 * sum(len(x) for x in members[0])),
                     "d2h_bytes_per_step": int(16 * sum(len(x) for x in members[0]))},
