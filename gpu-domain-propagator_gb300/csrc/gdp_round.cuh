@@ -860,17 +860,20 @@ __device__ __forceinline__ void flush_changed(const DevProblem &P, unsigned long
 
 // Commit changed variables nxt -> cur, apply the infeasibility rule, mark the
 // rows of changed variables for the next round, clear the bitmap.
+// One warp per word of the bitmap: lane l commits variable 32 w + l, then the
+// warp pushes the marks of each changed variable's rows together, 32 per step
+// (a thread walking its word's variables and their rows alone leaves the
+// commit of a round with many changes to a few long serial chains). tid /
+// nthreads: a grid of whole warps.
 __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, bool push_marks, int tid,
                                                int nthreads) {
+    const int lane = tid & 31;
     unsigned long long changed = 0;
-    for (int w = tid; w < P.n_chg_words; w += nthreads) {
-        unsigned bits = P.chg[w];
-        if (!bits) continue;
-        P.chg[w] = 0u;
-        changed += __popc(bits);
-        while (bits) {
-            const int j = w * 32 + __ffs(bits) - 1;
-            bits &= bits - 1;
+    for (int w = tid >> 5; w < P.n_chg_words; w += nthreads >> 5) {
+        const unsigned bits = P.chg[w];
+        if (!bits) continue;  // warp-uniform
+        if ((bits >> lane) & 1u) {
+            const int j = w * 32 + lane;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
             P.bnd32[j] = bnd_screen(b);
@@ -878,9 +881,17 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);
             }
-            if (push_marks)
-                for (int p = __ldg(P.var_ptr + j); p < __ldg(P.var_ptr + j + 1); p++)
-                    P.mark[__ldg(P.var_pos + p)] = round + 1;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            P.chg[w] = 0u;
+            changed += __popc(bits);
+        }
+        if (!push_marks) continue;
+        for (unsigned rem = bits; rem; rem &= rem - 1) {
+            const int j = w * 32 + __ffs(rem) - 1;
+            for (int p = __ldg(P.var_ptr + j) + lane; p < __ldg(P.var_ptr + j + 1); p += 32)
+                P.mark[__ldg(P.var_pos + p)] = round + 1;
         }
     }
     flush_changed(P, changed);
