@@ -18,9 +18,9 @@
 // followed by a full sweep: the marks are always pushed, so that rows the
 // model deferred are not swept along.
 // Split rows (longer than split_tile) are processed whenever marked. The plain
-// full sweep is the judge: the propagation ends only when a FULL round changes
-// nothing, so the result is a certified fixpoint of the same propagation
-// operator whatever the model decides.
+// full sweep decides the end: the propagation ends only when a FULL round
+// changes nothing, so the result is a certified fixpoint of the same
+// propagation operator whatever the model decides.
 //
 // Trace mode processes every marked row (exact marking) and logs, for each
 // marked SELL row of a marked round, its features before processing and the

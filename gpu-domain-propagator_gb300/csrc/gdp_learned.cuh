@@ -10,6 +10,7 @@ namespace gdp {
 namespace {
 
 constexpr int kRowInfoStreakShift = 8;
+constexpr int kMaxDeferRounds = 4;  // a marked row waits at most this many rounds for processing
 
 // The 16 features of row position p before it is processed in `round`.
 __device__ __forceinline__ void row_features(const DevProblem &P, int p, int round, int len, double lhs,
@@ -115,8 +116,12 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         }
         __syncwarp();
         // rows shorter than the model's minimum length are always processed:
-        // deferring them saves little and may stall a propagation front
-        const bool keep = act && (len < P.learn_min_len || L.z[rl] >= P.tau);
+        // deferring them saves little and may stall a propagation front; a
+        // row whose first unprocessed change is kMaxDeferRounds rounds old is
+        // processed too, so that no row is deferred (and scored) round after
+        // round while a long propagation never lets a flush happen
+        const bool keep = act && (len < P.learn_min_len || L.z[rl] >= P.tau ||
+                                  round - P.dirty[r] >= kMaxDeferRounds);  // the same for every lane of the row
         const unsigned deferred = __ballot_sync(kFull, leader0 && !keep);
         if (lane == 0 && deferred) atomicAdd(&P.flags[0].rows_deferred, (unsigned long long)__popc(deferred));
         any_deferred = deferred != 0;
