@@ -44,8 +44,8 @@ struct TilePart {
 struct XRow {
     long long base;
     int pos, len;
-    float u_hi;  // rows summed by several lanes: the screen's bound of max |a| (ub - lb)
-    int pad;
+    float u_hi;      // rows summed by several lanes: the screen's bound of max |a| (ub - lb)
+    float slack_lo;  // the screen's lower bound of min(rhs - minact, maxact - lhs)
 };
 
 // FP32 screen partial of a split-row tile (see Scr in gdp_device.cuh).

@@ -338,7 +338,8 @@ __device__ __forceinline__ ElemView sell_view(const DevProblem &P) {
 //   pass 2: candidates through the warp division queue.
 __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemView ev, int lg, int lane,
                                                 bool exact, int len,
-                                                int cnt, double lhs, double rhs, float u_hi, int *change,
+                                                int cnt, double lhs, double rhs, float u_hi, float slack_lo,
+                                                int *change,
                                                 unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
                                                 int *row_go = nullptr) {
     const int g = 1 << lg;
@@ -353,11 +354,16 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
     acc_init(s);
     double mn = 0.0;
     int dec = 0;
+    unsigned cmask = lg == 0 ? 0u : (cnt1 >= 32 ? ~0u : (1u << cnt1) - 1u);
     if (lg == 0) {
         // one lane per row, elements in order: the reference's left-to-right
         // sums and its sequential EPS-max of |a|(ub - lb) in the same loop, so
         // the row test is the reference's own (canConsBeTightened)
+        // cmask: the elements whose |a|(ub - lb) exceeds the screen's lower
+        // bound of both slacks -- the only ones that can yield a candidate
+        // (an integer compare of the keys; inf / NaN always pass)
         double m = 0.0;
+        const long long kcut = order_key(dbits(slack_lo == slack_lo ? (double)slack_lo : -1e308));
 #pragma unroll 4
         for (int i = 0; i < cnt1; i++) {
             const int j = __ldg(col + st * i);
@@ -366,6 +372,9 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
             acc_add_terms(s, a, b.x, b.y);
             const double d = dmul(fabs(a), dsub(b.y, b.x));
             if (eps_gt_fast(d, m)) m = d;
+            const long long db = dbits(d);
+            if (order_key(db) > kcut || (db & 0x7FF0000000000000LL) == 0x7FF0000000000000LL)
+                cmask |= 1u << (i & 31);
         }
         if (leader) {
             mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
@@ -412,33 +421,63 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
         int maxcnt = go ? cnt : 0;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) maxcnt = max(maxcnt, __shfl_xor_sync(kFull, maxcnt, off));
-        // software pipeline over the screen copies: element i + 2's column
-        // and coefficient and element i + 1's bounds are in flight while
-        // element i is tested; the FP64 values are read only for tests the
-        // FP32 box leaves open
+        // software pipeline over the screen copies: the element after next's
+        // column and coefficient and the next element's bounds are in flight
+        // while an element is tested; the FP64 values are read only for tests
+        // the FP32 box leaves open. A lane visits the elements of cmask (all
+        // of them for rows summed by several lanes).
         const float *a32 = ev.a32 + base;
-        const int ce = go ? cnt : 0;
-        int j1 = 0, j2 = 0;
-        float a1 = 0.0f, a2 = 0.0f;
-        float2 b1 = make_float2(0.0f, 0.0f);
-        if (ce > 0) { j1 = __ldg(col); a1 = __ldg(a32); }
-        if (ce > 1) { j2 = __ldg(col + st); a2 = __ldg(a32 + st); }
-        if (ce > 0) b1 = load_bnd32(P, j1);
-        for (int i = 0; i < maxcnt; i++) {
-            const int j = j1;
-            const float a = a1;
-            const float2 b = b1;
-            j1 = j2;
-            a1 = a2;
-            if (i + 2 < ce) { j2 = __ldg(col + st * (i + 2)); a2 = __ldg(a32 + st * (i + 2)); }
-            if (i + 1 < ce) b1 = load_bnd32(P, j1);
-            int sides = i < ce ? candidate_sides32(ws.rc[rl], a, b) : 0;
-            if (sides & 4) {
-                const double2 bd = load_bnd(P, j);
-                sides = candidate_sides(ws.rc[rl], __ldg(val + st * i), bd.x, bd.y);
+        if (__all_sync(kFull, cnt1 <= 32)) {
+            unsigned rem = go ? cmask : 0u;
+            int nvis = __popc(rem);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) nvis = max(nvis, __shfl_xor_sync(kFull, nvis, off));
+            int i1 = -1, i2 = -1, j1 = 0, j2 = 0;
+            float a1 = 0.0f, a2 = 0.0f;
+            float2 b1 = make_float2(0.0f, 0.0f);
+            if (rem) { i1 = __ffs(rem) - 1; rem &= rem - 1; j1 = __ldg(col + st * i1); a1 = __ldg(a32 + st * i1); }
+            if (rem) { i2 = __ffs(rem) - 1; rem &= rem - 1; j2 = __ldg(col + st * i2); a2 = __ldg(a32 + st * i2); }
+            if (i1 >= 0) b1 = load_bnd32(P, j1);
+            for (int t = 0; t < nvis; t++) {
+                const int i = i1, j = j1;
+                const float a = a1;
+                const float2 b = b1;
+                i1 = i2; j1 = j2; a1 = a2;
+                i2 = -1;
+                if (rem) { i2 = __ffs(rem) - 1; rem &= rem - 1; j2 = __ldg(col + st * i2); a2 = __ldg(a32 + st * i2); }
+                if (i1 >= 0) b1 = load_bnd32(P, j1);
+                int sides = i >= 0 ? candidate_sides32(ws.rc[rl], a, b) : 0;
+                if (sides & 4) {
+                    const double2 bd = load_bnd(P, j);
+                    sides = candidate_sides(ws.rc[rl], __ldg(val + st * i), bd.x, bd.y);
+                }
+                queue_push(Q, lane, sides, j, ((unsigned)max(i, 0) << 6) | ((unsigned)lane << 1));
+                queue_drain(Q, lane, false, run);
             }
-            queue_push(Q, lane, sides, j, ((unsigned)i << 6) | ((unsigned)lane << 1));
-            queue_drain(Q, lane, false, run);
+        } else {  // a lane holds more than 32 elements (thread_row_max or split_tile raised): every element
+            const int ce = go ? cnt : 0;
+            int j1 = 0, j2 = 0;
+            float a1 = 0.0f, a2 = 0.0f;
+            float2 b1 = make_float2(0.0f, 0.0f);
+            if (ce > 0) { j1 = __ldg(col); a1 = __ldg(a32); }
+            if (ce > 1) { j2 = __ldg(col + st); a2 = __ldg(a32 + st); }
+            if (ce > 0) b1 = load_bnd32(P, j1);
+            for (int i = 0; i < maxcnt; i++) {
+                const int j = j1;
+                const float a = a1;
+                const float2 b = b1;
+                j1 = j2;
+                a1 = a2;
+                if (i + 2 < ce) { j2 = __ldg(col + st * (i + 2)); a2 = __ldg(a32 + st * (i + 2)); }
+                if (i + 1 < ce) b1 = load_bnd32(P, j1);
+                int sides = i < ce ? candidate_sides32(ws.rc[rl], a, b) : 0;
+                if (sides & 4) {
+                    const double2 bd = load_bnd(P, j);
+                    sides = candidate_sides(ws.rc[rl], __ldg(val + st * i), bd.x, bd.y);
+                }
+                queue_push(Q, lane, sides, j, ((unsigned)i << 6) | ((unsigned)lane << 1));
+                queue_drain(Q, lane, false, run);
+            }
         }
         queue_drain(Q, lane, true, run);
         if (lane == 0) ws.st_div += (unsigned long long)Q.pushed;
@@ -471,7 +510,8 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     // FP32 screen
     bool exact = false;
     double lhs = 0.0, rhs = 0.0;
-    float u_hi = 0.0f;  // the row's bound of max |a| (ub - lb), leaders
+    float u_hi = 0.0f;     // the row's bound of max |a| (ub - lb), leaders
+    float slack_lo = 0.0f;  // the screen's lower bound of its slacks, leaders of exact rows
     {
         const int *col = P.sell_col + base;
         const float *val = P.sell_a32 + base;
@@ -489,6 +529,10 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
             rhs = __ldg(P.srow_rhs + r);
             exact = !scr_skips(c, len, lhs, rhs);
             u_hi = scr_u_bound(c);
+            if (exact) {
+                float hi;
+                scr_slack(c, len, lhs, rhs, slack_lo, hi);
+            }
         }
     }
     count_work(ws, lane, leader ? 1 : 0, leader ? len : 0, (leader && exact) ? len : 0);
@@ -498,14 +542,14 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         unsigned first = 0;
         if (lane == 0) first = atomicAdd(P.xctr + 16 * par + lg, (unsigned)__popc(bal));
         first = __shfl_sync(kFull, first, 0);
-        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len, u_hi, 0};
+        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len, u_hi, slack_lo};
         return;
     }
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
     if (!__any_sync(kFull, exact)) return;
     ws.base[lane] = base;
     __syncwarp();
-    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, u_hi, change, tight_ctr, ws);
+    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, u_hi, slack_lo, change, tight_ctr, ws);
 }
 
 // K slices of one-lane rows (g = 1) screened together in the deferred-exact
@@ -565,11 +609,17 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
         }
     }
     bool exact[K];
+    float slo[K];
     int rows = 0, nnz = 0, nnz_exact = 0, total = 0;
     unsigned bal[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
         exact[k] = act[k] && !scr_skips(c[k], len[k], lhs[k], rhs[k]);
+        slo[k] = 0.0f;
+        if (exact[k]) {
+            float hi;
+            scr_slack(c[k], len[k], lhs[k], rhs[k], slo[k], hi);
+        }
         rows += act[k] ? 1 : 0;
         nnz += len[k];
         nnz_exact += exact[k] ? len[k] : 0;
@@ -584,7 +634,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k], 0.0f, 0};
+        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k], 0.0f, slo[k]};
         first += __popc(bal[k]);
     }
 }
@@ -608,13 +658,14 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             int len = 0, cnt = 0;
             long long base = 0;
             double lhs = 0.0, rhs = 0.0;
-            float u_hi = 0.0f;
+            float u_hi = 0.0f, slack_lo = 0.0f;
             if (exact) {
                 const XRow x = P.xrow[P.cls_begin[lg] + k];
                 const int p = x.pos;
                 base = x.base + sub;
                 len = x.len;
                 u_hi = x.u_hi;
+                slack_lo = x.slack_lo;
                 cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
                 if (sub == 0) {
                     lhs = __ldg(P.srow_lhs + p);
@@ -624,7 +675,7 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             ws.base[lane] = base;
             __syncwarp();
             sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, u_hi,
-                            change, tight_ctr, ws);
+                            slack_lo, change, tight_ctr, ws);
             __syncwarp();
         }
     }
