@@ -2,6 +2,7 @@
 // interface.h symbols (include/interface.h of the reference, implemented in
 // its src/interface.cu:18-354) and the extended API of gdp_ext.h.
 #include <chrono>
+#include <cstring>
 #include <exception>
 #include <new>
 #include <string>
@@ -82,6 +83,13 @@ GDP_RETCODE gdp_default_options(gdp_options *o) {
 }
 
 const char *gdp_last_error(void) { return gdp::last_error(); }
+
+GDP_RETCODE gdp_release_cached_memory(void) {
+    return guarded([&]() -> GDP_RETCODE {
+        gdp::release_cached_memory();
+        return GDP_OKAY;
+    });
+}
 
 GDP_RETCODE gdp_context_create(int n_cons, int n_vars, int nnz, const int *col, const int *row_ptr,
                                const double *val, const double *lhs, const double *rhs,
@@ -206,6 +214,32 @@ GDP_RETCODE gdp_propagate(gdp_context *ctx, double *lbs, double *ubs, gdp_stats 
         const auto t0 = std::chrono::steady_clock::now();
         if (stats) *stats = gdp_stats{};
         const GDP_RETCODE rc = ctx->impl.propagate_host(lbs, ubs, stats);
+        if (stats)
+            stats->total_ms =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    });
+}
+
+GDP_RETCODE gdp_propagate_into(gdp_context *ctx, const double *lbs_in, const double *ubs_in, double *lbs_out,
+                               double *ubs_out, gdp_stats *stats) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!ctx || !lbs_in || !ubs_in || !lbs_out || !ubs_out) {
+            gdp::set_error("null argument");
+            return GDP_ERROR;
+        }
+        const auto t0 = std::chrono::steady_clock::now();
+        if (stats) *stats = gdp_stats{};
+        const long long n = ctx->impl.n;
+        // chunked copies on the host threads (one thread copies a few GB/s)
+        const long long chunk = 1 << 16;
+#pragma omp parallel for schedule(static)
+        for (long long c = 0; c < (n + chunk - 1) / chunk; c++) {
+            const long long b = c * chunk, len = std::min(chunk, n - b);
+            if (lbs_out != lbs_in) std::memcpy(lbs_out + b, lbs_in + b, sizeof(double) * (size_t)len);
+            if (ubs_out != ubs_in) std::memcpy(ubs_out + b, ubs_in + b, sizeof(double) * (size_t)len);
+        }
+        const GDP_RETCODE rc = ctx->impl.propagate_host(lbs_out, ubs_out, stats);
         if (stats)
             stats->total_ms =
                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -13,8 +13,12 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #ifdef _OPENMP
@@ -44,50 +48,146 @@ const char *last_error() { return g_last_error.c_str(); }
     } while (0)
 
 // ---------------------------------------------------------------------------
-Arena::~Arena() {
-    for (void *p : ptrs) cudaFree(p);
+namespace {
+// Device blocks of released arenas by (device, size). A request takes the
+// smallest cached block of its device that is at least as large and at most
+// 5/4 of the request. The cache keeps at most kCacheMax bytes; blocks beyond
+// that are freed. The object is never destroyed: at exit the CUDA runtime
+// may be gone before static destructors run, and the driver reclaims the
+// memory anyway.
+struct BlockCache {
+    std::mutex mu;
+    std::multimap<std::pair<int, size_t>, void *> blocks;
+    size_t bytes = 0;
+};
+constexpr size_t kCacheMax = size_t(32) << 30;
+BlockCache &block_cache() {
+    static BlockCache *c = new BlockCache;
+    return *c;
+}
+}  // namespace
+
+void release_cached_memory() {
+    BlockCache &c = block_cache();
+    std::lock_guard<std::mutex> g(c.mu);
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (const auto &kv : c.blocks) {
+        cudaSetDevice(kv.first.first);
+        cudaFree(kv.second);
+    }
+    cudaSetDevice(cur);
+    cudaGetLastError();
+    c.blocks.clear();
+    c.bytes = 0;
+}
+
+Arena::~Arena() { release(); }
+
+void Arena::release() {
+    if (blocks.empty()) return;
+    // a block may still be read by work on any stream of its device (the
+    // device-pointer entry points take the caller's stream): wait for the
+    // device, as cudaFree would
+    int cur = 0;
+    cudaGetDevice(&cur);
+    int synced = -1;
+    for (const Block &b : blocks)
+        if (b.dev != synced) {
+            cudaSetDevice(b.dev);
+            cudaDeviceSynchronize();
+            synced = b.dev;
+        }
+    cudaSetDevice(cur);
+    cudaGetLastError();
+    BlockCache &c = block_cache();
+    std::lock_guard<std::mutex> g(c.mu);
+    for (const Block &b : blocks) {
+        if (c.bytes + b.bytes <= kCacheMax) {
+            c.blocks.emplace(std::make_pair(b.dev, b.bytes), b.p);
+            c.bytes += b.bytes;
+        } else {
+            cudaFree(b.p);
+        }
+    }
+    blocks.clear();
 }
 
 void *Arena::alloc_bytes(size_t bytes) {
-    void *p = nullptr;
-    if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
+    bytes = (std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    ptrs.push_back(p);
+    {
+        BlockCache &c = block_cache();
+        std::lock_guard<std::mutex> g(c.mu);
+        auto it = c.blocks.lower_bound(std::make_pair(dev, bytes));
+        if (it != c.blocks.end() && it->first.first == dev && it->first.second - bytes <= bytes / 4) {
+            const Block blk{it->second, it->first.second, dev};
+            c.blocks.erase(it);
+            c.bytes -= blk.bytes;
+            blocks.push_back(blk);
+            return blk.p;
+        }
+    }
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {  // the cache may hold the memory: free it, retry once
+        cudaGetLastError();
+        release_cached_memory();
+        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    blocks.push_back(Block{p, bytes, dev});
     return p;
 }
 
 // ---------------------------------------------------------------------------
-GDP_RETCODE validate_csr(int m, int n, int nnz, const int *col, const int *row_ptr,
-                         const double *val, const int *vartype) {
+// The checks that make the raw arrays safe to copy: sizes, pointers and the
+// row pointer's end points.
+static GDP_RETCODE validate_shape(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
+                                  const int *vartype) {
     if (m < 0 || n < 0 || nnz < 0) { set_error("negative problem size"); return GDP_ERROR; }
     if (!col || !row_ptr || !val || !vartype) { set_error("null input array"); return GDP_ERROR; }
     if (row_ptr[0] != 0 || row_ptr[m] != nnz) {
         set_error("csr_row_ptrs must start at 0 and end at nnz");
         return GDP_ERROR;
     }
+    return GDP_OKAY;
+}
+
+GDP_RETCODE validate_csr(int m, int n, int nnz, const int *col, const int *row_ptr,
+                         const double *val, const int *vartype) {
+    if (validate_shape(m, n, nnz, col, row_ptr, val, vartype) != GDP_OKAY) return GDP_ERROR;
+    int bad_row = INT_MAX, bad_var = INT_MAX;
+#pragma omp parallel for reduction(min : bad_row) schedule(static)
     for (int i = 0; i < m; i++)
-        if (row_ptr[i + 1] < row_ptr[i]) { set_error("csr_row_ptrs is not monotone"); return GDP_ERROR; }
-    long long bad_col = -1, bad_val = -1;
-#pragma omp parallel for reduction(max : bad_col, bad_val) schedule(static)
-    for (int k = 0; k < nnz; k++) {
-        if ((unsigned)col[k] >= (unsigned)n) bad_col = std::max(bad_col, (long long)k);
-        if (!std::isfinite(val[k])) bad_val = std::max(bad_val, (long long)k);
-    }
-    if (bad_col >= 0) {
-        set_error("column index out of range at non-zero " + std::to_string(bad_col));
-        return GDP_ERROR;
-    }
-    if (bad_val >= 0) {
-        set_error("non-finite coefficient at non-zero " + std::to_string(bad_val));
-        return GDP_ERROR;
-    }
+        if (row_ptr[i + 1] < row_ptr[i]) bad_row = std::min(bad_row, i);
+    if (bad_row != INT_MAX) { set_error("csr_row_ptrs is not monotone"); return GDP_ERROR; }
+#pragma omp parallel for reduction(min : bad_var) schedule(static)
     for (int j = 0; j < n; j++)
-        if (vartype[j] != 0 && vartype[j] != 1 && vartype[j] != 3) {
-            set_error("vartype must be 0, 1 or 3 (variable " + std::to_string(j) + ")");
-            return GDP_ERROR;
-        }
+        if (vartype[j] != 0 && vartype[j] != 1 && vartype[j] != 3) bad_var = std::min(bad_var, j);
+    if (bad_var != INT_MAX) {
+        set_error("vartype must be 0, 1 or 3 (variable " + std::to_string(bad_var) + ")");
+        return GDP_ERROR;
+    }
+    return GDP_OKAY;
+}
+
+// The element checks (column range, finite coefficients) run on the device
+// over the uploaded raw CSR; this turns their result into the error.
+static GDP_RETCODE element_error(const int bad[2]) {
+    if (bad[0] != INT_MAX) {
+        set_error("column index out of range at non-zero " + std::to_string(bad[0]));
+        return GDP_ERROR;
+    }
+    if (bad[1] != INT_MAX) {
+        set_error("non-finite coefficient at non-zero " + std::to_string(bad[1]));
+        return GDP_ERROR;
+    }
     return GDP_OKAY;
 }
 
@@ -109,7 +209,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         return GDP_ERROR;
     }
     if (!lhs || !rhs) { set_error("null lhs/rhs"); return GDP_ERROR; }
-    if (validate_csr(m, n, nnz, col, row_ptr, val, vartype) != GDP_OKAY) return GDP_ERROR;
+    if (validate_csr(m, n, nnz, col, row_ptr, val, vartype) != GDP_OKAY) return GDP_ERROR;  // host part
 
     GDP_CUDA(cudaSetDevice(opts.device));
     cudaGetLastError();  // every call below is checked; start from a clean error state
@@ -120,7 +220,78 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     int sms = 0;
     GDP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opts.device));
     n_sms = sms;
+    int pageable = 0;
+    GDP_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, opts.device));
+    host_direct = pageable == 1;
 
+    // The raw CSR goes up from a helper thread, on a stream of its own, while
+    // this thread bins the rows: a copy from pageable memory returns only
+    // once its source has been staged, so issuing it here would serialise
+    // the two. This thread makes no CUDA call until the row layout is
+    // decided (the driver would hold it while the copy runs). The helper
+    // leaves once the copies are queued; the layout build that reads them
+    // waits for them on the device (an event), after the join. The element
+    // checks (column range, finite coefficients) run on the device over the
+    // copies.
+    Arena raw;  // raw CSR and row sides, released when the build is done
+    int *dcol = nullptr, *drp = nullptr;
+    double *dval = nullptr, *dlhs = nullptr, *drhs = nullptr;
+    std::string up_err;
+    struct UploadStream {  // the helper's stream and its completion event
+        cudaStream_t s = nullptr;
+        cudaEvent_t done = nullptr;
+        ~UploadStream() {
+            if (s) cudaStreamSynchronize(s);  // before the raw buffers can be freed
+            if (done) cudaEventDestroy(done);
+            if (s) cudaStreamDestroy(s);
+        }
+    } ups;
+    struct Joined {
+        std::thread t;
+        ~Joined() {
+            if (t.joinable()) t.join();
+        }
+    } uploader;  // declared after everything the thread touches: joined first
+    uploader.t = std::thread([&, dev = opts.device] {
+        auto fail = [&](const char *what, cudaError_t e) {
+            up_err = std::string(what) + ": " + cudaGetErrorString(e);
+            cudaGetLastError();
+        };
+        cudaError_t e = cudaSetDevice(dev);
+        if (e != cudaSuccess) return fail("cudaSetDevice", e);
+        const size_t nz = (size_t)std::max(nnz, 1);
+        dcol = (int *)raw.alloc_bytes(sizeof(int) * nz);
+        dval = (double *)raw.alloc_bytes(sizeof(double) * nz);
+        drp = (int *)raw.alloc_bytes(sizeof(int) * ((size_t)m + 1));
+        dlhs = (double *)raw.alloc_bytes(sizeof(double) * (size_t)std::max(m, 1));
+        drhs = (double *)raw.alloc_bytes(sizeof(double) * (size_t)std::max(m, 1));
+        if (!dcol || !dval || !drp || !dlhs || !drhs) {
+            up_err = "device allocation failed (raw CSR)";
+            return;
+        }
+        e = cudaStreamCreateWithFlags(&ups.s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return fail("cudaStreamCreate", e);
+        e = cudaEventCreateWithFlags(&ups.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) return fail("cudaEventCreate", e);
+        cudaStream_t us = ups.s;
+        if (nnz) e = cudaMemcpyAsync(dcol, col, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess && nnz)
+            e = cudaMemcpyAsync(dval, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(drp, row_ptr, sizeof(int) * ((size_t)m + 1), cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess && m) e = cudaMemcpyAsync(dlhs, lhs, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess && m) e = cudaMemcpyAsync(drhs, rhs, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess) e = cudaEventRecord(ups.done, us);
+        if (e != cudaSuccess) fail("raw CSR upload", e);
+    });
+
+    // host threads while the helper runs: one core stays free for it, so
+    // that no parallel region waits for a descheduled thread
+#ifdef _OPENMP
+    const int host_threads = std::max(1, omp_get_max_threads() - 1);
+#else
+    const int host_threads = 1;
+#endif
     // ---- row binning (SELL-g) ----
     // g = 1 for rows up to thread_row_max; g = smallest power of two >= len/32
     // (2..32) up to split_tile; longer rows are split into warp tiles.
@@ -131,9 +302,9 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         while (g < 32 && g * 32 < L) g <<= 1;
         return g;
     };
-    std::vector<int> len(m);
+    std::unique_ptr<int[]> len(new int[std::max(m, 1)]);
     int lmax = 0;  // longest SELL row
-#pragma omp parallel for reduction(max : lmax) schedule(static)
+#pragma omp parallel for reduction(max : lmax) schedule(static) num_threads(host_threads)
     for (int i = 0; i < m; i++) {
         len[i] = row_ptr[i + 1] - row_ptr[i];
         if (len[i] <= Ls) lmax = std::max(lmax, len[i]);
@@ -144,9 +315,14 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // contiguous row chunks (per-chunk histograms keep it stable). Split rows
     // (longer than Ls) are collected in row order and sorted by length.
     std::vector<int> sell_rows, split_rows;
+    // per SELL row length L: first position, and first element of the
+    // row-contiguous copy (rows of one length are consecutive positions)
+    std::vector<int> len_start((size_t)lmax + 1, 0);
+    std::vector<long long> len_base((size_t)lmax + 1, 0);
+    long long x_elems = 0;  // elements of the row-contiguous copy
     {
 #ifdef _OPENMP
-        const int nt = lmax <= (1 << 16) ? std::max(1, std::min(omp_get_max_threads(), 64)) : 1;
+        const int nt = lmax <= (1 << 16) ? std::min(host_threads, 64) : 1;
 #else
         const int nt = 1;
 #endif
@@ -169,12 +345,16 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         }
         // offsets: longer rows first; within a length, chunks in row order
         int acc = 0;
-        for (int L = lmax; L >= 1; L--)
+        for (int L = lmax; L >= 1; L--) {
+            len_start[L] = acc;
+            len_base[L] = x_elems;
             for (int t = 0; t < nt; t++) {
                 const int c = hist[(size_t)t * W + L];
                 hist[(size_t)t * W + L] = acc;
                 acc += c;
             }
+            x_elems += (long long)(acc - len_start[L]) * L;
+        }
         for (int t = 0; t < nt; t++) nsplit[t + 1] += nsplit[t];
         sell_rows.resize(acc);
         split_rows.resize(nsplit[nt]);
@@ -204,6 +384,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // its first (longest) row
     std::vector<long long> slice_ptr;
     std::vector<int> slice_row0, slice_lg;
+    int g1_begin = ns;  // first position of the one-lane rows
     {
         int cls_lo[6], cls_hi[6], cls_first[6];
         for (int c = 0; c < 6; c++) { cls_lo[c] = 0; cls_hi[c] = 0; }
@@ -221,6 +402,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             cls_hi[lg] = lo;
             p = lo;
         }
+        if (cls_hi[0] > cls_lo[0]) g1_begin = cls_lo[0];
         int nsl = 0;
         for (int lg = 5; lg >= 0; lg--) {
             cls_first[lg] = nsl;
@@ -234,7 +416,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         for (int lg = 5; lg >= 0; lg--) {
             const int per = 32 >> lg, g = 1 << lg, c0 = cls_lo[lg], c1 = cls_hi[lg];
             const int k_n = (c1 - c0 + per - 1) / per;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(host_threads)
             for (int k = 0; k < k_n; k++) {
                 const int s = cls_first[lg] + k, r0 = c0 + k * per;
                 slice_row0[s] = r0;
@@ -248,21 +430,8 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         n_slices = nsl;
     }
     sell_elems = slice_ptr[n_slices];
-    // per row position: length, sides, first element of the row-contiguous copy
-    std::vector<int> srow_len(std::max(ns, 1)), xptr(std::max(ns, 1), 0);
-    std::vector<double> srow_lhs(std::max(ns, 1)), srow_rhs(std::max(ns, 1));
-#pragma omp parallel for schedule(static)
-    for (int p = 0; p < ns; p++) {
-        const int i = order[p];
-        srow_len[p] = len[i];
-        srow_lhs[p] = lhs[i];
-        srow_rhs[p] = rhs[i];
-    }
-    long long x_elems = 0;
-    for (int p = 0; p < ns; p++) {
-        xptr[p] = (int)x_elems;
-        x_elems += srow_len[p];
-    }
+    // per row position (length, sides, first element of the row-contiguous
+    // copy, slice): built on the device from the row order
     // split rows: CSR-contiguous, warp tiles of split_tile non-zeros
     n_lrows = (int)split_rows.size();
     std::vector<long long> lrow_ptr(n_lrows + 1, 0);
@@ -333,22 +502,25 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.slice_ptr, const long long, slice_ptr);
     GDP_UP(P.slice_row0, const int, slice_row0);
     GDP_UP(P.slice_lg, const int, slice_lg);
-    GDP_UP(P.srow_len, const int, srow_len);
-    GDP_UP(P.xptr, const int, xptr);
-    {
-        std::vector<int> pos_slice(std::max(ns, 1), 0);
-#pragma omp parallel for schedule(static)
-        for (int s = 0; s < n_slices; s++)
-            for (int p = slice_row0[s]; p < slice_row0[s + 1]; p++) pos_slice[p] = s;
-        GDP_UP(P.pos_slice, const int, pos_slice);
+    int *d_srow_len = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
+    int *d_xptr = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
+    int *d_pos_slice = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
+    double *d_srow_lhs = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(ns, 1));
+    double *d_srow_rhs = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(ns, 1));
+    if (!d_srow_len || !d_xptr || !d_pos_slice || !d_srow_lhs || !d_srow_rhs) {
+        set_error("device allocation failed (row positions)");
+        return GDP_ERROR;
     }
-    GDP_UP(P.srow_lhs, const double, srow_lhs);
-    GDP_UP(P.srow_rhs, const double, srow_rhs);
+    P.srow_len = d_srow_len;
+    P.xptr = d_xptr;
+    P.pos_slice = d_pos_slice;
+    P.srow_lhs = d_srow_lhs;
+    P.srow_rhs = d_srow_rhs;
     P.n_lrows = n_lrows;
     P.n_tiles = n_tiles;
     {  // element arrays: the raw CSR goes up once and the device places every
-       // element (SELL slots, row-contiguous copy, split rows), then the FP32
-       // screen copies of the three coefficient arrays
+       // element (SELL slots, row-contiguous copy, split rows) together with
+       // its FP32 screen copy
         const size_t n_sell = (size_t)std::max<long long>(sell_elems, 1);
         const size_t n_x = (size_t)std::max<long long>(x_elems, 1);
         const size_t n_l = (size_t)std::max<long long>(lnnz, 1);
@@ -367,40 +539,56 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         }
         GDP_CUDA(cudaMemsetAsync(sc, 0, sizeof(int) * n_sell, stream));  // padding slots
         GDP_CUDA(cudaMemsetAsync(sv, 0, sizeof(double) * n_sell, stream));
-        Arena tmp;  // raw CSR and the row maps, freed when the build is done
-        const size_t nz = (size_t)std::max(nnz, 1);
-        int *dcol = (int *)tmp.alloc_bytes(sizeof(int) * nz);
-        double *dval = (double *)tmp.alloc_bytes(sizeof(double) * nz);
-        int *drp = (int *)tmp.alloc_bytes(sizeof(int) * ((size_t)m + 1));
+        GDP_CUDA(cudaMemsetAsync(sa, 0, sizeof(float) * n_sell, stream));
+        Arena tmp;  // the row maps, freed when the build is done
         int *dord = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
         int *dspl = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
         long long *dlrp = (long long *)tmp.alloc_bytes(sizeof(long long) * ((size_t)n_lrows + 1));
-        if (!dcol || !dval || !drp || !dord || !dspl || !dlrp) {
-            set_error("device allocation failed (raw CSR)");
+        int *dls = (int *)tmp.alloc_bytes(sizeof(int) * len_start.size());
+        long long *dlb = (long long *)tmp.alloc_bytes(sizeof(long long) * len_base.size());
+        int *dbad = (int *)tmp.alloc_bytes(sizeof(int) * 2);
+        if (!dord || !dspl || !dlrp || !dls || !dlb || !dbad) {
+            set_error("device allocation failed (row maps)");
             return GDP_ERROR;
         }
-        if (nnz) {
-            GDP_CUDA(cudaMemcpyAsync(dcol, col, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, stream));
-            GDP_CUDA(cudaMemcpyAsync(dval, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, stream));
+        uploader.t.join();
+        if (!up_err.empty()) {
+            set_error(up_err);
+            return GDP_ERROR;
         }
-        GDP_CUDA(cudaMemcpyAsync(drp, row_ptr, sizeof(int) * ((size_t)m + 1), cudaMemcpyHostToDevice, stream));
+        GDP_CUDA(cudaStreamWaitEvent(stream, ups.done, 0));
         if (ns) GDP_CUDA(cudaMemcpyAsync(dord, order.data(), sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, stream));
         if (n_lrows)
             GDP_CUDA(cudaMemcpyAsync(dspl, split_rows.data(), sizeof(int) * (size_t)n_lrows, cudaMemcpyHostToDevice,
                                      stream));
         GDP_CUDA(cudaMemcpyAsync(dlrp, lrow_ptr.data(), sizeof(long long) * ((size_t)n_lrows + 1),
                                  cudaMemcpyHostToDevice, stream));
+        GDP_CUDA(cudaMemcpyAsync(dls, len_start.data(), sizeof(int) * len_start.size(), cudaMemcpyHostToDevice,
+                                 stream));
+        GDP_CUDA(cudaMemcpyAsync(dlb, len_base.data(), sizeof(long long) * len_base.size(), cudaMemcpyHostToDevice,
+                                 stream));
+        const int no_bad[2] = {INT_MAX, INT_MAX};
+        GDP_CUDA(cudaMemcpyAsync(dbad, no_bad, sizeof(no_bad), cudaMemcpyHostToDevice, stream));
+        GDP_CUDA(check_csr_elements(dcol, dval, nnz, n, dbad, 8 * n_sms, stream));
         LayoutBuild L;
         L.col = dcol; L.row_ptr = drp; L.val = dval;
         L.n_srows = ns; L.order = dord; L.pos_slice = P.pos_slice; L.slice_row0 = P.slice_row0;
         L.slice_lg = P.slice_lg; L.xptr = P.xptr; L.slice_ptr = P.slice_ptr;
-        L.sell_col = sc; L.xcol = xc; L.sell_val = sv; L.xval = xv;
+        L.sell_col = sc; L.xcol = xc; L.sell_val = sv; L.xval = xv; L.sell_a32 = sa; L.xa32 = xa;
+        L.g1_begin = g1_begin; L.la32 = la;
         L.n_lrows = n_lrows; L.split_rows = dspl; L.lrow_ptr = dlrp; L.lcol = lc; L.lval = lv;
+        L.lhs = dlhs; L.rhs = drhs; L.len_start = dls; L.len_base = dlb; L.n_slices = n_slices;
+        L.srow_len_out = d_srow_len; L.xptr_out = d_xptr; L.pos_slice_out = d_pos_slice;
+        L.srow_lhs_out = d_srow_lhs; L.srow_rhs_out = d_srow_rhs;
+        // nothing up to the marking index uses a column as an index, so the
+        // build runs before the element checks' result is read
+        GDP_CUDA(build_layout_positions(L, 8 * n_sms, stream));
         GDP_CUDA(build_layout_elements(L, 8 * n_sms, stream));
-        GDP_CUDA(launch_coef_screen(sv, sa, (long long)n_sell, 8 * n_sms, stream));
-        GDP_CUDA(launch_coef_screen(xv, xa, (long long)n_x, 8 * n_sms, stream));
-        GDP_CUDA(launch_coef_screen(lv, la, (long long)n_l, 8 * n_sms, stream));
+        int bad[2];
+        GDP_CUDA(cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, stream));
         GDP_CUDA(cudaStreamSynchronize(stream));  // before the raw CSR is freed
+        raw.release();
+        if (element_error(bad) != GDP_OKAY) return GDP_ERROR;
         P.sell_col = sc; P.sell_val = sv; P.sell_a32 = sa;
         P.xcol = xc; P.xval = xv; P.xa32 = xa;
         P.lcol = lc; P.lval = lv; P.la32 = la;
@@ -732,6 +920,15 @@ GDP_RETCODE Context::trace(double *lbs, double *ubs, int capacity, float *x_out,
 }
 
 GDP_RETCODE Context::propagate_host(double *lbs, double *ubs, gdp_stats *st) {
+    if (host_direct) {
+        // coherent access to pageable memory (NVLink-C2C on Grace hosts): the
+        // first kernel reads the caller's bounds where they are, and the
+        // result is written back to them by a kernel once the run succeeded
+        if (run(lbs, ubs, d_lb, d_ub, stream, st) != GDP_OKAY) return GDP_ERROR;
+        GDP_CUDA(launch_copy_out(d_lb, d_ub, lbs, ubs, n, vec_blocks, stream));
+        GDP_CUDA(cudaStreamSynchronize(stream));
+        return GDP_OKAY;
+    }
     const size_t bytes = sizeof(double) * (size_t)n;
     GDP_CUDA(cudaMemcpyAsync(d_lb, lbs, bytes, cudaMemcpyHostToDevice, stream));
     GDP_CUDA(cudaMemcpyAsync(d_ub, ubs, bytes, cudaMemcpyHostToDevice, stream));

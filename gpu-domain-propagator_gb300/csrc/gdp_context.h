@@ -15,12 +15,24 @@ namespace gdp {
 void set_error(const std::string &msg);
 const char *last_error();
 
-// Owns device allocations; frees them on destruction.
+// Owns device allocations. Released blocks go to a process-wide cache of
+// device memory that later arenas draw from, so contexts of one problem size
+// can be created and destroyed without cudaMalloc / cudaFree (each costs up
+// to milliseconds for blocks of hundreds of MB).
 struct Arena {
-    std::vector<void *> ptrs;
+    struct Block {
+        void *p;
+        size_t bytes;
+        int dev;
+    };
+    std::vector<Block> blocks;
     ~Arena();
     void *alloc_bytes(size_t bytes);
+    void release();  // waits for the device, then returns every block to the cache
 };
+
+// Frees the cached device memory of released arenas (all devices).
+void release_cached_memory();
 
 GDP_RETCODE autotune(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
                      const double *lhs, const double *rhs, const double *lbs, const double *ubs,
@@ -57,6 +69,7 @@ public:
     long long sell_elems = 0;
     // the last propagation converged feasibly: P.bnd is a fixpoint of the problem
     bool certified = false;
+    bool host_direct = false;  // kernels read and write pageable host memory (coherent access)
     // GPU_LOOP graph (built on first use, reused while the context lives)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;

@@ -177,9 +177,10 @@ constexpr int kWarpsPerCta = 8;
 constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
 // Launch helpers (gdp_round.cu). All return the cudaError_t of the launch.
-int launch_coef_screen(const double *v, float *out, long long n, int blocks, cudaStream_t s);
 int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_interleave(const DevProblem &P, const double *lb, const double *ub, int blocks, cudaStream_t s);
+int launch_copy_out(const double *lb, const double *ub, double *lb_out, double *ub_out, int n, int blocks,
+                    cudaStream_t s);
 int launch_deinterleave(const DevProblem &P, double *lb, double *ub, int blocks, cudaStream_t s);
 int launch_mark_all(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_round_begin(const DevProblem &P, cudaStream_t s);
@@ -200,13 +201,33 @@ struct LayoutBuild {
     const long long *slice_ptr;
     int *sell_col, *xcol;
     double *sell_val, *xval;
+    float *sell_a32, *xa32;  // FP32 screen copies (coef_screen)
+    int g1_begin;            // first position of the one-lane rows (n_srows: none)
     int n_lrows;
     const int *split_rows;     // split-row slot -> row
     const long long *lrow_ptr;
     int *lcol;
     double *lval;
+    float *la32;
+    // row positions, built before the elements: SELL rows are sorted by
+    // length, longest first, so the rows of one length L are the consecutive
+    // positions from len_start[L] and their row-contiguous copies start at
+    // len_base[L] + (p - len_start[L]) * L
+    const double *lhs, *rhs;    // raw row sides (m)
+    const int *len_start;       // lmax + 1 entries
+    const long long *len_base;  // lmax + 1 entries
+    int n_slices;
+    int *srow_len_out, *xptr_out, *pos_slice_out;
+    double *srow_lhs_out, *srow_rhs_out;
 };
+// Per row position: length, sides, first element of the row-contiguous copy
+// and slice (the arrays that build_layout_elements reads as pos_slice, xptr).
+int build_layout_positions(const LayoutBuild &L, int blocks, cudaStream_t s);
 int build_layout_elements(const LayoutBuild &L, int blocks, cudaStream_t s);
+// The first out-of-range column index (bad[0]) and the first non-finite
+// coefficient (bad[1]) of the raw CSR, by atomicMin into bad, which the
+// caller sets to INT_MAX before.
+int check_csr_elements(const int *col, const double *val, int nnz, int n, int *bad, int blocks, cudaStream_t s);
 // gdp_layout.cu: variable -> row-position index for marking (scratch: n + 2 + (n+1)/1024 ints)
 int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s);
 

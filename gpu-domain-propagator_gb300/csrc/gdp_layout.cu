@@ -11,6 +11,9 @@
 // defined (it does not matter for marking).
 #include <cuda_runtime.h>
 
+#include <climits>
+
+#include "gdp_device.cuh"
 #include "gdp_internal.h"
 
 namespace gdp {
@@ -32,11 +35,14 @@ __device__ __forceinline__ void for_each_element(const DevProblem &P, F &&f) {
         const int len = rl < nrows ? P.srow_len[row0 + rl] : 0;
         const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
         const long long base = P.slice_ptr[s] + lane;
-        for (int i = 0; i < cnt; i++) f(P.sell_col[base + 32LL * i], row0 + rl);
+#pragma unroll 4
+        for (int i = 0; i < cnt; i++) f(__ldg(P.sell_col + base + 32LL * i), row0 + rl);
     }
     for (int t = warp; t < P.n_tiles; t += nwarps) {
         const int pos = P.n_srows + P.tile_row[t];
-        for (int k = P.tile_begin[t] + lane; k < P.tile_end[t]; k += 32) f(P.lcol[k], pos);
+        const int e = P.tile_end[t];
+#pragma unroll 4
+        for (int k = P.tile_begin[t] + lane; k < e; k += 32) f(__ldg(P.lcol + k), pos);
     }
 }
 
@@ -44,8 +50,9 @@ __global__ void k_count_cols(DevProblem P, int *cnt) {
     for_each_element(P, [&](int j, int) { atomicAdd(cnt + j, 1); });
 }
 
-__global__ void k_fill_cols(DevProblem P, const int *col_ptr, int *fill, int *pos_out) {
-    for_each_element(P, [&](int j, int pos) { pos_out[col_ptr[j] + atomicAdd(fill + j, 1)] = pos; });
+// fill[j] starts at var_ptr[j] and hands out the slots of column j
+__global__ void k_fill_cols(DevProblem P, int *fill, int *pos_out) {
+    for_each_element(P, [&](int j, int pos) { pos_out[atomicAdd(fill + j, 1)] = pos; });
 }
 
 // Block-level exclusive scan (Hillis-Steele in shared memory; counts fit int).
@@ -101,7 +108,7 @@ __global__ void k_add_offsets(int *out, const int *block_sums, int n) {
 int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s) {
     const int n1 = P.n + 1;
     const int nb = (n1 + kScanBlock - 1) / kScanBlock;
-    int *cnt = scratch;        // n + 1 counts, reused as fill cursors
+    int *cnt = scratch;        // n + 1 counts, then the fill cursors
     int *sums = scratch + n1;  // nb block sums
     cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n1, s);
     if (e != cudaSuccess) return (int)e;
@@ -109,22 +116,48 @@ int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *sc
     k_scan_blocks<<<nb, kScanBlock, 0, s>>>(cnt, var_ptr, sums, n1);
     k_scan_sums<<<1, kScanBlock, 0, s>>>(sums, nb);
     k_add_offsets<<<nb, kScanBlock, 0, s>>>(var_ptr, sums, n1);
-    e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n1, s);
+    e = cudaMemcpyAsync(cnt, var_ptr, sizeof(int) * (size_t)n1, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return (int)e;
-    k_fill_cols<<<blocks, 256, 0, s>>>(P, var_ptr, cnt, var_pos);
+    k_fill_cols<<<blocks, 256, 0, s>>>(P, cnt, var_pos);
     return (int)cudaGetLastError();
 }
 
 // ---- element arrays from the raw CSR -----------------------------------------
 // The host decides the layout (row order, slices, split-row tiles: O(m) work)
-// and uploads the CSR once; these kernels place every element: SELL slot and
-// row-contiguous copy (warp per row position), split-row arrays (block per
-// split row). Padding slots of the SELL arrays stay as cleared before.
+// and uploads the CSR once; these kernels check the elements (column range,
+// finite coefficients), fill the per-position arrays (thread per position)
+// and place every element with its FP32 screen copy: SELL slot and
+// row-contiguous copy, split-row arrays (block per split row). Padding slots
+// of the SELL arrays stay as cleared before.
 namespace {
+// Places the elements of SELL row positions, each with its FP32 screen copy
+// (coef_screen) in both layouts. One-lane rows (positions from g1_begin) go
+// thread per row: the threads of a warp hold consecutive rows of one slice,
+// so every step k stores 32 consecutive slots. Wider rows go warp per row.
 __global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
+    for (int p = L.g1_begin + tid; p < L.n_srows; p += stride) {
+        const int i = L.order[p];
+        const int s = L.pos_slice[p];
+        const long long base = L.slice_ptr[s] + (p - L.slice_row0[s]);
+        const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
+        const long long xb = L.xptr[p];
+        for (int k = 0; k < len; k++) {
+            const int c = L.col[b + k];
+            const double v = L.val[b + k];
+            const float a = coef_screen(v);
+            const long long e = base + 32LL * k;
+            L.sell_col[e] = c;
+            L.sell_val[e] = v;
+            L.sell_a32[e] = a;
+            L.xcol[xb + k] = c;
+            L.xval[xb + k] = v;
+            L.xa32[xb + k] = a;
+        }
+    }
     const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < L.n_srows; p += nwarps) {
+    for (int p = tid >> 5; p < L.g1_begin; p += stride >> 5) {
         const int i = L.order[p];
         const int s = L.pos_slice[p];
         const int lg = L.slice_lg[s], g = 1 << lg;
@@ -135,12 +168,49 @@ __global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
         for (int k = lane; k < len; k += 32) {
             const int c = L.col[b + k];
             const double v = L.val[b + k];
+            const float a = coef_screen(v);
             const long long e = base + 32LL * (k >> lg) + (k & (g - 1));
             L.sell_col[e] = c;
             L.sell_val[e] = v;
+            L.sell_a32[e] = a;
             L.xcol[xb + k] = c;
             L.xval[xb + k] = v;
+            L.xa32[xb + k] = a;
         }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_build_positions(LayoutBuild L) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < L.n_srows; p += stride) {
+        const int i = L.order[p];
+        const int len = L.row_ptr[i + 1] - L.row_ptr[i];
+        L.srow_len_out[p] = len;
+        L.srow_lhs_out[p] = L.lhs[i];
+        L.srow_rhs_out[p] = L.rhs[i];
+        L.xptr_out[p] = (int)(L.len_base[len] + (long long)(p - L.len_start[len]) * len);
+    }
+    for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < L.n_slices; sl += stride)
+        for (int p = L.slice_row0[sl]; p < L.slice_row0[sl + 1]; p++) L.pos_slice_out[p] = sl;
+}
+
+__global__ void __launch_bounds__(256) k_check_elements(const int *__restrict__ col, const double *__restrict__ val,
+                                                        int nnz, int n, int *bad) {
+    int bc = INT_MAX, bv = INT_MAX;
+    const int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += stride) {
+        if ((unsigned)__ldcs(col + k) >= (unsigned)n) bc = min(bc, k);
+        const long long b = __double_as_longlong(__ldcs(val + k));
+        if ((b & 0x7FF0000000000000LL) == 0x7FF0000000000000LL) bv = min(bv, k);  // inf or NaN
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        bc = min(bc, __shfl_xor_sync(0xffffffffu, bc, off));
+        bv = min(bv, __shfl_xor_sync(0xffffffffu, bv, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (bc != INT_MAX) atomicMin(bad, bc);
+        if (bv != INT_MAX) atomicMin(bad + 1, bv);
     }
 }
 
@@ -150,12 +220,24 @@ __global__ void __launch_bounds__(256) k_build_split(LayoutBuild L) {
         const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
         const long long o = L.lrow_ptr[r];
         for (int k = threadIdx.x; k < len; k += blockDim.x) {
+            const double v = L.val[b + k];
             L.lcol[o + k] = L.col[b + k];
-            L.lval[o + k] = L.val[b + k];
+            L.lval[o + k] = v;
+            L.la32[o + k] = coef_screen(v);
         }
     }
 }
 }  // namespace
+
+int build_layout_positions(const LayoutBuild &L, int blocks, cudaStream_t s) {
+    if (L.n_srows > 0) k_build_positions<<<blocks, 256, 0, s>>>(L);
+    return (int)cudaGetLastError();
+}
+
+int check_csr_elements(const int *col, const double *val, int nnz, int n, int *bad, int blocks, cudaStream_t s) {
+    if (nnz > 0) k_check_elements<<<blocks, 256, 0, s>>>(col, val, nnz, n, bad);
+    return (int)cudaGetLastError();
+}
 
 int build_layout_elements(const LayoutBuild &L, int blocks, cudaStream_t s) {
     if (L.n_srows > 0) k_build_sell<<<blocks, 256, 0, s>>>(L);

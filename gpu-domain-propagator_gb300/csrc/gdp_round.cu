@@ -66,12 +66,6 @@ __global__ void k_condition(DevProblem P, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
-// FP32 screen copies of coefficient values (coef_screen).
-__global__ void __launch_bounds__(256) k_coef_screen(const double *v, float *out, long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = coef_screen(v[i]);
-}
-
 __global__ void __launch_bounds__(256) k_check_bounds(DevProblem P) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < P.n; j += gridDim.x * blockDim.x) {
         const double2 b = P.bnd[j];
@@ -96,6 +90,16 @@ __global__ void __launch_bounds__(256) k_deinterleave(DevProblem P, double *lb, 
         const double2 b = P.bnd[j];
         lb[j] = b.x;
         ub[j] = b.y;
+    }
+}
+
+// Copies n bound pairs into the caller's arrays (host memory the device
+// reaches directly).
+__global__ void __launch_bounds__(256) k_copy_out(const double *lb, const double *ub, double *lb_out,
+                                                  double *ub_out, int n) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        lb_out[j] = lb[j];
+        ub_out[j] = ub[j];
     }
 }
 
@@ -165,10 +169,6 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
 }  // namespace
 
 // ---- launchers ------------------------------------------------------------
-int launch_coef_screen(const double *v, float *out, long long n, int blocks, cudaStream_t s) {
-    k_coef_screen<<<blocks, 256, 0, s>>>(v, out, n);
-    return (int)cudaGetLastError();
-}
 
 int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s) {
     if (P.n == 0) return 0;
@@ -178,6 +178,12 @@ int launch_check_bounds(const DevProblem &P, int blocks, cudaStream_t s) {
 
 int launch_interleave(const DevProblem &P, const double *lb, const double *ub, int blocks, cudaStream_t s) {
     k_interleave<<<blocks, 256, 0, s>>>(P, lb, ub);
+    return (int)cudaGetLastError();
+}
+
+int launch_copy_out(const double *lb, const double *ub, double *lb_out, double *ub_out, int n, int blocks,
+                    cudaStream_t s) {
+    if (n > 0) k_copy_out<<<blocks, 256, 0, s>>>(lb, ub, lb_out, ub_out, n);
     return (int)cudaGetLastError();
 }
 

@@ -111,6 +111,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
                                        _P_INT, C.POINTER(Options), C.POINTER(C.c_void_p)]
     lib.gdp_context_destroy.argtypes = [C.c_void_p]
     lib.gdp_propagate.argtypes = [C.c_void_p, _P_DBL, _P_DBL, C.POINTER(Stats)]
+    lib.gdp_propagate_into.argtypes = [C.c_void_p, _P_DBL, _P_DBL, _P_DBL, _P_DBL, C.POINTER(Stats)]
     lib.gdp_propagate_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
     lib.gdp_context_set_options.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.gdp_context_layout.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
@@ -167,6 +168,12 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
 
 def last_error() -> str:
     return load_library().gdp_last_error().decode(errors="replace")
+
+
+def release_cached_memory() -> None:
+    """Frees the device memory that destroyed contexts and batches left cached
+    for later ones (gdp_release_cached_memory)."""
+    _check(load_library().gdp_release_cached_memory(), "gdp_release_cached_memory")
 
 
 def _check(rc: int, what: str) -> None:
@@ -233,6 +240,10 @@ def propagate(mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_r
     """One-shot propagation (upload, propagate, download) with statistics."""
     lib = load_library()
     p = mip.normalized()
+    if p.m and p.n and p.nnz:  # a context for one call (the library copies the bounds in)
+        with Context(p, sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
+                     split_tile=split_tile, use_marking=use_marking) as ctx:
+            return ctx.propagate(lb, ub)
     lbo = _f64(p.lb if lb is None else lb).copy()
     ubo = _f64(p.ub if ub is None else ub).copy()
     o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
@@ -288,10 +299,14 @@ class Context:
         return dict(zip(keys, [int(v) for v in out]))
 
     def propagate(self, lb=None, ub=None) -> Tuple[np.ndarray, np.ndarray, dict]:
-        lbo = _f64(self.mip.lb if lb is None else lb).copy()
-        ubo = _f64(self.mip.ub if ub is None else ub).copy()
+        lbi = _f64(self.mip.lb if lb is None else lb)
+        ubi = _f64(self.mip.ub if ub is None else ub)
+        if len(lbi) != self.mip.n or len(ubi) != self.mip.n:
+            raise GDPError(f"expected {self.mip.n} bounds")
+        lbo, ubo = np.empty_like(lbi), np.empty_like(ubi)  # the library copies the inputs in
         st = Stats()
-        _check(self._lib.gdp_propagate(self._h, _pd(lbo), _pd(ubo), C.byref(st)), "gdp_propagate")
+        _check(self._lib.gdp_propagate_into(self._h, _pd(lbi), _pd(ubi), _pd(lbo), _pd(ubo), C.byref(st)),
+               "gdp_propagate_into")
         return lbo, ubo, st.as_dict()
 
     def set_model(self, model, threshold: float = 0.0, min_len: int = 8) -> None:

@@ -74,6 +74,12 @@ GDP_RETCODE gdp_default_options(gdp_options *opts);
 /* Last error message of the calling thread ("" if none). */
 const char *gdp_last_error(void);
 
+/* Device memory released by destroyed contexts and batches stays cached (up
+ * to 32 GiB) for later contexts of similar size, so that repeated
+ * create / destroy cycles allocate nothing; a failed allocation frees the
+ * cache and retries. This frees the cache now. */
+GDP_RETCODE gdp_release_cached_memory(void);
+
 /* Uploads a MIP (host CSR arrays, reference argument meaning) and builds the
  * device layout. opts may be NULL. The context owns its device memory and a
  * CUDA stream; it is not thread-safe (use one context per thread). */
@@ -87,6 +93,13 @@ GDP_RETCODE gdp_context_destroy(gdp_context *ctx);
 /* Propagates host bounds lbs/ubs (n_vars each, in/out) to a fixpoint.
  * stats may be NULL. */
 GDP_RETCODE gdp_propagate(gdp_context *ctx, double *lbs, double *ubs, gdp_stats *stats);
+
+/* As gdp_propagate, with the bounds read from lbs_in/ubs_in and the fixpoint
+ * written to lbs_out/ubs_out (n_vars each; an output may be its input). The
+ * inputs are copied to the outputs first (host threads), so on error the
+ * outputs hold the inputs. */
+GDP_RETCODE gdp_propagate_into(gdp_context *ctx, const double *lbs_in, const double *ubs_in, double *lbs_out,
+                               double *ubs_out, gdp_stats *stats);
 
 /* Same on device-resident bounds (d_lbs/d_ubs: n_vars doubles each in device
  * memory, in/out) on the given CUDA stream (NULL: the context's stream). The

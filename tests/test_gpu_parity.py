@@ -269,6 +269,68 @@ def test_single_row_and_empty_rows():
         assert_bitexact(lb, ub, ref.lb, ref.ub)
 
 
+@pytest.mark.parametrize("bad,msg", [("col", "column index out of range at non-zero 1"),
+                                     ("val", "non-finite coefficient at non-zero 2")])
+def test_invalid_elements_rejected_on_device(bad, msg):
+    """Column range and finite coefficients are checked over the uploaded CSR;
+    the error names the first bad non-zero, and the library stays usable."""
+    col, val = [0, 1, 1, 0], [1.0, 2.0, 3.0, 4.0]
+    if bad == "col":
+        col = [0, 7, 1, -1]
+    else:
+        val = [1.0, 2.0, np.inf, np.nan]
+    args = ([0, 2, 4], [1.0, 2.0], [3.0, 8.0])
+    with pytest.raises(gdp.GDPError, match=msg):
+        gdp.propagateGPUAtomic(2, 2, 4, col, args[0], val, [-1e20, -1e20], args[2], [0.0, 0.0], [10.0, 10.0],
+                               [3, 3])
+    lb, ub = gdp.propagateGPUAtomic(2, 2, 4, [0, 1, 1, 0], args[0], args[1] + [3.0, 4.0], [-1e20, -1e20], args[2],
+                                    [0.0, 0.0], [10.0, 10.0], [3, 3])
+    mip = gdp.MIP(np.array([0, 2, 4], np.int32), np.array([0, 1, 1, 0], np.int32), np.array([1.0, 2.0, 3.0, 4.0]),
+                  np.array([-1e20, -1e20]), np.array([3.0, 8.0]), np.zeros(2), np.full(2, 10.0),
+                  np.array([3, 3], np.int32))
+    ref = oracle.propagate(mip, oracle.JACOBI)
+    assert_bitexact(np.array(lb), np.array(ub), ref.lb, ref.ub)
+
+
+def test_cached_device_memory_reuse_and_release():
+    """Contexts draw on the memory that destroyed ones left cached; results do
+    not depend on what the reused blocks held, and the cache can be freed."""
+    mip_a = gdpgen.random_mip(1, seed=5, m=30_000, n=25_000, len_max=3000, dense_len=8000, n_dense_rows=2)
+    mip_b = gdpgen.random_mip(1, seed=6, m=20_000, n=18_000, len_max=2000, dense_len=5000, n_dense_rows=2)
+    ref_a = oracle.propagate(mip_a, oracle.JACOBI, split_len=TRM, split_tile=TILE, nthreads=8)
+    ref_b = oracle.propagate(mip_b, oracle.JACOBI, split_len=TRM, split_tile=TILE, nthreads=8)
+    for mip, ref in [(mip_a, ref_a), (mip_b, ref_b), (mip_a, ref_a), (mip_a, ref_a), (mip_b, ref_b)]:
+        for sync in SYNCS:
+            lb, ub, st = gpu(mip, sync)
+            assert st["rounds"] == ref.rounds
+            assert_bitexact(lb, ub, ref.lb, ref.ub)
+    gdp.release_cached_memory()
+    lb, ub, st = gpu(mip_b, gdp.MEGAKERNEL)
+    assert_bitexact(lb, ub, ref_b.lb, ref_b.ub)
+    gdp.release_cached_memory()
+
+
+def test_propagate_into_separate_and_aliased_outputs():
+    """gdp_propagate_into leaves its inputs alone, and equals gdp_propagate
+    (in place) when an output is its input."""
+    mip = gdpgen.random_mip(0, seed=11)
+    ref = oracle.propagate(mip, oracle.JACOBI, split_len=TRM, split_tile=TILE, nthreads=8)
+    lib = gdp.load_library()
+    with gdp.Context(mip, sync_type=gdp.MEGAKERNEL) as ctx:
+        lb_in, ub_in = mip.lb.astype(np.float64).copy(), mip.ub.astype(np.float64).copy()
+        keep_lb, keep_ub = lb_in.copy(), ub_in.copy()
+        lbo, ubo = np.full_like(lb_in, np.nan), np.full_like(ub_in, np.nan)
+        st = gdp.Stats()
+        assert lib.gdp_propagate_into(ctx._h, gdp._pd(lb_in), gdp._pd(ub_in), gdp._pd(lbo), gdp._pd(ubo),
+                                      None) == gdp.GDP_OKAY
+        assert_bitexact(lbo, ubo, ref.lb, ref.ub)
+        assert np.array_equal(lb_in, keep_lb) and np.array_equal(ub_in, keep_ub)
+        assert lib.gdp_propagate_into(ctx._h, gdp._pd(lb_in), gdp._pd(ub_in), gdp._pd(lb_in), gdp._pd(ub_in),
+                                      st) == gdp.GDP_OKAY
+        assert_bitexact(lb_in, ub_in, ref.lb, ref.ub)
+        assert st.rounds == ref.rounds
+
+
 def test_stats_accounting():
     mip = gdpgen.random_mip(0, seed=25)
     _, _, st = gpu(mip, gdp.MEGAKERNEL, marking=0)
