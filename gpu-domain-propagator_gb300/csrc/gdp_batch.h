@@ -46,7 +46,10 @@ public:
     // n_nodes bound vectors of ctx's problem (the context must outlive the batch).
     GDP_RETCODE init_nodes(Context *ctx, int n_nodes);
     // lbs[k], ubs[k]: member k's bounds (host, in/out).
-    GDP_RETCODE propagate(double *const *lbs, double *const *ubs, gdp_stats *member_stats, gdp_stats *total);
+    // Member k's bounds are read from lbs_in[k] / ubs_in[k] and its fixpoint
+    // written to lbs_out[k] / ubs_out[k] (an output may be its input).
+    GDP_RETCODE propagate(const double *const *lbs_in, const double *const *ubs_in, double *const *lbs_out,
+                          double *const *ubs_out, gdp_stats *member_stats, gdp_stats *total);
     // Instance batches: learned row marking for every member (m == nullptr: off).
     GDP_RETCODE set_model(const Mlp *m, float threshold, int min_len);
 
@@ -61,6 +64,8 @@ private:
     GDP_RETCODE finish_init(int device, int ctas_per_sm);
     GDP_RETCODE size_grid();
     GDP_RETCODE enqueue(cudaStream_t s);
+    void copy_in(const double *const *lbs, const double *const *ubs);
+    void copy_out(double *const *lbs, double *const *ubs);
 
     std::vector<std::unique_ptr<Context>> inst_;  // instances (units in heaviest-first order)
     Context *base_ = nullptr;                     // nodes

@@ -247,6 +247,43 @@ GDP_RETCODE Batch::set_model(const Mlp *m, float threshold, int min_len) {
     return GDP_OKAY;
 }
 
+// Member bounds to and from the pinned staging arrays, in pieces of 64K
+// variables spread over the host threads: one thread copies a few GB/s, and
+// node batches move hundreds of MB each way.
+namespace {
+template <class F>
+void for_each_piece(int n_units, const std::vector<long long> &var_base, F &&f) {
+    constexpr long long kPiece = 1 << 16;
+    std::vector<long long> first(n_units + 1, 0);  // first piece of each unit
+    for (int u = 0; u < n_units; u++)
+        first[u + 1] = first[u] + (var_base[u + 1] - var_base[u] + kPiece - 1) / kPiece;
+    const long long n_pieces = first[n_units];
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long q = 0; q < n_pieces; q++) {
+        // the unit whose pieces include q (units without variables have none)
+        const int u = (int)(std::upper_bound(first.begin(), first.end(), q) - first.begin()) - 1;
+        const long long off = (q - first[u]) * kPiece;
+        f(u, off, (size_t)std::min(kPiece, var_base[u + 1] - var_base[u] - off));
+    }
+}
+}  // namespace
+
+void Batch::copy_in(const double *const *lbs, const double *const *ubs) {
+    for_each_piece(n_units, var_base_, [&](int u, long long off, size_t n) {
+        const int k = member_of_unit_[u];
+        std::memcpy(h_lb_ + var_base_[u] + off, lbs[k] + off, sizeof(double) * n);
+        std::memcpy(h_ub_ + var_base_[u] + off, ubs[k] + off, sizeof(double) * n);
+    });
+}
+
+void Batch::copy_out(double *const *lbs, double *const *ubs) {
+    for_each_piece(n_units, var_base_, [&](int u, long long off, size_t n) {
+        const int k = member_of_unit_[u];
+        std::memcpy(lbs[k] + off, h_lb_ + var_base_[u] + off, sizeof(double) * n);
+        std::memcpy(ubs[k] + off, h_ub_ + var_base_[u] + off, sizeof(double) * n);
+    });
+}
+
 // The device part of one batch call, in stream order.
 GDP_RETCODE Batch::enqueue(cudaStream_t s) {
     const size_t vbytes = sizeof(double) * (size_t)total_vars_;
@@ -276,24 +313,21 @@ GDP_RETCODE Batch::enqueue(cudaStream_t s) {
     return GDP_OKAY;
 }
 
-GDP_RETCODE Batch::propagate(double *const *lbs, double *const *ubs, gdp_stats *member_stats, gdp_stats *total) {
+GDP_RETCODE Batch::propagate(const double *const *lbs_in, const double *const *ubs_in, double *const *lbs_out,
+                             double *const *ubs_out, gdp_stats *member_stats, gdp_stats *total) {
     const auto t0 = std::chrono::steady_clock::now();
-    if (!lbs || !ubs) {
+    if (!lbs_in || !ubs_in || !lbs_out || !ubs_out) {
         set_error("null bound arrays");
         return GDP_ERROR;
     }
     for (int u = 0; u < n_units; u++) {
         const int k = member_of_unit_[u];
-        const size_t n = (size_t)(var_base_[u + 1] - var_base_[u]);
-        if (n && (!lbs[k] || !ubs[k])) {
+        if (var_base_[u + 1] > var_base_[u] && (!lbs_in[k] || !ubs_in[k] || !lbs_out[k] || !ubs_out[k])) {
             set_error("null bounds for member " + std::to_string(k));
             return GDP_ERROR;
         }
-        if (n) {
-            std::memcpy(h_lb_ + var_base_[u], lbs[k], sizeof(double) * n);
-            std::memcpy(h_ub_ + var_base_[u], ubs[k], sizeof(double) * n);
-        }
     }
+    copy_in(lbs_in, ubs_in);
     // nodes start from the marks of their differences to the context's
     // fixpoint when its last propagation certified one; otherwise they sweep
     const int seed = nodes && base_ && base_->certified ? 1 : 0;
@@ -329,14 +363,7 @@ GDP_RETCODE Batch::propagate(double *const *lbs, double *const *ubs, gdp_stats *
         if (total) total->device_error = h_rounds_[0];
         return GDP_ERROR;
     }
-    for (int u = 0; u < n_units; u++) {
-        const int k = member_of_unit_[u];
-        const size_t n = (size_t)(var_base_[u + 1] - var_base_[u]);
-        if (n) {
-            std::memcpy(lbs[k], h_lb_ + var_base_[u], sizeof(double) * n);
-            std::memcpy(ubs[k], h_ub_ + var_base_[u], sizeof(double) * n);
-        }
-    }
+    copy_out(lbs_out, ubs_out);
     float ms = -1.f;
     if (cudaEventElapsedTime(&ms, ev0_, ev1_) != cudaSuccess) {
         ms = -1.f;

@@ -151,7 +151,16 @@ GDP_RETCODE gdp_batch_propagate(gdp_batch *b, double *const *lbs, double *const 
                                 gdp_stats *total) {
     return guarded([&]() -> GDP_RETCODE {
         if (!b) { gdp::set_error("null batch"); return GDP_ERROR; }
-        return b->impl.propagate(lbs, ubs, member_stats, total);
+        return b->impl.propagate(lbs, ubs, lbs, ubs, member_stats, total);
+    });
+}
+
+GDP_RETCODE gdp_batch_propagate_into(gdp_batch *b, const double *const *lbs_in, const double *const *ubs_in,
+                                     double *const *lbs_out, double *const *ubs_out, gdp_stats *member_stats,
+                                     gdp_stats *total) {
+    return guarded([&]() -> GDP_RETCODE {
+        if (!b) { gdp::set_error("null batch"); return GDP_ERROR; }
+        return b->impl.propagate(lbs_in, ubs_in, lbs_out, ubs_out, member_stats, total);
     });
 }
 

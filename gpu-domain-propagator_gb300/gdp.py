@@ -126,10 +126,12 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
                                      _PP_DBL, _PP_INT, C.POINTER(Options), C.POINTER(C.c_void_p)]
     lib.gdp_batch_create_nodes.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
     lib.gdp_batch_propagate.argtypes = [C.c_void_p, _PP_DBL, _PP_DBL, C.POINTER(Stats), C.POINTER(Stats)]
+    lib.gdp_batch_propagate_into.argtypes = [C.c_void_p, _PP_DBL, _PP_DBL, _PP_DBL, _PP_DBL, C.POINTER(Stats),
+                                             C.POINTER(Stats)]
     lib.gdp_batch_uses_graph.argtypes = [C.c_void_p]
     lib.gdp_batch_destroy.argtypes = [C.c_void_p]
-    for name in ("gdp_batch_create", "gdp_batch_create_nodes", "gdp_batch_propagate", "gdp_batch_uses_graph",
-                 "gdp_batch_destroy"):
+    for name in ("gdp_batch_create", "gdp_batch_create_nodes", "gdp_batch_propagate", "gdp_batch_propagate_into",
+                 "gdp_batch_uses_graph", "gdp_batch_destroy"):
         getattr(lib, name).restype = C.c_int
     _P_F = C.POINTER(C.c_float)
     lib.gdp_mlp_create.argtypes = [C.c_ulonglong, C.c_int, C.POINTER(C.c_void_p)]
@@ -445,16 +447,18 @@ class Batch:
     def propagate(self, lbs, ubs):
         """lbs, ubs: one array per member. Returns (lbs, ubs, member stats, total stats)."""
         k = len(self._sizes)
-        lbo = [_f64(x).copy() for x in lbs]
-        ubo = [_f64(x).copy() for x in ubs]
+        lbi = [_f64(x) for x in lbs]
+        ubi = [_f64(x) for x in ubs]
         for i in range(k):
-            if len(lbo[i]) != self._sizes[i] or len(ubo[i]) != self._sizes[i]:
+            if len(lbi[i]) != self._sizes[i] or len(ubi[i]) != self._sizes[i]:
                 raise GDPError(f"member {i}: expected {self._sizes[i]} bounds")
-        pl = (_P_DBL * k)(*[_pd(x) for x in lbo])
-        pu = (_P_DBL * k)(*[_pd(x) for x in ubo])
+        lbo = [np.empty_like(x) for x in lbi]  # written by the library (host threads)
+        ubo = [np.empty_like(x) for x in ubi]
+        arr = lambda xs: (_P_DBL * k)(*[_pd(x) for x in xs])
         st = (Stats * k)()
         tot = Stats()
-        _check(self._lib.gdp_batch_propagate(self._h, pl, pu, st, C.byref(tot)), "gdp_batch_propagate")
+        _check(self._lib.gdp_batch_propagate_into(self._h, arr(lbi), arr(ubi), arr(lbo), arr(ubo), st,
+                                                  C.byref(tot)), "gdp_batch_propagate_into")
         return lbo, ubo, [s.as_dict() for s in st], tot.as_dict()
 
     def close(self) -> None:

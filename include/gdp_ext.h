@@ -150,6 +150,13 @@ GDP_RETCODE gdp_batch_create_nodes(gdp_context *ctx, int n_nodes, gdp_batch **ou
 GDP_RETCODE gdp_batch_propagate(gdp_batch *b, double *const *lbs, double *const *ubs,
                                 gdp_stats *member_stats, gdp_stats *total);
 
+/* As gdp_batch_propagate, with member k's bounds read from lbs_in[k] /
+ * ubs_in[k] and its fixpoint written to lbs_out[k] / ubs_out[k] (an output
+ * may be its input); the outputs are written only when the call succeeds. */
+GDP_RETCODE gdp_batch_propagate_into(gdp_batch *b, const double *const *lbs_in, const double *const *ubs_in,
+                                     double *const *lbs_out, double *const *ubs_out, gdp_stats *member_stats,
+                                     gdp_stats *total);
+
 /* 1 if the batch runs as a captured CUDA graph (known after the first
  * propagation), 0 if it launches the same sequence directly. */
 int gdp_batch_uses_graph(const gdp_batch *b);

@@ -58,6 +58,24 @@ def test_instance_batch_matches_oracle():
         assert_bitexact(lbs[k], ubs[k], ref.lb, ref.ub, what=f"instance {k}")
 
 
+def test_batch_in_place_call_equals_into_call():
+    """gdp_batch_propagate (bounds in/out) and gdp_batch_propagate_into
+    (separate outputs, inputs untouched) give the same members."""
+    mips = _mixed_instances()[:4]
+    b = gdp.Batch.instances(mips)
+    lbs_in = [m.lb.astype(np.float64).copy() for m in mips]
+    ubs_in = [m.ub.astype(np.float64).copy() for m in mips]
+    r_into = b.propagate(lbs_in, ubs_in)
+    for k, m in enumerate(mips):
+        assert np.array_equal(lbs_in[k], m.lb) and np.array_equal(ubs_in[k], m.ub)
+    k = len(mips)
+    pl = (gdp._P_DBL * k)(*[gdp._pd(x) for x in lbs_in])
+    pu = (gdp._P_DBL * k)(*[gdp._pd(x) for x in ubs_in])
+    assert gdp.load_library().gdp_batch_propagate(b._h, pl, pu, None, None) == gdp.GDP_OKAY
+    for i in range(k):
+        assert_bitexact(lbs_in[i], ubs_in[i], r_into[0][i], r_into[1][i], what=f"member {i}")
+
+
 def test_instance_batch_repeat_and_graph():
     """Replaying the captured graph gives the same result; new bounds are honoured."""
     mips = _mixed_instances()[:3]
