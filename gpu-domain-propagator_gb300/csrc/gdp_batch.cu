@@ -153,10 +153,10 @@ __device__ __forceinline__ int unit_next_kind(const DevProblem &Pu, int r) {
     return learned_next_kind(fr.kind, fr.tight, fr.rows_deferred, Pu.n_srows, Pu.use_marking);
 }
 // A learned unit is finished after round r when it turned infeasible or a
-// FULL round changed nothing (its certification).
+// FULL or FLUSH round changed nothing (its certification).
 __device__ __forceinline__ bool unit_certified(const DevProblem &Pu, int r) {
     const RoundFlags &fr = Pu.flags[1 + (r & 1)];
-    return fr.kind == kRoundFull && fr.tight == 0u;
+    return learned_certifies(fr.kind, fr.tight);
 }
 
 // Round bookkeeping of unit u after round r (every phase of r is complete).

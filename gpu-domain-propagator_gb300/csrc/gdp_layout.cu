@@ -143,9 +143,10 @@ __global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
         const long long base = L.slice_ptr[s] + (p - L.slice_row0[s]);
         const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
         const long long xb = L.xptr[p];
+#pragma unroll 4
         for (int k = 0; k < len; k++) {
-            const int c = L.col[b + k];
-            const double v = L.val[b + k];
+            const int c = __ldg(L.col + b + k);
+            const double v = __ldg(L.val + b + k);
             const float a = coef_screen(v);
             const long long e = base + 32LL * k;
             L.sell_col[e] = c;
@@ -165,9 +166,10 @@ __global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
         const long long base = L.slice_ptr[s] + ((long long)rl << lg);
         const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
         const long long xb = L.xptr[p];
+#pragma unroll 2
         for (int k = lane; k < len; k += 32) {
-            const int c = L.col[b + k];
-            const double v = L.val[b + k];
+            const int c = __ldg(L.col + b + k);
+            const double v = __ldg(L.val + b + k);
             const float a = coef_screen(v);
             const long long e = base + 32LL * (k >> lg) + (k & (g - 1));
             L.sell_col[e] = c;
@@ -219,9 +221,10 @@ __global__ void __launch_bounds__(256) k_build_split(LayoutBuild L) {
         const int i = L.split_rows[r];
         const int b = L.row_ptr[i], len = L.row_ptr[i + 1] - b;
         const long long o = L.lrow_ptr[r];
+#pragma unroll 4
         for (int k = threadIdx.x; k < len; k += blockDim.x) {
-            const double v = L.val[b + k];
-            L.lcol[o + k] = L.col[b + k];
+            const double v = __ldg(L.val + b + k);
+            L.lcol[o + k] = __ldg(L.col + b + k);
             L.lval[o + k] = v;
             L.la32[o + k] = coef_screen(v);
         }

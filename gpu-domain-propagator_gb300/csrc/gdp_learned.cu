@@ -9,18 +9,20 @@
 //            marked row shorter than learn_min_len (the rest stay marked, their
 //            features ageing, so several markings of an unproductive row
 //            coalesce into one later processing);
-//   FLUSH    every marked row -- after a LEARNED round that changed nothing
+//   FLUSH    every marked row -- after the first round (and any FULL round)
+//            that tightened, and after a LEARNED round that changed nothing
 //            and met fewer marked rows than an eighth of all rows;
-//   FULL     every row -- the first round, after a FLUSH round that changed
-//            nothing, and after a LEARNED round that changed nothing with
-//            more marked rows than that (with use_marking == 0, every round).
+//   FULL     every row -- the first round, and after a LEARNED round that
+//            changed nothing with more marked rows than that (with
+//            use_marking == 0, every round).
 // Unlike the plain adaptive schedule, a round with many tightenings is not
 // followed by a full sweep: the marks are always pushed, so that rows the
 // model deferred are not swept along.
-// Split rows (longer than split_tile) are processed whenever marked. The plain
-// full sweep decides the end: the propagation ends only when a FULL round
-// changes nothing, so the result is a certified fixpoint of the same
-// propagation operator whatever the model decides.
+// Split rows (longer than split_tile) are processed whenever marked. The
+// propagation ends when a FULL or FLUSH round changes nothing: such a round
+// processed every row whose variables changed since its last processing, so
+// the result is a certified fixpoint of the same propagation operator
+// whatever the model decides (the certificate of exact marking).
 //
 // Trace mode processes every marked row (exact marking) and logs, for each
 // marked SELL row of a marked round, its features before processing and the
@@ -118,7 +120,7 @@ __global__ void __launch_bounds__(kCtaThreads, 2) k_megakernel_learned(DevProble
                 }
             }
             const unsigned t = *((volatile unsigned *)tight);
-            const bool certified = full && t == 0;
+            const bool certified = learned_certifies(kind, t);
             const unsigned long long marked =
                     *((volatile unsigned long long *)&P.flags[1 + par].rows_deferred);
             const int next = learned_next_kind(kind, t, marked, P.n_srows, P.use_marking);

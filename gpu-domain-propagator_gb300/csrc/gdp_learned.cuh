@@ -188,17 +188,29 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
 }
 
 // The kind of the round after one of kind `kind` that found `tight`
-// tightenings and met `marked` marked SELL rows (n_srows rows in all):
-// a round with tightenings is followed by a LEARNED round (FULL without
-// marking); a LEARNED round without tightenings by a FLUSH of the deferred
-// rows, or directly by the certifying FULL round when the marked rows were at
-// least an eighth of all rows; any other round without tightenings by FULL.
+// tightenings and met `marked` marked SELL rows (n_srows rows in all). A
+// round with tightenings is followed by a LEARNED round, except that a FULL
+// round is followed by a FLUSH (every row was just processed, so the model's
+// features tell the rows apart by nothing yet; FULL again without marking).
+// A LEARNED round without tightenings is followed by a FLUSH of the rows it
+// deferred, or by a FULL round when the marked rows were at least an eighth
+// of all rows. FULL and FLUSH rounds without tightenings end the propagation
+// (learned_certifies).
 __device__ __forceinline__ int learned_next_kind(int kind, unsigned tight, unsigned long long marked, int n_srows,
                                                  int use_marking) {
     if (tight == 0)
         return kind == kRoundLearned ? (marked * 8ULL >= (unsigned long long)n_srows ? kRoundFull : kRoundFlush)
                                      : kRoundFull;
-    return use_marking == 0 ? kRoundFull : kRoundLearned;
+    if (use_marking == 0) return kRoundFull;
+    return kind == kRoundFull ? kRoundFlush : kRoundLearned;
+}
+
+// A round certifies the fixpoint when it changed nothing and processed every
+// row whose variables changed since its last processing: a FULL round, or a
+// FLUSH (every marked row; split rows are processed whenever marked, and a
+// SELL row stays marked until processed).
+__device__ __forceinline__ bool learned_certifies(int kind, unsigned tight) {
+    return tight == 0 && (kind == kRoundFull || kind == kRoundFlush);
 }
 
 // Marks row position p dirty for round `round` (a variable of it changed):
