@@ -233,7 +233,12 @@ int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_
 }
 
 int phase_occupancy(int *act, int *cand, int *mega) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(act, k_activity, kCtaThreads, 0);
+    // the megakernel's shared memory (warp queues and row constants, ~29 KB
+    // per CTA, 3 CTAs per SM) is small: prefer a carveout that just holds it,
+    // the rest of the 256 KB per SM serving as L1 for the element streams
+    cudaError_t e = cudaFuncSetAttribute(k_megakernel, cudaFuncAttributePreferredSharedMemoryCarveout, 40);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(act, k_activity, kCtaThreads, 0);
     if (e != cudaSuccess) return (int)e;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(cand, k_exact, kCtaThreads, 0);
     if (e != cudaSuccess) return (int)e;
