@@ -103,8 +103,14 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         __syncwarp();
     }
     if (select) {
+        // rows the model decides for: marked, at least learn_min_len long and
+        // younger than the deferral cap (the others are processed whatever
+        // their score); a 16-row tile without one is not scored
+        const unsigned need = __ballot_sync(kFull, leader0 && len >= P.learn_min_len &&
+                                                       round - P.dirty[r] < kMaxDeferRounds);
         const int ntiles = ((32 >> lg) + 15) >> 4;
         for (int tile = 0; tile < ntiles; tile++) {
+            if (!(need & (lg == 0 ? 0xFFFFu << (16 * tile) : kFull))) continue;  // warp-uniform
             unsigned a[4];
             load_a_smem(&feat[tile * 16][0], lane, a);
             float z0, z1;
@@ -119,9 +125,10 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         // deferring them saves little and may stall a propagation front; a
         // row whose first unprocessed change is kMaxDeferRounds rounds old is
         // processed too, so that no row is deferred (and scored) round after
-        // round while a long propagation never lets a flush happen
-        const bool keep = act && (len < P.learn_min_len || L.z[rl] >= P.tau ||
-                                  round - P.dirty[r] >= kMaxDeferRounds);  // the same for every lane of the row
+        // round while a long propagation never lets a flush happen (L.z of
+        // those rows may be stale: their tile may have gone unscored)
+        const bool keep = act && (len < P.learn_min_len || round - P.dirty[r] >= kMaxDeferRounds ||
+                                  L.z[rl] >= P.tau);  // the same for every lane of the row
         const unsigned deferred = __ballot_sync(kFull, leader0 && !keep);
         if (lane == 0 && deferred) atomicAdd(&P.flags[0].rows_deferred, (unsigned long long)__popc(deferred));
         any_deferred = deferred != 0;
