@@ -205,8 +205,11 @@ namespace {
 // round r in flags[1 + (r & 1)].kind; a slice whose marked rows the model
 // deferred is queued again for the next round, and a unit ends only with a FULL
 // round that changes nothing, exactly as in its single-problem learned run.
+// Both instantiations run 3 CTAs per SM: the learned one then keeps 80
+// registers and spills part of the MLP's fragments to L1, which measured far
+// faster than 2 CTAs per SM without spills (the round work is latency-bound).
 template <bool kLearned>
-__global__ void __launch_bounds__(kCtaThreads, kLearned ? 2 : 3) k_batch_loop(BatchDev B) {
+__global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
     __shared__ WarpSmem ws[kWarpsPerCta];
     __shared__ LearnSmem ls[kLearned ? kWarpsPerCta : 1];
     const int lane = threadIdx.x & 31;
