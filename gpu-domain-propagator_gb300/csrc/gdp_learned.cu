@@ -81,7 +81,7 @@ __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round,
     flush_changed(P, changed);
 }
 
-__global__ void __launch_bounds__(kCtaThreads, 2) k_megakernel_learned(DevProblem P) {
+__global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel_learned(DevProblem P) {
     __shared__ WarpSmem ws[kWarpsPerCta];
     __shared__ LearnSmem ls[kWarpsPerCta];
     const int lane = threadIdx.x & 31;
