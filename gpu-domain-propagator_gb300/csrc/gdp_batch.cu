@@ -205,11 +205,12 @@ namespace {
 // round r in flags[1 + (r & 1)].kind; a slice whose marked rows the model
 // deferred is queued again for the next round, and a unit ends only with a FULL
 // round that changes nothing, exactly as in its single-problem learned run.
-// Both instantiations run 3 CTAs per SM: the learned one then keeps 80
-// registers and spills part of the MLP's fragments to L1, which measured far
-// faster than 2 CTAs per SM without spills (the round work is latency-bound).
+// Both instantiations run 5 CTAs per SM (48 registers, spills served by L1):
+// the round work is latency-bound, and on 128 chain instances the learned
+// loop took 2,093 / 912 / 866 / 844 / 1,269 ms at 2 / 3 / 4 / 5 / 6 CTAs per
+// SM, the plain one 590 / 567 / 561 / 566 ms at 3 / 4 / 5 / 6.
 template <bool kLearned>
-__global__ void __launch_bounds__(kCtaThreads, 3) k_batch_loop(BatchDev B) {
+__global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
     __shared__ WarpSmem ws[kWarpsPerCta];
     __shared__ LearnSmem ls[kLearned ? kWarpsPerCta : 1];
     const int lane = threadIdx.x & 31;
