@@ -44,7 +44,7 @@ WORKLOAD = ("power-law MIP: m=2,000,000 rows, n=1,500,000 vars, Zipf(1.8) row le
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)  # ~0.8 s timed on config 1: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gdp", "reference"], default="gdp")
     ap.add_argument("--sync", choices=["megakernel", "cpu_loop", "gpu_loop"], default="megakernel")
@@ -125,7 +125,7 @@ class Clocks:
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.p = None
