@@ -316,7 +316,10 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                 if (!grid_barrier(B.barrier, B.error)) return;
             }
         }
-        // ---- F
+        // ---- F (a row recorded infeasible in round r turns into the unit's
+        // verdict here, where the variable rule sets it)
+        for (int u = gtid; u < B.n_units; u += gthreads)
+            if (B.units[u].flags[0].infeasible_row != INT_MAX) B.units[u].flags[0].infeasible = 1;
         const bool more = r < B.max_rounds;
         if (blockIdx.x == 0) {
             if (more)

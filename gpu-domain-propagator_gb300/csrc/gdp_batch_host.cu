@@ -152,7 +152,10 @@ GDP_RETCODE Batch::finish_init(int device, int ctas_per_sm) {
     GDP_BCUDA(cudaMallocHost(&h_flags_, sizeof(RoundFlags) * 3 * (size_t)n_units));
     GDP_BCUDA(cudaMallocHost(&h_flags_init_, sizeof(RoundFlags) * 3 * (size_t)n_units));
     std::memset(h_flags_init_, 0, sizeof(RoundFlags) * 3 * (size_t)n_units);
-    for (int u = 0; u < n_units; u++) h_flags_init_[3 * u].infeasible_var = INT_MAX;
+    for (int u = 0; u < n_units; u++) {
+        h_flags_init_[3 * u].infeasible_var = INT_MAX;
+        h_flags_init_[3 * u].infeasible_row = INT_MAX;
+    }
     GDP_BCUDA(cudaMallocHost(&h_rounds_, sizeof(int) * 2));
     GDP_BCUDA(cudaMallocHost(&h_seed_, sizeof(int) * (size_t)n_units));
     GDP_BCUDA(cudaMallocHost(&h_lb_, sizeof(double) * (size_t)std::max<long long>(total_vars_, 1)));
@@ -374,12 +377,14 @@ GDP_RETCODE Batch::propagate(const double *const *lbs_in, const double *const *u
     gdp_stats tot{};
     tot.converged = 1;
     tot.infeasible_var = -1;
+    tot.infeasible_row = -1;
     for (int u = 0; u < n_units; u++) {
         const RoundFlags &f = h_flags_[3 * u];
         gdp_stats st{};
         st.rounds = f.rounds;
         st.infeasible = f.infeasible;
-        st.infeasible_var = f.infeasible ? f.infeasible_var : -1;
+        st.infeasible_var = (f.infeasible && f.infeasible_var != INT_MAX) ? f.infeasible_var : -1;
+        st.infeasible_row = (f.infeasible && f.infeasible_row != INT_MAX) ? f.infeasible_row : -1;
         st.converged = (f.infeasible || !f.change) ? 1 : 0;
         st.kernel_launches = 5;
         st.changed_vars = (long long)f.changed_vars;
@@ -387,6 +392,10 @@ GDP_RETCODE Batch::propagate(const double *const *lbs_in, const double *const *u
         st.nnz_processed = (long long)f.nnz_proc;
         st.nnz_exact = (long long)f.nnz_exact;
         st.rows_deferred = (long long)f.rows_deferred;
+        st.divisions = (long long)f.divisions;
+        st.rows_exact = (long long)f.rows_exact;
+        st.rows_go = (long long)f.rows_go;
+        st.rows_seqmax = (long long)f.rows_seqmax;
         st.full_rounds = f.full_rounds;
         st.bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc +
                                36.0 * (double)(var_base_[u + 1] - var_base_[u]) * (double)f.rounds;
@@ -401,6 +410,10 @@ GDP_RETCODE Batch::propagate(const double *const *lbs_in, const double *const *u
         tot.nnz_processed += st.nnz_processed;
         tot.nnz_exact += st.nnz_exact;
         tot.rows_deferred += st.rows_deferred;
+        tot.divisions += st.divisions;
+        tot.rows_exact += st.rows_exact;
+        tot.rows_go += st.rows_go;
+        tot.rows_seqmax += st.rows_seqmax;
         tot.full_rounds = std::max(tot.full_rounds, st.full_rounds);
         tot.bytes_algorithmic += st.bytes_algorithmic;
     }

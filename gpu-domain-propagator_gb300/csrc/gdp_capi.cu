@@ -50,7 +50,7 @@ GDP_RETCODE propagate_once_impl(int n_cons, int n_vars, int nnz, const int *col,
     if (stats) *stats = gdp_stats{};
     // reference GPU_propagator.cuh:113-116: empty problems are a no-op
     if (n_cons == 0 || n_vars == 0 || nnz == 0) {
-        if (stats) { stats->converged = 1; stats->infeasible_var = -1; }
+        if (stats) { stats->converged = 1; stats->infeasible_var = -1; stats->infeasible_row = -1; }
         return GDP_OKAY;
     }
     if (!lbs || !ubs) { gdp::set_error("null lbs/ubs"); return GDP_ERROR; }

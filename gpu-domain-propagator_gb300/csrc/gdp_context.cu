@@ -593,6 +593,12 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         P.xcol = xc; P.xval = xv; P.xa32 = xa;
         P.lcol = lc; P.lval = lv; P.la32 = la;
     }
+    {  // original row of every position (row-side infeasibility names it)
+        std::vector<int> pos_row((size_t)std::max(ns + n_lrows, 1), 0);
+        std::copy(order.begin(), order.end(), pos_row.begin());
+        std::copy(split_rows.begin(), split_rows.end(), pos_row.begin() + ns);
+        GDP_UP(P.pos_row, const int, pos_row);
+    }
     GDP_UP(P.lrow_lhs, const double, lrow_lhs);
     GDP_UP(P.lrow_rhs, const double, lrow_rhs);
     GDP_UP(P.lrow_tile0, const int, lrow_tile0);
@@ -779,6 +785,7 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
     RoundFlags init[3];
     std::memset(init, 0, sizeof(init));
     init[0].infeasible_var = INT_MAX;
+    init[0].infeasible_row = INT_MAX;
     GDP_CUDA(cudaMemcpyAsync(P.flags, init, sizeof(init), cudaMemcpyHostToDevice, s));
     GDP_CUDA(cudaMemsetAsync(P.queue, 0, sizeof(unsigned) * 8, s));
     GDP_CUDA(cudaMemsetAsync(P.xctr, 0, sizeof(unsigned) * 32, s));
@@ -816,7 +823,8 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         }
         st->rounds = f.rounds;
         st->infeasible = f.infeasible;
-        st->infeasible_var = f.infeasible ? f.infeasible_var : -1;
+        st->infeasible_var = (f.infeasible && f.infeasible_var != INT_MAX) ? f.infeasible_var : -1;
+        st->infeasible_row = (f.infeasible && f.infeasible_row != INT_MAX) ? f.infeasible_row : -1;
         st->converged = (f.infeasible || !f.change) ? 1 : 0;
         st->device_error = f.error;
         st->kernel_launches = launches;
@@ -828,6 +836,7 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         st->divisions = (long long)f.divisions;
         st->rows_exact = (long long)f.rows_exact;
         st->rows_go = (long long)f.rows_go;
+        st->rows_seqmax = (long long)f.rows_seqmax;
         st->full_rounds = f.full_rounds;
         st->bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc + 36.0 * n * (double)f.rounds;
         st->device_ms = ms;

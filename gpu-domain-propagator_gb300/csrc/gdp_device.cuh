@@ -213,17 +213,41 @@ __device__ __forceinline__ DeltaBox delta_box(long long ab, long long lbb, long 
 }
 
 // Activity accumulator: the reference's computeActivities terms with integer
-// classification (no FP64 compares); U carries the row's FP32 bound of the
-// maximum of |a| (ub - lb) (from the screen, see scr_u_bound), which the row
-// test of rows summed by several lanes uses.
+// classification (no FP64 compares), plus the first maximum of the FP64
+// |a| (ub - lb) over the elements seen: km is its order key (order_key of its
+// bit pattern; the maximum is never negative, so km is its bit pattern), p its
+// element index within the row. The virtual element 0.0 at index -1 stands for
+// the initial value of the reference's maxactdelta, so km >= 0 always.
 struct Acc {
     double minact, maxact;
     int minf, maxf;
-    float U;
+    long long km;
+    int p;
 };
 __device__ __forceinline__ void acc_init(Acc &s) {
-    s.minact = 0.0; s.maxact = 0.0; s.minf = 0; s.maxf = 0; s.U = 0.0f;
+    s.minact = 0.0; s.maxact = 0.0; s.minf = 0; s.maxf = 0; s.km = 0; s.p = -1;
 }
+// Order key of +inf: keys above it are NaN, which the reference's EPSGT never
+// takes as a new maximum.
+constexpr long long kKeyPosInf = 0x7FF0000000000000LL;
+// Element k with d = fl(|a| fl(ub - lb)) (the reference's maxactdelta term):
+// elements are visited in increasing k per accumulator, so a strict compare
+// keeps the first index of the maximum.
+__device__ __forceinline__ void acc_add_delta(Acc &s, double d, int k) {
+    const long long kd = order_key(dbits(d));
+    if (kd > s.km && kd <= kKeyPosInf) {
+        s.km = kd;
+        s.p = k;
+    }
+}
+// Combines first maxima: the larger, of equal ones the earlier element.
+__device__ __forceinline__ void acc_take_max(Acc &s, long long km, int p) {
+    if (km > s.km || (km == s.km && p < s.p)) {
+        s.km = km;
+        s.p = p;
+    }
+}
+__device__ __forceinline__ double acc_max(const Acc &s) { return __longlong_as_double(s.km); }
 // The activity terms and infinity counts of one element.
 __device__ __forceinline__ void acc_add_terms(Acc &s, double a, double lb, double ub) {
     const long long ab = dbits(a), lbb = dbits(lb), ubb = dbits(ub);
@@ -242,7 +266,7 @@ __device__ __forceinline__ void acc_combine(Acc &a, const Acc &b) {
     a.maxact = dadd(a.maxact, b.maxact);
     a.minf += b.minf;
     a.maxf += b.maxf;
-    a.U = fmaxf(a.U, b.U);
+    acc_take_max(a, b.km, b.p);
 }
 
 // min(rhs - minact, maxact - lhs) as std::min(s, t) in canConsBeTightened.
@@ -250,19 +274,54 @@ __device__ __forceinline__ double row_min_slack(double minact, double maxact, do
     const double s = dsub(rhs, minact), t = dsub(maxact, lhs);
     return (t < s) ? t : s;
 }
-// The row filter of rows summed by several lanes: true if no variable of the
-// row can be tightened. U (scr_u_bound of the row's screen) bounds every
-// FP64 |a| (ub - lb) from above, so U <= mn leaves no candidate for which
-// EPSGT(|a| (ub - lb), slack) holds: skipping such a row changes nothing.
-__device__ __forceinline__ bool u_filter_skips(int minf, int maxf, float U, double mn) {
-    if (minf > 1 && maxf > 1) return true;
-    return mn < kInf && (double)U <= mn;
-}
 // The reference's decision from its sequential maxactdelta (canConsBeTightened).
 __device__ __forceinline__ bool reference_row_go(int minf, int maxf, double maxactdelta, double mn) {
     if (minf > 1 && maxf > 1) return false;
     if (maxactdelta < kInf) return !eps_le(maxactdelta, mn);
     return true;
+}
+
+// The reference's row test (canConsBeTightened, src/propagation_methods.cuh:
+// 136-154) from the row's FP64 maximum M of |a| (ub - lb) (with the leading
+// 0.0) instead of its sequential EPS-max m (computeActivities :188-190, where
+// an element replaces m only when it exceeds m by more than EPS).
+// Let p be the first index of M. After element p, m = M unless
+// fl(M - m_before) <= EPS; later elements never replace m. Hence m <= M, and
+// m >= M - EPS - ulp(EPS)/2 (Sterbenz makes M - m_before exact unless both are
+// below 2 EPS). m >= 1e20 exactly when M >= 1e20 (doubles near 1e20 are 16384
+// apart). So, with v = fl(M - mn):
+//   v <= EPS                      -> fl(m - mn) <= v: the reference skips;
+//   v > kGoClear (2.00001e-9)     -> m - mn > 1.00001e-9: it processes the row;
+//   in between                    -> only m itself decides (seq_eps_max).
+// Returns 0 (skip), 1 (process) or 2 (undecided: compute m).
+constexpr double kGoClear = 2.00001e-9;
+__device__ __forceinline__ int row_go_from_max(int minf, int maxf, double M, double mn) {
+    if (minf > 1 && maxf > 1) return 0;
+    if (M >= kInf) return 1;
+    const double v = dsub(M, mn);
+    if (v <= kEps) return 0;
+    return (v > kGoClear || v != v) ? 1 : 2;  // NaN: the reference's !EPSLE(m, NaN) holds
+}
+
+// Row-side infeasibility: the reference's isConsInfeasible
+// (src/propagation_methods.cuh:156-159, minact > rhs or maxact < lhs), taken
+// only on a side with a finite constraint side and no infinite contribution,
+// and with the relative tolerance of var_infeasible: an absolute EPS would
+// flag feasible rows whose FP64 activities (terms up to 1e5, thousands of
+// them) carry rounding errors of that size.
+__device__ __forceinline__ bool row_infeasible(double minact, double maxact, int minf, int maxf, double lhs,
+                                               double rhs) {
+    if (minf == 0 && !is_posinf(rhs)) {
+        double s = fmax(fabs(minact), fabs(rhs));
+        if (s < 1.0) s = 1.0;
+        if (dsub(minact, rhs) > dmul(kFeasTol, s)) return true;
+    }
+    if (maxf == 0 && !is_neginf(lhs)) {
+        double s = fmax(fabs(maxact), fabs(lhs));
+        if (s < 1.0) s = 1.0;
+        if (dsub(lhs, maxact) > dmul(kFeasTol, s)) return true;
+    }
+    return false;
 }
 
 // ---- FP32 row screen -------------------------------------------------------
@@ -433,10 +492,10 @@ __device__ __forceinline__ DeltaBox delta_box32(float a, float2 b) {
     return r;
 }
 
-// True when the row filter certainly skips the row: u_filter_skips (the
-// exact pass's rule for rows summed by several lanes) and the reference's
-// test (its sequential maxactdelta is at most the largest |a| (ub - lb) up to
-// FP64 rounding) both skip it.
+// True when the reference's row test certainly skips the row, whatever order
+// the exact pass sums it in: its sequential maxactdelta is at most the largest
+// FP64 |a| (ub - lb), which the widened U bounds, and U <= min slack. Such a
+// row is not infeasible either (both slacks are >= 0).
 __device__ __forceinline__ bool scr_skips(const Scr &c, int n, double lhs, double rhs) {
     if (c.minf > 1 && c.maxf > 1) return true;
     float mn_lo, mn_hi;

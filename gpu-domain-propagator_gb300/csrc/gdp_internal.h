@@ -30,12 +30,15 @@
 
 namespace gdp {
 
-// Partial activities of a split-row tile (and of a whole split row).
+// Partial activities of a split-row tile (and of a whole split row), with
+// the first maximum of the FP64 |a| (ub - lb) over the tile's elements: km its
+// bit pattern (never negative), p its element index within the row (-1: the
+// leading 0.0 of the reference's maxactdelta).
 struct TilePart {
     double minact, maxact;
+    long long km;
     int minf, maxf;
-    float U;  // the row's FP32 bound of max |a|(ub - lb) (from its screen)
-    int pad;
+    int p, pad;
 };
 
 // A row queued for the deferred exact pass: the index of its first element
@@ -44,8 +47,8 @@ struct TilePart {
 struct XRow {
     long long base;
     int pos, len;
-    float u_hi;      // rows summed by several lanes: the screen's bound of max |a| (ub - lb)
     float slack_lo;  // the screen's lower bound of min(rhs - minact, maxact - lhs)
+    int pad;
 };
 
 // FP32 screen partial of a split-row tile (see Scr in gdp_device.cuh).
@@ -69,6 +72,7 @@ struct RoundFlags {
     int exact;           // multi-tile rows of this round that need the exact pass
     int full_rounds;     // learned marking: rounds that swept every row
     int kind;            // learned marking, batched engine: kind of the round ([1 + parity])
+    int infeasible_row;  // smallest row (original index) found infeasible (INT_MAX if none)
     unsigned long long changed_vars;  // committed variable changes, all rounds
     unsigned long long rows_proc;     // rows processed (screened), all rounds
     unsigned long long nnz_proc;      // their non-zeros
@@ -77,6 +81,7 @@ struct RoundFlags {
     unsigned long long divisions;     // candidate divisions (bound candidates computed)
     unsigned long long rows_exact;    // SELL rows through the exact FP64 pass
     unsigned long long rows_go;       // ... of which had their candidates computed
+    unsigned long long rows_seqmax;   // rows whose row test needed the sequential EPS-max (seq_eps_max)
 };
 
 enum DeviceError : int {
@@ -103,6 +108,8 @@ struct DevProblem {
     const double *xval;
     const float *xa32;           // screen copies of xval
     const double *srow_lhs, *srow_rhs;
+    // original row index of each position (SELL positions, then split rows)
+    const int *pos_row;
     // split rows
     int n_lrows, n_tiles;
     const int *lcol;

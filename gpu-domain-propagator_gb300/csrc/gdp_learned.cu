@@ -53,11 +53,13 @@ __device__ __forceinline__ void learned_activity_phase(const DevProblem &P, int 
     if (lane == 0 && L.marked) atomicAdd(marked_ctr, L.marked);
 }
 
-// Commit changed variables; mark their rows for the next round: SELL rows
-// become (or stay) dirty, split rows get the next round's stamp.
+// Commit changed variables (and the round's row-side infeasibility, as in
+// finalize_words); mark their rows for the next round: SELL rows become (or
+// stay) dirty, split rows get the next round's stamp.
 __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round, bool push, int tid,
                                                  int nthreads) {
     unsigned long long changed = 0;
+    if (tid == 0 && P.flags[0].infeasible_row != INT_MAX) P.flags[0].infeasible = 1;
     for (int w = tid; w < P.n_chg_words; w += nthreads) {
         unsigned bits = P.chg[w];
         if (!bits) continue;

@@ -158,11 +158,10 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
     if (g > 1) scr_group_reduce(c, g);
     bool exact = false;
     float2 st = make_float2(0.f, 0.f);
-    float u_hi = 0.0f, slack_lo = 0.0f;
+    float slack_lo = 0.0f;
     if (leader) {
         exact = !scr_skips(c, len, lhs, rhs);
         st = screen_stats(c, len, lhs, rhs);
-        u_hi = scr_u_bound(c);
         if (exact) {
             float hi;
             scr_slack(c, len, lhs, rhs, slack_lo, hi);
@@ -174,7 +173,7 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
     if (__any_sync(kFull, exact)) {
         ws.base[lane] = base;
         __syncwarp();
-        sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, u_hi, slack_lo, change, tight_ctr, ws,
+        sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, r, slack_lo, change, tight_ctr, ws,
                         L.tight, L.go);
     }
     __syncwarp();

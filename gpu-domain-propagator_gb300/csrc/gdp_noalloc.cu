@@ -16,9 +16,14 @@
 // that overlap on the GPU (different streams or threads at the same time)
 // race on it and must be serialized by the caller.
 //
-// Rows are summed left to right by one thread each (the reference's order),
-// so results equal those of the context path for every row up to the
-// context's thread_row_max; longer rows serialize on one thread here.
+// The CSR is checked on the device before any round (row pointers, column
+// range, variable types, finite coefficients), so a bad index is reported as
+// an error instead of turning into an out-of-range access.
+//
+// Rows are summed left to right by one thread each with the reference's row
+// test (the reference's cpu_omp round function, bit for bit), so results
+// equal those of the context path for every row up to the context's
+// thread_row_max; longer rows serialize on one thread here.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -37,14 +42,16 @@ constexpr int kNoallocMaxVars = 1 << 20;
 constexpr int kNoallocWords = kNoallocMaxVars / 32;
 constexpr size_t kNoallocBytes =
         2 * sizeof(double) * (size_t)kNoallocMaxVars + sizeof(unsigned) * (size_t)kNoallocWords + 256;
+static_assert(sizeof(RoundFlags) + 4 * sizeof(int) <= 256, "flags and input checks fit the reserve");
 
-// [lb_nxt: kNoallocMaxVars doubles][ub_nxt: kNoallocMaxVars doubles][bitmap][flags]
+// [lb_nxt: kNoallocMaxVars doubles][ub_nxt: kNoallocMaxVars doubles][bitmap][flags][input checks]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 struct NoallocView {
     double *lb_nxt, *ub_nxt;
     unsigned *chg;
     RoundFlags *flags;
+    int *bad;  // first offending index per input check (INT_MAX: none), see k_noalloc_validate
 };
 
 NoallocView view_of(unsigned char *base) {
@@ -53,6 +60,7 @@ NoallocView view_of(unsigned char *base) {
     v.ub_nxt = v.lb_nxt + kNoallocMaxVars;
     v.chg = reinterpret_cast<unsigned *>(v.ub_nxt + kNoallocMaxVars);
     v.flags = reinterpret_cast<RoundFlags *>(v.chg + kNoallocWords);
+    v.bad = reinterpret_cast<int *>(v.flags + 1);
     return v;
 }
 
@@ -67,6 +75,27 @@ struct Csr {
     const double *val, *lhs, *rhs;
     double *lb, *ub;
 };
+
+// Input checks of the device CSR, each reading only in-range entries of the
+// arrays it checks: bad[0] the first row i with row_ptr[i + 1] < row_ptr[i]
+// (-1: row_ptr[0] != 0 or row_ptr[m] != nnz), bad[1] the first non-zero whose
+// column is outside [0, n), bad[2] the first variable whose type is not 0, 1
+// or 3, bad[3] the first non-finite coefficient.
+__global__ void k_noalloc_validate(Csr A, int nnz, NoallocView S) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    if (tid == 0 && (A.row_ptr[0] != 0 || A.row_ptr[A.m] != nnz)) atomicMin(S.bad + 0, -1);
+    for (int i = tid; i < A.m; i += nt)
+        if (A.row_ptr[i + 1] < A.row_ptr[i]) atomicMin(S.bad + 0, i);
+    for (int k = tid; k < nnz; k += nt) {
+        const int j = A.col[k];
+        if (j < 0 || j >= A.n) atomicMin(S.bad + 1, k);
+        if (!isfinite(A.val[k])) atomicMin(S.bad + 3, k);
+    }
+    for (int j = tid; j < A.n; j += nt) {
+        const int t = A.vartype[j];
+        if (t != 0 && t != 1 && t != 3) atomicMin(S.bad + 2, j);
+    }
+}
 
 __global__ void k_noalloc_check(Csr A, NoallocView S) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.n; j += gridDim.x * blockDim.x)
@@ -89,6 +118,8 @@ __global__ void k_noalloc_round(Csr A, NoallocView S) {
             acts_add(a, A.val[k], A.lb[j], A.ub[j]);
         }
         const double lhs = A.lhs[i], rhs = A.rhs[i];
+        if (e > b && row_infeasible(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs, rhs))
+            atomicMin(&S.flags->infeasible_row, i);
         if (e > b && can_cons_be_tightened(a, lhs, rhs)) {
             const RowCand rc = row_cand(a, lhs, rhs);
             for (int k = b; k < e; k++) {
@@ -110,6 +141,7 @@ __global__ void k_noalloc_round(Csr A, NoallocView S) {
 
 __global__ void k_noalloc_finalize(Csr A, NoallocView S, int words) {
     int changed = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && S.flags->infeasible_row != INT_MAX) S.flags->infeasible = 1;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
         unsigned bits = S.chg[w];
         if (!bits) continue;
@@ -173,7 +205,7 @@ GDP_RETCODE propagate_noalloc(int m, int n, int nnz, const int *d_col, const int
         return GDP_ERROR;
     }
     if (m == 0 || n == 0 || nnz == 0) {
-        if (st) { st->converged = 1; st->infeasible_var = -1; }
+        if (st) { st->converged = 1; st->infeasible_var = -1; st->infeasible_row = -1; }
         return GDP_OKAY;
     }
     if (!d_col || !d_row_ptr || !d_val || !d_lhs || !d_rhs || !d_lb || !d_ub || !d_vartype) {
@@ -187,9 +219,38 @@ GDP_RETCODE propagate_noalloc(int m, int n, int nnz, const int *d_col, const int
     const Csr A{m, n, d_col, d_row_ptr, d_vartype, d_val, d_lhs, d_rhs, d_lb, d_ub};
     const int words = (n + 31) / 32;
 
+    // the input checks first: nothing below indexes with the caller's CSR
+    // until they have passed
+    const int no_bad[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
+    int bad[4];
+    NA_CUDA(cudaMemcpyAsync(S.bad, no_bad, sizeof(no_bad), cudaMemcpyHostToDevice, s));
+    const int big = m > nnz ? (m > n ? m : n) : (nnz > n ? nnz : n);
+    k_noalloc_validate<<<(big + 255) / 256 < 1024 ? (big + 255) / 256 : 1024, 256, 0, s>>>(A, nnz, S);
+    NA_CUDA(cudaGetLastError());
+    NA_CUDA(cudaMemcpyAsync(bad, S.bad, sizeof(bad), cudaMemcpyDeviceToHost, s));
+    NA_CUDA(cudaStreamSynchronize(s));
+    if (bad[0] != INT_MAX) {
+        set_error(bad[0] < 0 ? std::string("csr_row_ptrs must start at 0 and end at nnz")
+                             : "csr_row_ptrs is not monotone (row " + std::to_string(bad[0]) + ")");
+        return GDP_ERROR;
+    }
+    if (bad[1] != INT_MAX) {
+        set_error("column index out of range at non-zero " + std::to_string(bad[1]));
+        return GDP_ERROR;
+    }
+    if (bad[2] != INT_MAX) {
+        set_error("vartype must be 0, 1 or 3 (variable " + std::to_string(bad[2]) + ")");
+        return GDP_ERROR;
+    }
+    if (bad[3] != INT_MAX) {
+        set_error("non-finite coefficient at non-zero " + std::to_string(bad[3]));
+        return GDP_ERROR;
+    }
+
     RoundFlags init;
     std::memset(&init, 0, sizeof(init));
     init.infeasible_var = INT_MAX;
+    init.infeasible_row = INT_MAX;
     NA_CUDA(cudaMemcpyAsync(S.flags, &init, sizeof(init), cudaMemcpyHostToDevice, s));
     NA_CUDA(cudaMemsetAsync(S.chg, 0, sizeof(unsigned) * (size_t)words, s));
     NA_CUDA(cudaMemcpyAsync(S.lb_nxt, d_lb, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s));
@@ -215,9 +276,10 @@ GDP_RETCODE propagate_noalloc(int m, int n, int nnz, const int *d_col, const int
     if (st) {
         st->rounds = f.rounds;
         st->infeasible = f.infeasible;
-        st->infeasible_var = f.infeasible ? f.infeasible_var : -1;
+        st->infeasible_var = (f.infeasible && f.infeasible_var != INT_MAX) ? f.infeasible_var : -1;
+        st->infeasible_row = (f.infeasible && f.infeasible_row != INT_MAX) ? f.infeasible_row : -1;
         st->converged = (f.infeasible || !f.change) ? 1 : 0;
-        st->kernel_launches = launches;
+        st->kernel_launches = launches + 1;
         st->changed_vars = f.changed_vars;
         st->rows_processed = (long long)f.rounds * m;
         st->nnz_processed = (long long)f.rounds * nnz;

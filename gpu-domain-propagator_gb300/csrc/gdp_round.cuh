@@ -218,13 +218,13 @@ struct WarpSmem {
     // work statistics of this warp, written by lane 0 and flushed to the
     // round flags once per phase (not once per item: same-address atomics
     // from every warp for every item would serialise in L2)
-    unsigned long long st_rows, st_nnz, st_exact, st_div, st_xrows, st_go;
+    unsigned long long st_rows, st_nnz, st_exact, st_div, st_xrows, st_go, st_seq;
 };
 
 __device__ __forceinline__ void stats_zero(WarpSmem &ws, int lane) {
     if (lane == 0) {
         ws.st_rows = 0; ws.st_nnz = 0; ws.st_exact = 0; ws.st_div = 0;
-        ws.st_xrows = 0; ws.st_go = 0;
+        ws.st_xrows = 0; ws.st_go = 0; ws.st_seq = 0;
     }
 }
 __device__ __forceinline__ void stats_flush(const DevProblem &P, WarpSmem &ws, int lane) {
@@ -235,9 +235,91 @@ __device__ __forceinline__ void stats_flush(const DevProblem &P, WarpSmem &ws, i
         if (ws.st_div) atomicAdd(&P.flags[0].divisions, ws.st_div);
         if (ws.st_xrows) atomicAdd(&P.flags[0].rows_exact, ws.st_xrows);
         if (ws.st_go) atomicAdd(&P.flags[0].rows_go, ws.st_go);
+        if (ws.st_seq) atomicAdd(&P.flags[0].rows_seqmax, ws.st_seq);
         ws.st_rows = 0; ws.st_nnz = 0; ws.st_exact = 0; ws.st_div = 0;
-        ws.st_xrows = 0; ws.st_go = 0;
+        ws.st_xrows = 0; ws.st_go = 0; ws.st_seq = 0;
     }
+}
+
+// A row whose activities exclude [lhs, rhs] (row_infeasible): only its index is
+// recorded here; the finalize step of the round turns it into the verdict, so
+// that every driver completes the round as the oracle does.
+__device__ __forceinline__ void record_row_infeasible(const DevProblem &P, int pos) {
+    atomicMin(&P.flags[0].infeasible_row, __ldg(P.pos_row + pos));
+}
+
+// ---- the reference's sequential EPS-max, for rows row_go_from_max leaves open
+// First maximum (order key, index) of d_k = fl(|a_k| fl(ub - lb)) over the
+// elements [0, e) of a row stored contiguously at (col, val), with the
+// leading 0.0 at index -1; NaN terms never count. All 32 lanes call it and
+// every lane returns the result (a butterfly of an associative selection).
+__device__ __forceinline__ void row_first_max(const DevProblem &P, const int *col, const double *val, int e,
+                                              int lane, long long &km, int &p) {
+    Acc s;
+    acc_init(s);
+    for (int k = lane; k < e; k += 32) {
+        const double2 b = load_bnd(P, __ldg(col + k));
+        acc_add_delta(s, dmul(fabs(__ldg(val + k)), dsub(b.y, b.x)), k);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const long long ok = __shfl_xor_sync(kFull, s.km, off);
+        const int op = __shfl_xor_sync(kFull, s.p, off);
+        acc_take_max(s, ok, op);
+    }
+    km = s.km;
+    p = s.p;
+}
+
+// The reference's sequential EPS-max of the row's elements [0, len)
+// (computeActivities, src/propagation_methods.cuh:188-190), given the first
+// maximum (km, p) of [0, len). Over a prefix [0, E) with first maximum (M, q),
+// m(E) = fl(M - m(q)) > EPS ? M : m(q) (row_go_from_max), and m(E) = M outright
+// when the first maximum M' of [0, q) has fl(M - M') > EPS; m = 0 when the
+// maximum is the leading 0.0. The prefix maxima are warp passes; their values
+// wait in a stack of one level per lane. A chain deeper than 32 levels (values
+// each within EPS of the next) ends with a serial scan. All 32 lanes call it.
+__device__ __noinline__ double seq_eps_max(const DevProblem &P, const int *col, const double *val, int len,
+                                           long long km, int p, int lane) {
+    double stack = 0.0;
+    int depth = 0, E = len;
+    double x = 0.0;
+    for (;;) {
+        if (p < 0) {
+            x = 0.0;
+            break;
+        }
+        const double M = __longlong_as_double(km);
+        if (depth == 32) {
+            double m = 0.0;
+            if (lane == 0)
+                for (int k = 0; k < E; k++) {
+                    const double2 b = load_bnd(P, __ldg(col + k));
+                    const double d = dmul(fabs(__ldg(val + k)), dsub(b.y, b.x));
+                    if (eps_gt(d, m)) m = d;
+                }
+            x = __shfl_sync(kFull, m, 0);
+            break;
+        }
+        if (lane == depth) stack = M;
+        depth++;
+        long long km2;
+        int p2;
+        row_first_max(P, col, val, p, lane, km2, p2);
+        if (p2 >= 0 && eps_gt(M, __longlong_as_double(km2))) {
+            depth--;  // m(E) = M
+            x = M;
+            break;
+        }
+        E = p;
+        km = km2;
+        p = p2;
+    }
+    for (int i = depth - 1; i >= 0; i--) {
+        const double Mi = __shfl_sync(kFull, stack, i);
+        if (eps_gt(Mi, x)) x = Mi;
+    }
+    return x;
 }
 
 // Warp-level dynamic work counter that keeps the next claim in flight while
@@ -279,7 +361,8 @@ __device__ __forceinline__ void acc_group_reduce(Acc &s, int g) {
         o.maxact = __shfl_down_sync(kFull, s.maxact, off);
         o.minf = __shfl_down_sync(kFull, s.minf, off);
         o.maxf = __shfl_down_sync(kFull, s.maxf, off);
-        o.U = __shfl_down_sync(kFull, s.U, off);
+        o.km = __shfl_down_sync(kFull, s.km, off);
+        o.p = __shfl_down_sync(kFull, s.p, off);
         acc_combine(s, o);
     }
 }
@@ -333,12 +416,16 @@ __device__ __forceinline__ ElemView sell_view(const DevProblem &P) {
 // The leader lane of each row (sub == 0) holds its position, lhs and rhs.
 //   pass 1: exact FP64 activities. g == 1 rows are summed left to right,
 //           with the reference's sequential EPS-max of |a|(ub - lb) in the
-//           same loop, and take the reference's row test; g > 1 rows are
-//           combined by a shuffle tree and use the FP32 bound rule.
+//           same loop; g > 1 rows are combined by a shuffle tree together
+//           with the first FP64 maximum of |a|(ub - lb), from which
+//           row_go_from_max takes the reference's decision (seq_eps_max over
+//           the row-contiguous copy where it cannot). Every row takes the
+//           reference's row test, and every row is checked for row-side
+//           infeasibility.
 //   pass 2: candidates through the warp division queue.
 __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemView ev, int lg, int lane,
                                                 bool exact, int len,
-                                                int cnt, double lhs, double rhs, float u_hi, float slack_lo,
+                                                int cnt, double lhs, double rhs, int pos, float slack_lo,
                                                 int *change,
                                                 unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
                                                 int *row_go = nullptr) {
@@ -387,13 +474,32 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
             const double a = __ldg(val + st * i);
             const double2 b = load_bnd(P, j);
             acc_add_terms(s, a, b.x, b.y);
+            acc_add_delta(s, dmul(fabs(a), dsub(b.y, b.x)), sub + (i << lg));
         }
         acc_group_reduce(s, g);
         if (leader) {
             mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
-            dec = u_filter_skips(s.minf, s.maxf, u_hi, mn) ? 0 : 1;
+            dec = row_go_from_max(s.minf, s.maxf, acc_max(s), mn);
+        }
+        // rows whose test only the sequential EPS-max decides (the largest
+        // |a| (ub - lb) exceeds the slack by EPS to 2.00001e-9): the warp
+        // computes it row by row over the row-contiguous copy
+        unsigned amb = __ballot_sync(kFull, leader && dec == 2);
+        if (lane == 0) ws.st_seq += __popc(amb);
+        while (amb) {
+            const int src = __ffs(amb) - 1;
+            amb &= amb - 1;
+            const int apos = __shfl_sync(kFull, pos, src);
+            const int alen = __shfl_sync(kFull, len, src);
+            const long long akm = __shfl_sync(kFull, s.km, src);
+            const int ap = __shfl_sync(kFull, s.p, src);
+            const double amn = __shfl_sync(kFull, mn, src);
+            const long long xb = __ldg(P.xptr + apos);
+            const double m = seq_eps_max(P, P.xcol + xb, P.xval + xb, alen, akm, ap, lane);
+            if (lane == src) dec = eps_le(m, amn) ? 0 : 1;
         }
     }
+    if (leader && row_infeasible(s.minact, s.maxact, s.minf, s.maxf, lhs, rhs)) record_row_infeasible(P, pos);
     {
         const unsigned bx = __ballot_sync(kFull, leader);
         if (lane == 0) ws.st_xrows += __popc(bx);
@@ -510,7 +616,6 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     // FP32 screen
     bool exact = false;
     double lhs = 0.0, rhs = 0.0;
-    float u_hi = 0.0f;     // the row's bound of max |a| (ub - lb), leaders
     float slack_lo = 0.0f;  // the screen's lower bound of its slacks, leaders of exact rows
     {
         const int *col = P.sell_col + base;
@@ -528,7 +633,6 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
             lhs = __ldg(P.srow_lhs + r);
             rhs = __ldg(P.srow_rhs + r);
             exact = !scr_skips(c, len, lhs, rhs);
-            u_hi = scr_u_bound(c);
             if (exact) {
                 float hi;
                 scr_slack(c, len, lhs, rhs, slack_lo, hi);
@@ -542,14 +646,14 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         unsigned first = 0;
         if (lane == 0) first = atomicAdd(P.xctr + 16 * par + lg, (unsigned)__popc(bal));
         first = __shfl_sync(kFull, first, 0);
-        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len, u_hi, slack_lo};
+        if (exact) P.xrow[P.cls_begin[lg] + first + __popc(bal & ((1u << lane) - 1u))] = XRow{xbase, r, len, slack_lo, 0};
         return;
     }
     exact = __shfl_sync(kFull, exact, rl << lg) && act;
     if (!__any_sync(kFull, exact)) return;
     ws.base[lane] = base;
     __syncwarp();
-    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, u_hi, slack_lo, change, tight_ctr, ws);
+    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, r, slack_lo, change, tight_ctr, ws);
 }
 
 // K slices of one-lane rows (g = 1) screened together in the deferred-exact
@@ -634,7 +738,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k], 0.0f, slo[k]};
+        if (exact[k]) P.xrow[first + __popc(bal[k] & lt)] = XRow{xbase[k], r[k], len[k], slo[k], 0};
         first += __popc(bal[k]);
     }
 }
@@ -655,16 +759,16 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             const int k = (int)__shfl_sync(kFull, k0, 0) + rl;
             if (k - rl >= n) break;
             const bool exact = k < n;
-            int len = 0, cnt = 0;
+            int len = 0, cnt = 0, pos = 0;
             long long base = 0;
             double lhs = 0.0, rhs = 0.0;
-            float u_hi = 0.0f, slack_lo = 0.0f;
+            float slack_lo = 0.0f;
             if (exact) {
                 const XRow x = P.xrow[P.cls_begin[lg] + k];
                 const int p = x.pos;
+                pos = p;
                 base = x.base + sub;
                 len = x.len;
-                u_hi = x.u_hi;
                 slack_lo = x.slack_lo;
                 cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
                 if (sub == 0) {
@@ -674,7 +778,7 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             }
             ws.base[lane] = base;
             __syncwarp();
-            sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, u_hi,
+            sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, pos,
                             slack_lo, change, tight_ctr, ws);
             __syncwarp();
         }
@@ -691,25 +795,43 @@ __device__ __forceinline__ void acc_shfl_reduce(Acc &s) {
         o.maxact = __shfl_down_sync(kFull, s.maxact, off);
         o.minf = __shfl_down_sync(kFull, s.minf, off);
         o.maxf = __shfl_down_sync(kFull, s.maxf, off);
-        o.U = __shfl_down_sync(kFull, s.U, off);
+        o.km = __shfl_down_sync(kFull, s.km, off);
+        o.p = __shfl_down_sync(kFull, s.p, off);
         acc_combine(s, o);
     }
 }
 
-// Decision (the FP32 bound rule) and candidates of split row `row` over the
-// element range [b, e) of one tile, from the row's complete activities held by
-// lane 0; the warp queues the divisions.
+// The reference's row test (row_go_from_max, seq_eps_max where it cannot
+// decide) and the candidates of split row `row` over the element range
+// [b, e) of one tile, from the row's complete activities and first maximum
+// held by lane 0; the warp queues the divisions. The row's first tile also
+// checks it for row-side infeasibility.
 __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int row, int b, int e, const Acc &s0,
                                                      int lane, int *change, unsigned *tight_ctr, WarpSmem &ws) {
     RowC c;
     int go = 0;
+    double mn = 0.0;
+    const int t0 = __ldg(P.lrow_tile0 + row);
+    const int rb = __ldg(P.tile_begin + t0);
     if (lane == 0) {
         const double lhs = __ldg(P.lrow_lhs + row), rhs = __ldg(P.lrow_rhs + row);
-        const double mn = row_min_slack(s0.minact, s0.maxact, lhs, rhs);
-        go = !u_filter_skips(s0.minf, s0.maxf, s0.U, mn);
+        mn = row_min_slack(s0.minact, s0.maxact, lhs, rhs);
+        go = row_go_from_max(s0.minf, s0.maxf, acc_max(s0), mn);
+        if (b == rb && row_infeasible(s0.minact, s0.maxact, s0.minf, s0.maxf, lhs, rhs))
+            record_row_infeasible(P, P.n_srows + row);
         c = make_rowc(s0.minact, s0.maxact, s0.minf, s0.maxf, lhs, rhs);
     }
     go = __shfl_sync(kFull, go, 0);
+    if (go == 2) {  // every tile of the row reaches the same m
+        const int re = __ldg(P.tile_end + __ldg(P.lrow_tile0 + row + 1) - 1);
+        const double m = seq_eps_max(P, P.lcol + rb, P.lval + rb, re - rb, __shfl_sync(kFull, s0.km, 0),
+                                     __shfl_sync(kFull, s0.p, 0), lane);
+        if (lane == 0) {
+            go = eps_le(m, mn) ? 0 : 1;
+            if (b == rb) ws.st_seq++;
+        }
+        go = __shfl_sync(kFull, go, 0);
+    }
     if (!go) return;
     c.slack = __shfl_sync(kFull, c.slack, 0);
     c.surplus = __shfl_sync(kFull, c.surplus, 0);
@@ -771,9 +893,11 @@ __device__ __forceinline__ void scr_shfl_reduce(Scr &c) {
     }
 }
 
-// Exact FP64 partial of the element range [b, e): lane l sums elements l,
-// l+32, ... in order, shuffle tree across lanes; lane 0 holds the result.
-__device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int lane) {
+// Exact FP64 partial of the element range [b, e) of a split row whose first
+// element is rb: lane l sums elements l, l+32, ... in order, shuffle tree
+// across lanes, with the first maximum of |a| (ub - lb) (indices from rb);
+// lane 0 holds the result.
+__device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int rb, int lane) {
     Acc s;
     acc_init(s);
 #pragma unroll 4
@@ -782,6 +906,7 @@ __device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int
         const double a = __ldg(P.lval + k);
         const double2 bb = load_bnd(P, j);
         acc_add_terms(s, a, bb.x, bb.y);
+        acc_add_delta(s, dmul(fabs(a), dsub(bb.y, bb.x)), k - rb);
     }
     acc_shfl_reduce(s);
     return s;
@@ -822,8 +947,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     }
     if (!single) return true;
     if (!__shfl_sync(kFull, exact, 0)) return false;
-    Acc s = tile_exact(P, b, e, lane);
-    s.U = scr_u_bound(c);  // lane 0 decides with it
+    const Acc s = tile_exact(P, b, e, b, lane);
     split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, ws);
     return false;
 }
@@ -854,12 +978,11 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
     }
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
-    const Acc s = tile_exact(P, b, e, lane);
+    const Acc s = tile_exact(P, b, e, __ldg(P.tile_begin + t0), lane);
     if (lane == 0) {
-        // every tile of the row carries the row's bound of max |a| (ub - lb)
         TilePart tp;
-        tp.minact = s.minact; tp.maxact = s.maxact; tp.minf = s.minf; tp.maxf = s.maxf;
-        tp.U = scr_u_bound(c);
+        tp.minact = s.minact; tp.maxact = s.maxact; tp.km = s.km; tp.minf = s.minf; tp.maxf = s.maxf;
+        tp.p = s.p;
         tp.pad = 0;
         P.tile_part[t] = tp;
         ws.st_exact += (unsigned long long)(e - b);
@@ -882,16 +1005,17 @@ __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane
     Acc s;
     acc_init(s);
     for (int b = t0; b < t1; b += 32) {
-        TilePart p = {0.0, 0.0, 0, 0, 0.0f, 0};
-        if (b + lane < t1) p = P.tile_part[b + lane];
+        TilePart tp = {0.0, 0.0, 0, 0, 0, -1, 0};
+        if (b + lane < t1) tp = P.tile_part[b + lane];
         const int cnt = min(32, t1 - b);
         for (int i = 0; i < cnt; i++) {
             Acc o;
-            o.minact = __shfl_sync(kFull, p.minact, i);
-            o.maxact = __shfl_sync(kFull, p.maxact, i);
-            o.minf = __shfl_sync(kFull, p.minf, i);
-            o.maxf = __shfl_sync(kFull, p.maxf, i);
-            o.U = __shfl_sync(kFull, p.U, i);
+            o.minact = __shfl_sync(kFull, tp.minact, i);
+            o.maxact = __shfl_sync(kFull, tp.maxact, i);
+            o.minf = __shfl_sync(kFull, tp.minf, i);
+            o.maxf = __shfl_sync(kFull, tp.maxf, i);
+            o.km = __shfl_sync(kFull, tp.km, i);
+            o.p = __shfl_sync(kFull, tp.p, i);
             if (lane == 0) {
                 if (b + i == t0) s = o;
                 else acc_combine(s, o);
@@ -909,7 +1033,8 @@ __device__ __forceinline__ void flush_changed(const DevProblem &P, unsigned long
     if ((threadIdx.x & 31) == __ffs(active) - 1 && changed) atomicAdd(&P.flags[0].changed_vars, changed);
 }
 
-// Commit changed variables nxt -> cur, apply the infeasibility rule, mark the
+// Commit changed variables nxt -> cur, apply the infeasibility rules (a row
+// recorded infeasible in this round, a variable whose bounds cross), mark the
 // rows of changed variables for the next round, clear the bitmap.
 // One warp per word of the bitmap: lane l commits variable 32 w + l, then the
 // warp pushes the marks of each changed variable's rows together, 32 per step
@@ -920,6 +1045,7 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
                                                int nthreads) {
     const int lane = tid & 31;
     unsigned long long changed = 0;
+    if (tid == 0 && P.flags[0].infeasible_row != INT_MAX) P.flags[0].infeasible = 1;
     for (int w = tid >> 5; w < P.n_chg_words; w += nthreads >> 5) {
         const unsigned bits = P.chg[w];
         if (!bits) continue;  // warp-uniform

@@ -78,10 +78,11 @@ class Stats(C.Structure):
         ("nnz_exact", C.c_longlong),
         ("rows_deferred", C.c_longlong),
         ("full_rounds", C.c_int),
-        ("pad_", C.c_int),
+        ("infeasible_row", C.c_int),
         ("divisions", C.c_longlong),
         ("rows_exact", C.c_longlong),
         ("rows_go", C.c_longlong),
+        ("rows_seqmax", C.c_longlong),
     ]
 
     def as_dict(self) -> dict:

@@ -47,8 +47,11 @@ typedef struct {
 typedef struct {
     int rounds;             /* rounds executed (the reference's prop_round - 1) */
     int converged;          /* 1: the last round changed nothing (or infeasible) */
-    int infeasible;         /* 1: some variable has lb - ub > GDP_FEASTOL*max(1,|lb|,|ub|) */
-    int infeasible_var;     /* smallest violating variable, -1 if feasible */
+    int infeasible;         /* 1: some variable has lb - ub > GDP_FEASTOL*max(1,|lb|,|ub|), or some
+                               row's activities exclude its sides: with no infinite contribution on
+                               that side, minact - rhs or lhs - maxact > GDP_FEASTOL*max(1,|act|,|side|)
+                               (the reference's isConsInfeasible with a relative tolerance) */
+    int infeasible_var;     /* smallest violating variable, -1 if none */
     int device_error;       /* device-side error code, 0 if none */
     int kernel_launches;    /* kernels launched by the propagation */
     long long changed_vars; /* variable bound changes committed, summed over rounds */
@@ -62,10 +65,12 @@ typedef struct {
                                went through the exact FP64 pass, summed over rounds */
     long long rows_deferred; /* learned marking: marked rows the model left for a later round */
     int full_rounds;        /* learned marking: rounds that swept every row (incl. the certification) */
-    int pad_;
+    int infeasible_row;     /* smallest row found infeasible by the row rule, -1 if none */
     long long divisions;    /* bound candidates computed (one FP64 division each), summed over rounds */
     long long rows_exact;   /* rows up to split_tile non-zeros that went through the exact FP64 pass */
     long long rows_go;      /* ... of which passed the row test (candidates computed) */
+    long long rows_seqmax;  /* row tests that needed the reference's sequential EPS-max of |a|(ub-lb)
+                               (the FP64 maximum exceeded the slack by EPS to 2.00001e-9) */
 } gdp_stats;
 
 /* Fills *opts with the defaults. */

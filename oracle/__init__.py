@@ -32,7 +32,7 @@ _P_DBL = C.POINTER(C.c_double)
 class _Result(C.Structure):
     _fields_ = [("rounds", C.c_int), ("converged", C.c_int), ("infeasible", C.c_int),
                 ("infeasible_var", C.c_int), ("candidates", C.c_longlong), ("rows_processed", C.c_longlong),
-                ("nnz_processed", C.c_longlong), ("rows_go", C.c_longlong)]
+                ("nnz_processed", C.c_longlong), ("rows_go", C.c_longlong), ("infeasible_row", C.c_int)]
 
 
 class _Acts(C.Structure):
@@ -52,6 +52,7 @@ class Result:
     rows_processed: int = 0
     nnz_processed: int = 0
     rows_go: int = 0  # GPU mode: processed rows of at most split_tile non-zeros that passed their row test
+    infeasible_row: int = -1  # smallest row the row rule found infeasible (-1: none)
 
 
 _o = None
@@ -92,6 +93,7 @@ def lib():
         o.gdpo_activities.argtypes = [C.c_int, _P_INT, _P_INT, _P_DBL, _P_DBL, _P_DBL]
         o.gdpo_activities.restype = _Acts
         o.gdpo_var_infeasible.argtypes = [C.c_double, C.c_double]
+        o.gdpo_row_infeasible.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double]
         o.gdpo_jacobi_round.argtypes = [C.c_int, C.c_int, _P_INT, _P_INT, _P_DBL, _P_DBL, _P_DBL, _P_DBL, _P_DBL,
                                         _P_INT, C.POINTER(C.c_ubyte), _P_DBL, _P_DBL, C.POINTER(C.c_ubyte),
                                         C.c_int]
@@ -135,8 +137,8 @@ def _pd(a):
 def propagate(mip, schedule: int = JACOBI, max_rounds: int = 0, nthreads: int = 1, lb=None, ub=None,
               split_len: int = 0, split_tile: int = 0) -> Result:
     """Oracle restatement (libgdporacle.so). split_len/split_tile > 0 sum rows
-    longer than split_len in the GPU path's tile order (gdpo_activities_split)
-    instead of left to right."""
+    longer than split_len in the GPU path's lane-group / warp-tile order
+    instead of left to right (the row test and candidates stay the reference's)."""
     o = lib()
     rp, col, val, lhs, rhs, vt = _arrays(mip)
     lbo = np.array(mip.lb if lb is None else lb, dtype=np.float64, copy=True)
@@ -151,7 +153,7 @@ def propagate(mip, schedule: int = JACOBI, max_rounds: int = 0, nthreads: int = 
     if rc != 0:
         raise ValueError(f"oracle rejected the input ({rc})")
     return Result(lbo, ubo, res.rounds, bool(res.converged), bool(res.infeasible), res.infeasible_var, dt,
-                  res.rows_processed, res.nnz_processed, res.rows_go)
+                  res.rows_processed, res.nnz_processed, res.rows_go, res.infeasible_row)
 
 
 def ref_propagate(mip, schedule: int = JACOBI, max_rounds: int = 0, lb=None, ub=None) -> Result:

@@ -11,6 +11,7 @@
  */
 #include "gdp_oracle.h"
 
+#include <limits.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -56,6 +57,25 @@ int gdpo_can_cons_be_tightened(double minact, double maxact, int minact_inf, int
 /* reference src/propagation_methods.cuh:156-159 */
 int gdpo_is_cons_infeasible(double minact, double maxact, double rhs, double lhs) {
     return (minact > rhs || maxact < lhs);
+}
+
+/* Row-side infeasibility rule of this project (the reference never calls
+ * isConsInfeasible on a propagation path): the reference's isConsInfeasible
+ * (src/propagation_methods.cuh:156-159), taken only on a side with a finite
+ * constraint side and no infinite contribution, with the relative tolerance
+ * of gdpo_var_infeasible. */
+int gdpo_row_infeasible(double minact, double maxact, int minf, int maxf, double lhs, double rhs) {
+    if (minf == 0 && !is_posinf(rhs)) {
+        double s = fabs(minact) > fabs(rhs) ? fabs(minact) : fabs(rhs);
+        if (s < 1.0) s = 1.0;
+        if (minact - rhs > O_FEASTOL * s) return 1;
+    }
+    if (maxf == 0 && !is_neginf(lhs)) {
+        double s = fabs(maxact) > fabs(lhs) ? fabs(maxact) : fabs(lhs);
+        if (s < 1.0) s = 1.0;
+        if (lhs - maxact > O_FEASTOL * s) return 1;
+    }
+    return 0;
 }
 
 /* reference src/propagation_methods.cuh:78-106 */
@@ -149,73 +169,27 @@ gdpo_acts gdpo_activities(int row, const int *col, const int *row_ptr, const dou
 static inline void atomic_max_d(double *addr, double v);
 static inline void atomic_min_d(double *addr, double v);
 
-/* ---- GPU mode: the row rule and summation order of the GB300 kernels ----
+/* ---- GPU mode: the summation order of the GB300 kernels ----
  * Rows up to thread_row_max non-zeros follow the reference exactly. Longer
- * rows differ in two ways that the GPU kernels use and the tests pin bit for
- * bit:
- *  1. the row test uses an FP32 upper bound U >= max |a|(ub-lb) instead of the
- *     sequential EPS-max: a row is skipped when both infinity counts exceed 1,
- *     or when min(rhs-minact, maxact-lhs) < 1e20 and U*(1+2^-20) <= that
- *     minimum. U bounds the reference's maxactdelta from above, so every row
- *     the reference processes is processed (the per-variable tests are the
- *     reference's, exact); extra rows only matter when some |a|(ub-lb) lies
- *     within 2e-9 of the slack.
- *  2. rows up to split_tile non-zeros are summed by a group of g lanes
- *     (gdpo_lanes_per_row): lane l sums elements l, l+g, ... in order and a
- *     shuffle tree combines the group; longer rows are summed per warp tile
- *     of split_tile non-zeros (lane l sums elements l, l+32, ... of the tile,
- *     shuffle tree over 32 lanes), tile partials combined in tile order.
- * U is the GPU screen's bound of max |a| (ub - lb): the maximum, NaN
- * propagating, of |a32| * fma(|ub32| + |lb32|, 2^-21, ub32 - lb32) over the
- * round-to-nearest float copies of the coefficients and bounds (screen_coef,
- * screen_bound), evaluated in float exactly like the GPU. */
+ * rows are summed in another order, which the GPU kernels use and the tests
+ * pin bit for bit:
+ *  - rows up to split_tile non-zeros are summed by a group of g lanes
+ *    (gdpo_lanes_per_row): lane l sums elements l, l+g, ... in order and a
+ *    shuffle tree combines the group;
+ *  - longer rows are summed per warp tile of split_tile non-zeros (lane l
+ *    sums elements l, l+32, ... of the tile, shuffle tree over 32 lanes),
+ *    tile partials combined in tile order.
+ * Every row takes the reference's row test (canConsBeTightened) with the
+ * reference's sequential maxactdelta, which does not depend on how the
+ * activities are summed (the kernels reach the same decision from the
+ * row's FP64 maximum of |a|(ub-lb) and, where that cannot decide, the
+ * sequential EPS-max itself). */
 typedef struct {
     double minact, maxact;
     int minf, maxf;
-    float U;
 } gacc;
 
-static inline uint64_t dbits(double x) { uint64_t b; memcpy(&b, &x, 8); return b; }
-static inline float fbits(uint32_t b) { float f; memcpy(&f, &b, 4); return f; }
-
-/* FP32 copies the GPU screen reads: coefficients in (0, 1e-9] -> NaN, above
- * 2^40 in magnitude -> +-inf, non-zero below 2^-60 -> NaN with a's sign;
- * bounds counted as infinite (lb <= -1e20, ub >= 1e20) -> -inf / +inf, finite
- * bounds above 2^100 in magnitude -> NaN; all else round-to-nearest. */
-static inline float screen_coef(double a) {
-    const double m = fabs(a);
-    if (a > 0.0 && a <= O_EPS) return NAN;
-    if (m > 0x1p40) return a > 0 ? INFINITY : -INFINITY;
-    if (m != 0.0 && m < 0x1p-60) return a > 0 ? NAN : -NAN;
-    return (float)a;
-}
-static inline float screen_bound(double x, int upper) {
-    if (upper ? x >= O_INF : x <= -O_INF) return upper ? INFINITY : -INFINITY;
-    if (fabs(x) > 0x1p100 || isnan(x)) return NAN;
-    return (float)x;
-}
-static inline float max_nan(float a, float b) { return (isnan(a) || isnan(b)) ? NAN : (a > b ? a : b); }
-static inline float screen_delta(double coeff, double l, double u) {
-    const float a = screen_coef(coeff), l32 = screen_bound(l, 0), u32 = screen_bound(u, 1);
-    const float d = u32 - l32, w = fabsf(u32) + fabsf(l32);
-    return fabsf(a) * fmaf(w, 0x1p-21f, d);
-}
-/* float(U * (1 + 2^-20) + 2^-80) rounded upwards (the GPU's __fmaf_ru), from
- * exact double arithmetic: U * (1 + 2^-20) has at most 45 significant bits. */
-static inline float ru_float(double x) {
-    float f = (float)x;
-    if ((double)f < x) f = nextafterf(f, INFINITY);
-    return f;
-}
-static inline float u_bound(float U) {
-    if (isnan(U)) return U;
-    const double y = (double)U * (1.0 + 0x1p-20);
-    if (y < 0x1p-27) return ru_float(y + 0x1p-80); /* exact in double */
-    const float fy = ru_float(y);
-    return ((double)fy - y >= 0x1p-80) ? fy : nextafterf(fy, INFINITY);
-}
-
-static inline void gacc_init(gacc *s) { s->minact = 0.0; s->maxact = 0.0; s->minf = 0; s->maxf = 0; s->U = 0.0f; }
+static inline void gacc_init(gacc *s) { s->minact = 0.0; s->maxact = 0.0; s->minf = 0; s->maxf = 0; }
 
 static inline void gacc_add(gacc *s, double coeff, double l, double u) {
     const int pos = coeff > O_EPS;
@@ -226,7 +200,6 @@ static inline void gacc_add(gacc *s, double coeff, double l, double u) {
     s->maxf += max_inf;
     if (!min_inf) s->minact = s->minact + (coeff > 0 ? coeff * l : coeff * u);
     if (!max_inf) s->maxact = s->maxact + (coeff > 0 ? coeff * u : coeff * l);
-    s->U = max_nan(s->U, screen_delta(coeff, l, u));
 }
 
 static inline void gacc_combine(gacc *a, const gacc *b) {
@@ -234,7 +207,6 @@ static inline void gacc_combine(gacc *a, const gacc *b) {
     a->maxact = a->maxact + b->maxact;
     a->minf += b->minf;
     a->maxf += b->maxf;
-    a->U = max_nan(a->U, b->U);
 }
 
 static gacc gacc_tile(int b, int e, const int *col, const double *val, const double *lb, const double *ub) {
@@ -290,31 +262,37 @@ static gacc gpu_row_acts(int row, const int *col, const int *row_ptr, const doub
     return a;
 }
 
-int gdpo_gpu_row_go(double minact, double maxact, int minf, int maxf, float U, double lhs, double rhs) {
-    if (minf > 1 && maxf > 1) return 0;
-    const double s = rhs - minact, t = maxact - lhs;
-    const double mn = (t < s) ? t : s;
-    const float Ub = u_bound(U);
-    if (mn < O_INF && (double)Ub <= mn) return 0;
-    return 1;
+/* The reference's maxactdelta of a row: the sequential EPS-max of
+ * |a|(ub-lb) in row order (src/propagation_methods.cuh:188-190). */
+static double seq_maxactdelta(int row, const int *col, const int *row_ptr, const double *val, const double *lb,
+                              const double *ub) {
+    double m = 0.0;
+    for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
+        const double d = fabs(val[k]) * (ub[col[k]] - lb[col[k]]);
+        if (eps_gt(d, m)) m = d;
+    }
+    return m;
 }
 
 static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, const double *lb, const double *ub,
                       const int *vartype, double *lb_out, double *ub_out,
-                      unsigned char *var_changed, int *go);
+                      unsigned char *var_changed, int *go, int *infeas);
 
-/* Rows up to thread_row_max non-zeros: the GPU's FP32 bound only pre-filters,
- * an exact second pass takes the reference's decision, so these rows follow
- * the reference exactly (jacobi_row). Longer rows: warp tiles + U rule. */
+/* Rows up to thread_row_max non-zeros follow the reference exactly
+ * (jacobi_row). Longer rows: the kernels' summation order, the reference's
+ * row test and candidates. */
 static int jacobi_row_gpu(int row, const int *col, const int *row_ptr, const double *val, const double *lhs,
                           const double *rhs, const double *lb, const double *ub, const int *vartype,
                           double *lb_out, double *ub_out, unsigned char *var_changed, int thread_row_max,
-                          int tile, int *go) {
+                          int tile, int *go, int *infeas) {
     if (row_ptr[row + 1] - row_ptr[row] <= thread_row_max)
-        return jacobi_row(row, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, var_changed, go);
+        return jacobi_row(row, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, var_changed, go,
+                          infeas);
     const gacc a = gpu_row_acts(row, col, row_ptr, val, lb, ub, thread_row_max, tile);
-    *go = gdpo_gpu_row_go(a.minact, a.maxact, a.minf, a.maxf, a.U, lhs[row], rhs[row]);
+    *infeas = gdpo_row_infeasible(a.minact, a.maxact, a.minf, a.maxf, lhs[row], rhs[row]);
+    *go = gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minf, a.maxf, lhs[row], rhs[row],
+                                     seq_maxactdelta(row, col, row_ptr, val, lb, ub));
     if (!*go) return 0;
     int any = 0;
     for (int k = row_ptr[row]; k < row_ptr[row + 1]; k++) {
@@ -372,9 +350,10 @@ static inline void atomic_min_d(double *addr, double v) {
 static int jacobi_row(int row, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, const double *lb, const double *ub,
                       const int *vartype, double *lb_out, double *ub_out,
-                      unsigned char *var_changed, int *go) {
+                      unsigned char *var_changed, int *go, int *infeas) {
     const gdpo_acts a = gdpo_activities(row, col, row_ptr, val, lb, ub);
     int any = 0;
+    *infeas = gdpo_row_infeasible(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[row], rhs[row]);
     *go = gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[row], rhs[row],
                                      a.maxactdelta);
     if (!*go) return 0;
@@ -405,8 +384,9 @@ int gdpo_jacobi_round(int m, int n, const int *col, const int *row_ptr, const do
 #endif
     for (int i = 0; i < m; i++) {
         if (mark && !mark[i]) continue;
-        int go;
-        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL, &go);
+        int go, infeas;
+        const int t = jacobi_row(i, col, row_ptr, val, lhs, rhs, lb, ub, vartype, lb_out, ub_out, NULL, &go,
+                                 &infeas);
         if (t && tight_row) tight_row[i] = 1;
         change |= t;
     }
@@ -456,6 +436,7 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
     const int gpu_mode = split_tile > 0;
     memset(&r, 0, sizeof(r));
     r.infeasible_var = -1;
+    r.infeasible_row = -1;
     if (max_rounds <= 0) max_rounds = O_MAX_ROUNDS;
     if (m == 0 || n == 0 || nnz == 0) {
         r.converged = 1;
@@ -488,6 +469,7 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
         r.rounds++;
         change = 0;
         long long rows = 0, nz = 0, cands = 0, go_rows = 0;
+        int inf_row = INT_MAX; /* smallest row found infeasible in this round */
         for (int i = 0; i < m; i++)
             if (mark[i]) { rows++; nz += row_ptr[i + 1] - row_ptr[i]; }
         if (schedule == GDPO_SCHED_SEQUENTIAL) {
@@ -495,6 +477,9 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
             for (int i = 0; i < m; i++) {
                 if (!mark[i]) continue;
                 const gdpo_acts a = gdpo_activities(i, col, row_ptr, val, lb, ub);
+                if (inf_row == INT_MAX &&
+                    gdpo_row_infeasible(a.minact, a.maxact, a.minact_inf, a.maxact_inf, lhs[i], rhs[i]))
+                    inf_row = i;
                 if (!gdpo_can_cons_be_tightened(a.minact, a.maxact, a.minact_inf, a.maxact_inf,
                                                 lhs[i], rhs[i], a.maxactdelta))
                     continue;
@@ -515,19 +500,20 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
             memcpy(ub_snap, ub, sizeof(double) * (size_t)n);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads > 0 ? nthreads : 1) \
-        reduction(| : change) reduction(+ : go_rows)
+        reduction(| : change) reduction(+ : go_rows) reduction(min : inf_row)
 #endif
             for (int i = 0; i < m; i++) {
                 if (!mark[i]) continue;
-                int go = 0;
+                int go = 0, infeas = 0;
                 if (gpu_mode) {
                     change |= jacobi_row_gpu(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
-                                             ub, var_changed, split_len, split_tile, &go);
+                                             ub, var_changed, split_len, split_tile, &go, &infeas);
                     if (go && row_ptr[i + 1] - row_ptr[i] <= split_tile) go_rows++;
                 } else {
                     change |= jacobi_row(i, col, row_ptr, val, lhs, rhs, lb_snap, ub_snap, vartype, lb,
-                                         ub, var_changed, &go);
+                                         ub, var_changed, &go, &infeas);
                 }
+                if (infeas && i < inf_row) inf_row = i;
             }
         }
         /* marking for the next round: reference src/propagation_methods.cu:3-13 */
@@ -537,10 +523,14 @@ int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr,
             var_changed[j] = 0;
             if (schedule != GDPO_SCHED_SEQUENTIAL) cands++;
             for (int k = col_ptr[j]; k < col_ptr[j + 1]; k++) mark[row_idx[k]] = 1;
-            if (!r.infeasible && gdpo_var_infeasible(lb[j], ub[j])) {
+            if (r.infeasible_var < 0 && gdpo_var_infeasible(lb[j], ub[j])) {
                 r.infeasible = 1;
                 r.infeasible_var = j;
             }
+        }
+        if (inf_row != INT_MAX) {
+            r.infeasible = 1;
+            r.infeasible_row = inf_row;
         }
         r.rows_processed += rows;
         r.nnz_processed += nz;

@@ -41,6 +41,7 @@ typedef struct {
     long long nnz_processed;  /* their non-zeros */
     long long rows_go;        /* GPU mode: processed rows of at most split_tile non-zeros that passed
                                  their row test (summed over rounds) */
+    int infeasible_row;       /* smallest row found infeasible by the row rule in the last round, or -1 */
 } gdpo_result;
 
 /* --- reference math, one function each (known-answer tests call these) --- */
@@ -61,8 +62,10 @@ void gdpo_tighten_variable(double coeff, double lhs, double rhs, double minact, 
                            int *lb_tightened, double *newlb, int *ub_tightened, double *newub);
 gdpo_acts gdpo_activities(int row, const int *col, const int *row_ptr, const double *val,
                           const double *lb, const double *ub);
-/* infeasibility rule applied after every round (variable crossing) */
+/* infeasibility rules applied in every round: variable crossing (after the
+ * round) and the row rule (every processed row, on the activities it computed) */
 int gdpo_var_infeasible(double lb, double ub);
+int gdpo_row_infeasible(double minact, double maxact, int minf, int maxf, double lhs, double rhs);
 
 /* --- full propagation to a fixpoint ---
  * lb/ub in/out. max_rounds <= 0 means the reference cap (100). nthreads > 1
@@ -75,19 +78,17 @@ int gdpo_propagate(int m, int n, int nnz, const int *col, const int *row_ptr, co
                    const int *vartype, int schedule, int max_rounds, int nthreads,
                    gdpo_result *res);
 
-/* gdpo_propagate in GPU mode when split_tile > 0 (JACOBI schedule): the GB300
- * kernels' row test (FP32 upper bound of max |a|(ub-lb), see gdp_oracle.c)
- * and, for rows longer than split_len (the kernels' thread_row_max), their
- * warp-tile summation order with split_tile non-zeros per tile. split_tile = 0
- * is the reference mode (identical to gdpo_propagate). */
+/* gdpo_propagate in GPU mode when split_tile > 0 (JACOBI schedule): rows
+ * longer than split_len (the kernels' thread_row_max) are summed in the GB300
+ * kernels' lane-group / warp-tile order with split_tile non-zeros per tile
+ * (see gdp_oracle.c); the row test and candidates stay the reference's.
+ * split_tile = 0 is the reference mode (identical to gdpo_propagate). */
 int gdpo_propagate_ex(int m, int n, int nnz, const int *col, const int *row_ptr, const double *val,
                       const double *lhs, const double *rhs, double *lb, double *ub,
                       const int *vartype, int schedule, int max_rounds, int nthreads,
                       int split_len, int split_tile, gdpo_result *res);
 /* lanes per row the GPU mode uses for a row of len non-zeros */
 int gdpo_lanes_per_row(int len, int thread_row_max, int tile);
-/* the GPU mode's row test */
-int gdpo_gpu_row_go(double minact, double maxact, int minf, int maxf, float U, double lhs, double rhs);
 
 /* One JACOBI round on a snapshot, restricted to rows with mark[row] != 0
  * (mark == NULL: every row). Writes candidates into lb_out/ub_out (which must

@@ -11,9 +11,11 @@
  * (src/propagators/sequential_propagator.h:241-278,
  *  src/propagators/OMP_propagator.h:168-211) around the reference's
  * sequentialPropagationRound<double> / OMPPropagationRound<double> with a
- * configurable round cap, the project's infeasibility rule after each round
- * (untimed) and wall-clock timing of the round calls only, which is where the
- * reference places its own timers.
+ * configurable round cap, the project's infeasibility rules after each round
+ * (untimed: variable crossing, and the row rule on the activities the round
+ * function left in minacts/maxacts for every row it processed) and wall-clock
+ * timing of the round calls only, which is where the reference places its own
+ * timers.
  */
 #include "propagators/sequential_propagator.h"
 #include "propagators/OMP_propagator.h"
@@ -27,6 +29,22 @@ bool var_infeasible(double lb, double ub) {
     double s = std::fabs(lb) > std::fabs(ub) ? std::fabs(lb) : std::fabs(ub);
     if (s < 1.0) s = 1.0;
     return (lb - ub) > 1e-6 * s;
+}
+
+/* The row rule: the reference's isConsInfeasible on a side with a finite
+ * constraint side and no infinite contribution, relative tolerance 1e-6. */
+bool row_infeasible(double minact, double maxact, int minf, int maxf, double lhs, double rhs) {
+    if (minf == 0 && !ISPOSINF(rhs)) {
+        double s = std::fabs(minact) > std::fabs(rhs) ? std::fabs(minact) : std::fabs(rhs);
+        if (s < 1.0) s = 1.0;
+        if (minact - rhs > 1e-6 * s) return true;
+    }
+    if (maxf == 0 && !ISNEGINF(lhs)) {
+        double s = std::fabs(maxact) > std::fabs(lhs) ? std::fabs(maxact) : std::fabs(lhs);
+        if (s < 1.0) s = 1.0;
+        if (lhs - maxact > 1e-6 * s) return true;
+    }
+    return false;
 }
 
 /* CSC pattern by counting sort (the reference uses cuSPARSE for this). */
@@ -74,10 +92,12 @@ int gdpref_propagate(int m, int n, int nnz, const int *col, const int *row_ptr, 
     int round = 0;
     double seconds = 0.0;
     std::vector<double> lb_before(n), ub_before(n);
+    std::vector<int> marked_before(m);
     while (round < max_rounds && change_found && !infeasible) {
         round++;
         std::copy(lb, lb + n, lb_before.begin());
         std::copy(ub, ub + n, ub_before.begin());
+        std::copy(consmarked.begin(), consmarked.end(), marked_before.begin());
         auto t0 = std::chrono::steady_clock::now();
         if (schedule == 0) {
             change_found = OMPPropagationRound<double>(
@@ -95,6 +115,10 @@ int gdpref_propagate(int m, int n, int nnz, const int *col, const int *row_ptr, 
         seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         for (int j = 0; j < n && !infeasible; j++)
             if ((lb[j] != lb_before[j] || ub[j] != ub_before[j]) && var_infeasible(lb[j], ub[j]))
+                infeasible = true;
+        for (int i = 0; i < m && !infeasible; i++)
+            if (marked_before[i] &&
+                row_infeasible(minacts[i], maxacts[i], minacts_inf[i], maxacts_inf[i], lhs[i], rhs[i]))
                 infeasible = true;
     }
     for (auto &l : locks) omp_destroy_lock(&l);

@@ -82,3 +82,32 @@ def permute(mip: MIP, row_perm: np.ndarray | None = None, col_perm: np.ndarray |
     return MIP(row_ptr, np.concatenate(cols).astype(np.int32) if cols else np.zeros(0, np.int32),
                np.concatenate(vals) if vals else np.zeros(0), mip.lhs[rp].copy(), mip.rhs[rp].copy(),
                mip.lb[cp].copy(), mip.ub[cp].copy(), mip.vartype[cp].copy())
+
+
+def row_infeasible_mip() -> MIP:
+    """x1 + x2 >= 1e-3 with x1 fixed at 1e4 and x2 at -1e4 (continuous): the
+    row's maximum activity 0 is below its lhs (a row the row rule flags: 1e-3 >
+    1e-6 * max(1, 0, 1e-3)), while the candidates move each bound by 1e-3 only,
+    within the variable rule's tolerance 1e-6 * 1e4 -- no variable crosses."""
+    return MIP(np.array([0, 2], np.int32), np.array([0, 1], np.int32), np.array([1.0, 1.0]),
+               np.array([1e-3]), np.array([1e20]), np.array([1e4, -1e4]), np.array([1e4, -1e4]),
+               np.array([3, 3], np.int32))
+
+
+def eps_band_mip(length: int = 64, blocker: bool = True, p: int | None = None, q: int | None = None) -> MIP:
+    """One row sum_k x_k <= 1 over continuous x_k in [0, u_k] (lhs = -inf), so
+    its slack is 1 and d_k = u_k. Every u_k is 0.5 except u_p = 1 + 1.5e-9,
+    the row's maximum d, which exceeds the slack by 1.5e-9 -- inside the
+    (EPS, 2.00001e-9] band where only the reference's sequential EPS-max
+    decides the row test. With `blocker`, an earlier u_q = 1 + 0.7e-9 becomes
+    that EPS-max and u_p never replaces it (it exceeds it by 0.8e-9 <= EPS):
+    the reference skips the row. Without it the EPS-max is u_p, the row is
+    processed and u_p tightens to 1."""
+    p = length - 5 if p is None else p
+    q = 3 if q is None else q
+    u = np.full(length, 0.5)
+    u[p] = 1.0 + 1.5e-9
+    if blocker:
+        u[q] = 1.0 + 0.7e-9
+    return MIP(np.array([0, length], np.int32), np.arange(length, dtype=np.int32), np.ones(length),
+               np.array([-1e20]), np.array([1.0]), np.zeros(length), u, np.full(length, 3, np.int32))

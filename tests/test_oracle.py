@@ -207,3 +207,52 @@ def test_infeasible_chain_detected_like_reference():
     ref = oracle.ref_propagate(mip, oracle.SEQUENTIAL, max_rounds=2000)
     assert r.infeasible and ref.infeasible and r.rounds == ref.rounds
     assert oracle.propagate(mip, oracle.JACOBI, max_rounds=2000).infeasible
+
+
+# ---- the row rule and the EPS band of the row test -------------------------
+def test_row_rule_flags_infeasible_row():
+    """A row whose activities exclude its sides is infeasible even when no
+    variable crosses beyond the variable rule's tolerance (both schedules,
+    GPU mode, and the reference harness applying the same rule to the
+    activities its own round functions computed)."""
+    from gdp_testutil import row_infeasible_mip
+    mip = row_infeasible_mip()
+    for kw in (dict(schedule=oracle.JACOBI), dict(schedule=oracle.SEQUENTIAL),
+               dict(schedule=oracle.JACOBI, split_len=1, split_tile=1)):
+        r = oracle.propagate(mip, **kw)
+        assert r.infeasible and r.rounds == 1, kw
+        assert r.infeasible_row == 0 and r.infeasible_var == -1, kw
+    o = oracle.lib()
+    assert o.gdpo_row_infeasible(0.0, 0.0, 0, 0, 1e-3, 1e20)
+    assert not o.gdpo_row_infeasible(0.0, 0.0, 0, 1, 1e-3, 1e20)  # an infinite contribution: no verdict
+    assert not o.gdpo_row_infeasible(0.0, 0.0, 0, 0, 5e-7, 1e20)  # within the tolerance
+    assert o.gdpo_row_infeasible(2.5, 9.0, 0, 0, -1e20, 2.0)
+    if oracle.ref_available():
+        for schedule in (oracle.JACOBI, oracle.SEQUENTIAL):
+            r = oracle.ref_propagate(mip, schedule)
+            assert r.infeasible and r.rounds == 1
+
+
+@pytest.mark.parametrize("blocker", [True, False])
+def test_eps_band_row_test(blocker):
+    """The reference's sequential EPS-max decides the row test when the row's
+    maximum |a|(ub-lb) exceeds the slack by EPS to 2 EPS: with an earlier
+    element within EPS below the maximum the row is skipped, without it the
+    maximum's variable tightens. The GPU mode (rows summed in lane groups or
+    warp tiles) decides like the reference."""
+    from gdp_testutil import eps_band_mip
+    for length, trm, tile in ((64, 32, 1024), (3000, 32, 1024), (64, 4, 16)):
+        mip = eps_band_mip(length, blocker, q=3, p=length - 5)
+        ref = oracle.propagate(mip, oracle.JACOBI)
+        gpu_mode = oracle.propagate(mip, oracle.JACOBI, split_len=trm, split_tile=tile)
+        seq = oracle.propagate(mip, oracle.SEQUENTIAL)
+        p = length - 5
+        if blocker:
+            assert ref.rounds == 1 and ref.ub[p] == 1.0 + 1.5e-9
+        else:
+            assert ref.rounds == 2 and ref.ub[p] == 1.0
+        assert_bitexact(gpu_mode.lb, gpu_mode.ub, ref.lb, ref.ub)
+        assert_bitexact(seq.lb, seq.ub, ref.lb, ref.ub)
+        if oracle.ref_available():
+            r = oracle.ref_propagate(mip, oracle.JACOBI)
+            assert_bitexact(r.lb, r.ub, ref.lb, ref.ub)

@@ -17,7 +17,8 @@ import pytest
 
 import gdp
 import gdpgen
-from gdp_testutil import assert_bitexact
+import oracle
+from gdp_testutil import assert_bitexact, row_infeasible_mip
 
 pytestmark = pytest.mark.gpu
 
@@ -61,3 +62,40 @@ def test_noalloc_rejects_more_variables_than_its_scratch():
     n = gdp.NOALLOC_MAX_VARS + 1
     with pytest.raises(gdp.GDPError, match="at most"):
         gdp.propagate_noalloc(1, n, 1, 1, 1, 1, 1, 1, 1, 1, 1)
+
+
+def test_noalloc_long_rows_follow_the_reference_order():
+    """Rows longer than the context path's thread_row_max are still summed
+    left to right by one thread here, with the reference's row test: the
+    result equals the oracle's restatement of the reference's cpu_omp round
+    function bit for bit, on a power-law instance with rows up to 5,000
+    non-zeros."""
+    torch = pytest.importorskip("torch")
+    mip = gdpgen.random_mip(1, seed=303, m=20_000, n=15_000, len_max=2000, dense_len=5000, n_dense_rows=2)
+    assert np.diff(mip.row_ptr).max() > 32
+    lb, ub, st = _noalloc(torch, mip)
+    ref = oracle.propagate(mip, oracle.JACOBI, nthreads=8)
+    assert st["rounds"] == ref.rounds and bool(st["infeasible"]) == ref.infeasible
+    assert_bitexact(lb, ub, ref.lb, ref.ub, what="noalloc vs reference order")
+
+
+def test_noalloc_checks_its_input_before_indexing():
+    """A column index outside [0, n) is reported as an error by the device
+    check that runs before any round reads the CSR; a valid call afterwards
+    works (the shared working array is re-initialized)."""
+    torch = pytest.importorskip("torch")
+    mip = gdpgen.random_mip(0, seed=304)
+    bad = gdp.MIP(mip.row_ptr, mip.col.copy(), mip.val, mip.lhs, mip.rhs, mip.lb, mip.ub, mip.vartype)
+    bad.col[5] = mip.n + 7
+    with pytest.raises(gdp.GDPError, match="column index out of range at non-zero 5"):
+        _noalloc(torch, bad)
+    lb, ub, st = _noalloc(torch, mip)
+    rlb, rub, rst = gdp.propagate(mip, sync_type=gdp.CPU_LOOP)
+    assert st["rounds"] == rst["rounds"]
+    assert_bitexact(lb, ub, rlb, rub, what="noalloc after a rejected call")
+
+
+def test_noalloc_flags_an_infeasible_row():
+    torch = pytest.importorskip("torch")
+    lb, ub, st = _noalloc(torch, row_infeasible_mip())
+    assert st["infeasible"] == 1 and st["infeasible_row"] == 0 and st["infeasible_var"] == -1
