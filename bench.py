@@ -12,16 +12,35 @@ fixpoint (or the 100-round cap) with device-resident data: one persistent
 megakernel launch. `value` is ms per step; `e2e` is the same propagation
 through the reference-facing C call propagateConstraintsGPUAtomicDouble with
 host buffers (upload, layout, propagation and download inside the timed
-region). `--impl reference` times the reference's CPU algorithm (the oracle
-port of cpu_omp: Jacobi rounds on every host core) on the same instance.
+region).
+
+After the timed region, untimed:
+  * cpu_baseline: the oracle's restatements of the reference's cpu_seq (one
+    thread) and cpu_omp (8 threads, the reference's SHARED_MEM_THREADS, and
+    every host core) run to the fixpoint on the same instance, median of up
+    to 3 runs each within --cpu-budget-s;
+  * parity: the GPU's fixpoint against those runs (round counts, verdicts,
+    integer-bound mismatches, continuous deviations), and against cpu_seq on
+    the same generator without equality rows;
+  * workloads: the batched and learned workloads (branch-and-bound nodes,
+    heterogeneous instances, learned covering/knapsack marking, chain
+    instances with and without learned marking), each timed against the plain
+    single-problem GPU path on the same members, member results checked.
+
+`--impl reference` times the reference's CPU algorithm (the oracle's
+restatement of cpu_omp, Jacobi rounds on every host core) on the same
+instance: full propagations to the fixpoint, as many as --ref-budget-s allows.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gdp|reference]
 """
 from __future__ import annotations
 
 import argparse
+import copy
+import ctypes as C
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -39,9 +58,10 @@ for _p in (str(ROOT), str(PKG)):
 
 WORKLOAD = ("power-law MIP: m=2,000,000 rows, n=1,500,000 vars, Zipf(1.8) row lengths in [2,20000] "
             "+ 32 rows x 100,000 nnz, coef +-LogUniform[1e-2,1e3], 30% equality rows; seed 1000+rank")
+REF_OMP_THREADS = 8  # the reference's SHARED_MEM_THREADS (src/params.h:13)
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)  # ~0.8 s timed on config 1: several clock samples
@@ -49,26 +69,30 @@ def parse():
     ap.add_argument("--impl", choices=["gdp", "reference"], default="gdp")
     ap.add_argument("--sync", choices=["megakernel", "cpu_loop", "gpu_loop"], default="megakernel")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink m/n (testing only; the bench line is m=2M)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-budget-s", type=float, default=30.0)
+    ap.add_argument("--no-workloads", action="store_true", help="skip the batched / learned sub-results")
+    ap.add_argument("--cpu-budget-s", type=float, default=60.0, help="CPU baseline runs (cpu_seq, cpu_omp)")
+    ap.add_argument("--ref-budget-s", type=float, default=150.0, help="--impl reference: timed propagations")
     ap.add_argument("--max-rounds", type=int, default=0)
     ap.add_argument("--marking", type=int, default=1, help="1: process only rows with a changed variable")
     ap.add_argument("--trm", type=int, default=0, help="thread_row_max (0: library default)")
     ap.add_argument("--tile", type=int, default=0, help="split_tile (0: library default)")
     ap.add_argument("--workload", choices=["plain", "nodes", "instances", "chains", "cover"], default="plain",
-                    help="plain: the power-law MIP (the bench line); nodes / instances / chains: batched "
-                         "workloads timed against per-member plain propagations")
+                    help="plain: the power-law MIP (the bench line); the others: one batched / learned "
+                         "workload alone, timed against per-member plain propagations")
     ap.add_argument("--members", type=int, default=0, help="batch members (0: the workload's default)")
     ap.add_argument("--autotune", action="store_true",
-                    help="plain: pick row bins and loop schedule with gdp_autotune first (untimed)")
+                    help="pick row bins and loop schedule with gdp_autotune first (untimed)")
     ap.add_argument("--train-seeds", type=int, default=200, help="cover: instances traced for training")
     ap.add_argument("--eval-seeds", type=int, default=50, help="cover: held-out instances evaluated")
     ap.add_argument("--train-scale", type=float, default=0.1, help="cover: size of the traced instances")
     ap.add_argument("--learned", action="store_true",
                     help="instances / chains: learned row marking in the batch (MLP trained on the GPU on "
                          "traces of smaller instances of the same generator), timed beside the exact-marking batch")
-    return ap.parse_args()
+    ap.add_argument("--full-sweep-baseline", action="store_true",
+                    help="batched workloads: also time the members one by one with full sweeps every round")
+    return ap.parse_args(argv)
 
 
 def dist_init(args):
@@ -78,7 +102,8 @@ def dist_init(args):
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if args.impl == "gdp":
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if args.impl == "gdp" else "gloo")
     return ws, rank, local
 
@@ -99,7 +124,7 @@ def max_over_ranks(ws, x: float) -> float:
     return float(t.item())
 
 
-def make_instance(args, rank):
+def make_instance(args, rank, **overrides):
     import gdpgen
     m = int(2_000_000 * args.scale)
     n = int(1_500_000 * args.scale)
@@ -107,8 +132,19 @@ def make_instance(args, rank):
     if args.scale < 1.0:
         kw = dict(len_max=max(16, int(20000 * args.scale)), dense_len=max(32, int(100_000 * args.scale)))
     t0 = time.perf_counter()
-    mip = gdpgen.random_mip(1, seed=1000 + rank, m=m, n=n, **kw)
+    mip = gdpgen.random_mip(1, seed=1000 + rank, m=m, n=n, **kw, **overrides)
     return mip, time.perf_counter() - t0
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip() + f" ({platform.machine()})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.processor() or platform.machine()
 
 
 class Clocks:
@@ -159,68 +195,125 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(mip, gpu_rounds: int, budget_s: float, max_rounds: int):
-    """The oracle port of the reference's cpu_omp (Jacobi rounds, OpenMP on
-    every host core), timed on the same instance. Runs to the fixpoint when a
-    2-round probe projects it within the budget, else reports the projection."""
+# ---- CPU baselines and parity ------------------------------------------------
+def timed_oracle(mip, schedule: int, nthreads: int, budget_s: float, max_runs: int = 3):
+    """Full propagations with the oracle until max_runs or the budget is spent
+    (at least one): (median seconds, runs, first result)."""
+    import oracle
+    times, first = [], None
+    t_start = time.perf_counter()
+    while len(times) < max_runs:
+        r = oracle.propagate(mip, schedule, nthreads=nthreads)
+        times.append(r.seconds)
+        first = first or r
+        if time.perf_counter() - t_start + r.seconds > budget_s:
+            break
+    return statistics.median(times), len(times), first
+
+
+def compare_bounds(lb, ub, ref_lb, ref_ub, vartype) -> dict:
+    """Integer bounds unequal, continuous bounds beyond 1e-9 rel / 1e-12 abs,
+    and the largest continuous deviations, of a fixpoint against a reference."""
+    is_int = np.asarray(vartype) != 3
+    bad_int = bad_cont = 0
+    max_abs = max_rel = 0.0
+    for x, y in ((lb, ref_lb), (ub, ref_ub)):
+        x = np.clip(np.asarray(x, np.float64), -1e20, 1e20)
+        y = np.clip(np.asarray(y, np.float64), -1e20, 1e20)
+        d = np.abs(x - y)
+        bad_int += int(np.count_nonzero(is_int & (x != y)))
+        bad_cont += int(np.count_nonzero((~is_int) & ~(d <= 1e-12 + 1e-9 * np.abs(y))))
+        c = ~is_int & (d > 0)
+        if c.any():
+            max_abs = max(max_abs, float(d[c].max()))
+            max_rel = max(max_rel, float((d[c] / np.maximum(np.abs(y[c]), 1e-300)).max()))
+    return {"int_mismatches": bad_int, "cont_beyond_tol": bad_cont, "cont_max_abs": max_abs,
+            "cont_max_rel": max_rel}
+
+
+def compare(lb, ub, ref, vartype) -> dict:
+    return compare_bounds(lb, ub, ref.lb, ref.ub, vartype)
+
+
+def cpu_reference(mip, budget_s: float):
+    """cpu_seq (1 thread), cpu_omp (8 threads and every host core): timing and results."""
     import oracle
     cores = os.cpu_count() or 1
-    probe_rounds = 2
-    r = oracle.propagate(mip, oracle.JACOBI, max_rounds=probe_rounds, nthreads=cores)
-    per_round = r.seconds / max(1, r.rounds)
-    projected = per_round * max(1, gpu_rounds)
-    if projected <= budget_s:
-        full = oracle.propagate(mip, oracle.JACOBI, max_rounds=max_rounds, nthreads=cores)
-        return {"value": full.seconds * 1e3, "unit": "ms", "cores": cores, "kind": "port",
-                "sample": f"full propagation to fixpoint ({full.rounds} rounds), Jacobi schedule "
-                          f"(the reference's cpu_omp round function), {cores} threads",
-                "rounds": full.rounds}
-    return {"value": projected * 1e3, "unit": "ms", "cores": cores, "kind": "port",
-            "sample": f"first {r.rounds} rounds timed ({r.seconds:.2f} s, all rows marked), "
-                      f"scaled to the GPU's {gpu_rounds} rounds; Jacobi schedule, {cores} threads",
-            "rounds": gpu_rounds}
+    share = budget_s / 3.0
+    seq_s, seq_n, seq = timed_oracle(mip, oracle.SEQUENTIAL, 1, share)
+    omp8_s, omp8_n, omp = timed_oracle(mip, oracle.JACOBI, REF_OMP_THREADS, share)
+    ompa_s, ompa_n, _ = timed_oracle(mip, oracle.JACOBI, cores, share)
+    base = {"value": ompa_s * 1e3, "unit": "ms", "cores": cores, "kind": "port",
+            "sample": f"full propagations to the fixpoint on the bench instance; value = cpu_omp (Jacobi rounds, "
+                      f"the reference's OMPPropagationRound restated by the oracle) on all {cores} host cores, "
+                      f"median of {ompa_n}",
+            "cpu_model": cpu_model(),
+            "cpu_seq": {"ms": seq_s * 1e3, "threads": 1, "runs": seq_n, "rounds": seq.rounds,
+                        "infeasible": seq.infeasible},
+            "cpu_omp_8": {"ms": omp8_s * 1e3, "threads": REF_OMP_THREADS, "runs": omp8_n, "rounds": omp.rounds,
+                          "infeasible": omp.infeasible},
+            "cpu_omp_all": {"ms": ompa_s * 1e3, "threads": cores, "runs": ompa_n}}
+    return base, seq, omp
 
 
+def parity_entry(lb, ub, st, ref, vartype, schedule: str) -> dict:
+    e = {"schedule": schedule, "rounds": {"gpu": int(st["rounds"]), "ref": int(ref.rounds)},
+         "infeasible": {"gpu": bool(st["infeasible"]), "ref": bool(ref.infeasible)}}
+    e.update(compare(lb, ub, ref, vartype))
+    return e
+
+
+# ---- reference arm ------------------------------------------------------------
 def run_reference(args, ws, rank):
+    """The reference's CPU algorithm on every host core: the oracle port of
+    cpu_omp (Jacobi rounds) propagating the bench instance to the fixpoint.
+    Warm-up and timed steps are full propagations; when --steps + --warmup of
+    them would exceed --ref-budget-s, fewer are run and the line says so."""
     if rank != 0:
         return 0
-    mip, _ = make_instance(args, rank)
     import oracle
+    mip, _ = make_instance(args, rank)
     cores = os.cpu_count() or 1
-    times, rounds = [], 0
-    for i in range(args.warmup + args.steps):
-        r = oracle.propagate(mip, oracle.JACOBI, max_rounds=max(2, min(args.max_rounds or 100, 3)),
-                             nthreads=cores)
-        if i >= args.warmup:
-            times.append(r.seconds / max(1, r.rounds))
-        rounds = r.rounds
-    # full-propagation round count (for scaling the per-round sample to ms-to-fixpoint)
+    t0 = time.perf_counter()
     probe = oracle.propagate(mip, oracle.JACOBI, max_rounds=args.max_rounds, nthreads=cores)
-    per_round = statistics.median(times)
-    value = probe.seconds * 1e3
-    line = {"metric": "ms-to-fixpoint", "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+    per = max(probe.seconds, time.perf_counter() - t0)
+    room = max(1, int(args.ref_budget_s / max(per, 1e-3)))
+    warm = max(0, min(args.warmup - 1, room - args.steps))  # the probe counts as one warm-up
+    steps = max(1, min(args.steps, room - warm))
+    for _ in range(warm):
+        oracle.propagate(mip, oracle.JACOBI, max_rounds=args.max_rounds, nthreads=cores)
+    times, rounds = [], probe.rounds
+    for _ in range(steps):
+        r = oracle.propagate(mip, oracle.JACOBI, max_rounds=args.max_rounds, nthreads=cores)
+        times.append(r.seconds * 1e3)
+        rounds = r.rounds
+    value = statistics.median(times)
+    line = {"metric": "ms-to-fixpoint", "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": steps,
+            "warmup": warm + 1, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": probe.rounds,
-                       "parallelism": "replicas"},
+            "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": rounds,
+                       "parallelism": "replicas", "steps_requested": args.steps,
+                       "warmup_requested": args.warmup},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port",
-                             "sample": f"{probe.rounds}-round propagation to fixpoint; median per-round time of "
-                                       f"{args.steps} timed 3-round samples = {per_round * 1e3:.1f} ms; "
-                                       f"Jacobi schedule (reference cpu_omp round function), {cores} threads"},
+                             "cpu_model": cpu_model(),
+                             "sample": f"{steps} timed full propagations to the fixpoint ({rounds} rounds), median; "
+                                       f"Jacobi schedule (the reference's cpu_omp round function restated by the "
+                                       f"oracle), {cores} threads; min {min(times):.0f} ms, max {max(times):.0f} ms"},
             "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
+# ---- batched workloads (configs 2 and 4) -------------------------------------
 BATCH_WORKLOADS = {
-    "nodes": "256 branch-and-bound nodes of one power-law MIP (m=200,000, n=150,000, Zipf(1.8) rows, ~2.4M nnz): "
+    "nodes": "256 branch-and-bound nodes of one power-law MIP (m=200,000, n=150,000, Zipf(1.8) rows, 4.1M nnz): "
              "root fixpoint + k~U{1..50} integer variables fixed to a random in-domain value",
     "instances": "64 power-law MIPs, m log-uniform in [1,000, 500,000], n=0.75m",
-    "chains": "128 chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
-              "[100,000, 1,000,000], 60% integer vars, 15% infinite bounds, 10% made infeasible",
-    "chains_learned": "128 chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
-                      "[100,000, 1,000,000], 60% integer vars, 15% infinite bounds, 10% made infeasible; "
+    "chains": "chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
+              "[100,000, 1,000,000] x scale, 60% integer vars, 15% infinite bounds, 10% made infeasible",
+    "chains_learned": "chain+power-law MIPs (50/50 rows x_{i+1}-x_i<=c_i and Zipf rows), m log-uniform in "
+                      "[100,000, 1,000,000] x scale, 60% integer vars, 15% infinite bounds, 10% made infeasible; "
                       "learned marking (MLP 16-64-64-1, BF16, trained on the GPU on traces of 16 instances "
                       "of one tenth the size) in the one persistent batch launch",
 }
@@ -261,10 +354,13 @@ def _node_bounds(mip, root_lb, root_ub, n_nodes, seed):
     return lbs, ubs
 
 
-def run_batched(args, ws, rank, local):
-    """A batch timed against the same members propagated one by one through the
-    plain single-problem path (full sweeps every round, the reference's
-    schedule) and through the single-problem path with its adaptive marking."""
+def batched_result(args, local) -> dict:
+    """A batch timed against the same members propagated one by one through
+    the plain single-problem GPU path (the library's default options: adaptive
+    marking, megakernel), and optionally with full sweeps every round (the
+    reference's schedule). Members are checked against their single-problem
+    result: bit for bit for exact marking; for learned marking the same
+    verdict, integer bounds bit for bit and the continuous deviation reported."""
     import torch
 
     import gdp
@@ -273,7 +369,7 @@ def run_batched(args, ws, rank, local):
     mip, mips = _batch_members(args)
     gen_s = time.perf_counter() - t0
     # chains of up to 5,000 links take up to that many Jacobi rounds to reach
-    # their fixpoint: the chain workload's default cap lets every member certify
+    # their fixpoint: the chain workload's cap lets every member certify;
     # learned rounds defer rows and so take more rounds: room for them too
     max_rounds = args.max_rounds or (10_000 if args.workload == "chains" else 1_000 if args.learned else 0)
     t0 = time.perf_counter()
@@ -283,7 +379,8 @@ def run_batched(args, ws, rank, local):
         members = _node_bounds(mip, rlb, rub, args.members or 256, seed=5)
         batch = gdp.Batch.nodes(ctx, len(members[0]))
         plain_mips = [mip] * len(members[0])
-        sizes = {"m": mip.m, "n": mip.n, "nnz": mip.nnz, "root_rounds": rst["rounds"]}
+        sizes = {"m": mip.m, "n": mip.n, "nnz": mip.nnz, "root_rounds": rst["rounds"],
+                 "members": len(members[0])}
     else:
         batch = gdp.Batch.instances(mips, autotune=args.autotune, max_rounds=max_rounds)
         members = ([m.lb for m in mips], [m.ub for m in mips])
@@ -294,8 +391,8 @@ def run_batched(args, ws, rank, local):
     learned_info = None
     exact_batch_ms = None
     if args.learned and args.workload != "nodes":
-        import marking
         import gdpgen
+        import marking
         # the exact-marking batch first (same members, same launch), then the model
         for _ in range(args.warmup):
             batch.propagate(*members)
@@ -326,13 +423,15 @@ def run_batched(args, ws, rank, local):
     value = statistics.median(dev_ms)
 
     # plain: every member alone, device-resident bounds, CUDA-event time of its round loop
-    def plain_total(marking):
+    def plain_total(use_marking):
         ctxs = {}
-        total, rounds, agree, n_same = 0.0, [], True, 0
+        total, rounds, n_exact, n_same = 0.0, [], 0, 0
+        worst = {"int_mismatches": 0, "cont_beyond_tol": 0, "cont_max_abs": 0.0, "cont_max_rel": 0.0}
         for k, pm in enumerate(plain_mips):
             key = id(pm)
             if key not in ctxs:
-                ctxs[key] = gdp.Context(pm, sync_type=gdp.MEGAKERNEL, use_marking=marking, max_rounds=max_rounds)
+                ctxs[key] = gdp.Context(pm, sync_type=gdp.MEGAKERNEL, use_marking=use_marking,
+                                        max_rounds=max_rounds)
             c = ctxs[key]
             d_lb = torch.tensor(members[0][k], dtype=torch.float64, device="cuda")
             d_ub = torch.tensor(members[1][k], dtype=torch.float64, device="cuda")
@@ -341,70 +440,80 @@ def run_batched(args, ws, rank, local):
             total += st["device_ms"]
             rounds.append(st["rounds"])
             plb, pub = d_lb.cpu().numpy(), d_ub.cpu().numpy()
-            if learned_info is None:
-                agree &= (st["rounds"] == sts[k]["rounds"] and bool(st["infeasible"]) == bool(sts[k]["infeasible"])
-                          and np.array_equal(plb.view(np.int64), blb[k].view(np.int64))
-                          and np.array_equal(pub.view(np.int64), bub[k].view(np.int64)))
-            else:
-                # learned rounds reach the same certified fixpoint in another
-                # order: the same verdict; integer bounds equal, continuous ones
-                # within 1e-8 relative / 1e-9 absolute (feasible members)
-                same = bool(st["infeasible"]) == bool(sts[k]["infeasible"])
-                if same and not st["infeasible"]:
-                    same = (np.allclose(plb, blb[k], rtol=1e-8, atol=1e-9, equal_nan=True)
-                            and np.allclose(pub, bub[k], rtol=1e-8, atol=1e-9, equal_nan=True))
-                agree &= same
-                n_same += int(same)
+            exact = (st["rounds"] == sts[k]["rounds"] and bool(st["infeasible"]) == bool(sts[k]["infeasible"])
+                     and np.array_equal(plb.view(np.int64), blb[k].view(np.int64))
+                     and np.array_equal(pub.view(np.int64), bub[k].view(np.int64)))
+            n_exact += int(exact)
+            same = bool(st["infeasible"]) == bool(sts[k]["infeasible"])
+            if same and not st["infeasible"]:
+                c = compare_bounds(blb[k], bub[k], plb, pub, plain_mips[k].vartype)
+                same = c["int_mismatches"] == 0 and c["cont_beyond_tol"] == 0
+                for f in ("int_mismatches", "cont_beyond_tol"):
+                    worst[f] += c[f]
+                for f in ("cont_max_abs", "cont_max_rel"):
+                    worst[f] = max(worst[f], c[f])
+            n_same += int(same)
         for c in ctxs.values():
             c.close()
-        return total, rounds, agree, n_same
+        return total, rounds, n_exact, n_same, worst
 
-    plain_full_ms, rounds_full, agree_full, same_full = plain_total(0)
-    plain_adapt_ms, _, agree_adapt, same_adapt = plain_total(1)
-    line = {"metric": "ms-to-fixpoint", "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+    plain_ms, rounds_plain, exact_plain, same_plain, worst_plain = plain_total(1)
+    out = {"workload": BATCH_WORKLOADS[args.workload + ("_learned" if learned_info else "")],
+           "value": value, "unit": "ms", "steps": args.steps, "e2e_ms": statistics.median(e2e_ms),
+           **sizes, "scale": args.scale, "max_rounds": max_rounds or 100,
+           "batch_rounds": tot["rounds"], "infeasible_members": tot["infeasible"],
+           "converged_members": int(sum(bool(s["converged"]) for s in sts)),
+           "rows_processed": tot["rows_processed"], "nnz_processed": tot["nnz_processed"],
+           "nnz_exact": tot["nnz_exact"], "rows_deferred": tot["rows_deferred"], "graph": batch.uses_graph,
+           "autotune": getattr(batch, "tuned", None), "learned": learned_info,
+           "plain_gpu_ms": plain_ms, "plain_gpu_rounds_max": max(rounds_plain),
+           "speedup_vs_plain_gpu": plain_ms / value,
+           "members_bitexact_with_plain": f"{exact_plain}/{len(plain_mips)}",
+           "members_within_tolerance_of_plain": f"{same_plain}/{len(plain_mips)}",
+           "worst_member_deviation": worst_plain,
+           "h2d_bytes_per_step": int(16 * sum(len(x) for x in members[0])),
+           "d2h_bytes_per_step": int(16 * sum(len(x) for x in members[0])),
+           "gpu_launches": int(tot["kernel_launches"]), "clocks": clk,
+           "setup_s": {"generate": gen_s, "build": build_s}}
+    if exact_batch_ms is not None:
+        out["exact_marking_batch_ms"] = exact_batch_ms
+        out["speedup_vs_exact_marking_batch"] = exact_batch_ms / value
+    if args.full_sweep_baseline:
+        full_ms, rounds_full, exact_full, _, _ = plain_total(0)
+        out["full_sweep_ms"] = full_ms
+        out["speedup_vs_full_sweep"] = full_ms / value
+        out["members_bitexact_with_full_sweep"] = f"{exact_full}/{len(plain_mips)}"
+    batch.close()
+    if args.workload == "nodes":
+        ctx.close()
+    return out
+
+
+def run_batched(args, ws, rank, local):
+    r = batched_result(args, local)
+    line = {"metric": "ms-to-fixpoint", "value": r["value"], "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["value"], "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOADS[args.workload + ("_learned" if learned_info and
-                                                                   args.workload == "chains" else "")],
-                       **sizes, "scale": args.scale,
-                       "max_rounds": max_rounds or 100,
-                       "batch_rounds": tot["rounds"], "infeasible_members": tot["infeasible"],
-                       "converged_members": int(sum(bool(s["converged"]) for s in sts)),
-                       "rows_processed": tot["rows_processed"], "nnz_processed": tot["nnz_processed"],
-                       "nnz_exact": tot["nnz_exact"], "graph": batch.uses_graph, "parallelism": "single",
-                       "autotune": getattr(batch, "tuned", None),
-                       "learned": learned_info, "rows_deferred": tot["rows_deferred"]},
-            "plain": {"full_sweep_ms": plain_full_ms, "adaptive_marking_ms": plain_adapt_ms,
-                      "rounds_max": max(rounds_full), "rounds_sum": int(sum(rounds_full)),
-                      **({"bitexact_full_sweep": bool(agree_full), "bitexact_adaptive": bool(agree_adapt)}
-                         if learned_info is None else
-                         {"same_fixpoint_members_full_sweep": f"{same_full}/{len(plain_mips)}",
-                          "same_fixpoint_members_adaptive": f"{same_adapt}/{len(plain_mips)}"}),
-                      "speedup_vs_full_sweep": plain_full_ms / value,
-                      "speedup_vs_adaptive": plain_adapt_ms / value,
-                      **({} if exact_batch_ms is None else
-                         {"exact_marking_batch_ms": exact_batch_ms,
-                          "speedup_vs_exact_marking_batch": exact_batch_ms / value})},
-            "e2e": {"value": statistics.median(e2e_ms), "unit": "ms",
-                    "h2d_bytes_per_step": int(16 * sum(len(x) for x in members[0])),
-                    "d2h_bytes_per_step": int(16 * sum(len(x) for x in members[0]))},
-            "gpu_launches": int(tot["kernel_launches"]), "clocks": clk,
-            "setup_s": {"generate": gen_s, "build": build_s}}
+            "config": {k: v for k, v in r.items() if k not in ("value", "unit", "clocks", "e2e_ms")},
+            "e2e": {"value": r["e2e_ms"], "unit": "ms", "h2d_bytes_per_step": r["h2d_bytes_per_step"],
+                    "d2h_bytes_per_step": r["d2h_bytes_per_step"]},
+            "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
+# ---- learned marking on covering / knapsack MIPs (config 3) ------------------
 COVER = ("set-covering/knapsack MIPs: 500,000 covering rows (0/1 coefficients, length U{5..60}, rhs>=1) + "
          "50,000 knapsack rows (int coefficients U{1..1000}, capacity 0.3 row sum) over 400,000 binary and "
          "50,000 continuous vars")
 
 
-def run_cover(args, ws, rank, local):
-    """Learned marking on covering/knapsack MIPs: the MLP is trained on the GPU
-    on traces of `train_seeds` instances and evaluated on `eval_seeds` held-out
-    seeds against plain full-sweep propagation (the reference's schedule) and
-    exact marking (the engine without the model)."""
+def cover_result(args, local) -> dict:
+    """The MLP is trained on the GPU on traces of `train_seeds` instances and
+    evaluated on `eval_seeds` held-out seeds against plain full-sweep
+    propagation (the reference's schedule) and the plain GPU path (exact
+    marking: the engine without the model)."""
     import torch
 
     import gdp
@@ -421,7 +530,7 @@ def run_cover(args, ws, rank, local):
     t0 = time.perf_counter()
     model, tau, info = marking.train_marking_model(x, y, epochs=4, batch=8192, seed=1, recall=0.98)
     train_s = time.perf_counter() - t0
-    plain_ms = exact_ms = learned_ms = 0.0
+    ms = {"plain": 0.0, "exact": 0.0, "learned": 0.0}
     agree = 0
     rows = {"plain": 0, "exact": 0, "learned": 0}
     nnz = {"plain": 0, "exact": 0, "learned": 0}
@@ -447,36 +556,80 @@ def run_cover(args, ws, rank, local):
             rows[name] += st["rows_processed"]
             nnz[name] += st["nnz_processed"]
             rounds[name].append(st["rounds"])
-        plain_ms += res["plain"][2]["device_ms"]
-        exact_ms += res["exact"][2]["device_ms"]
-        learned_ms += res["learned"][2]["device_ms"]
+            ms[name] += st["device_ms"]
         agree += int(np.array_equal(res["learned"][0], res["plain"][0]) and
                      np.array_equal(res["learned"][1], res["plain"][1]))
     clk = clocks.stop()
-    line = {"metric": "ms-to-fixpoint", "value": learned_ms, "unit": "ms", "n_gpus": ws, "steps": args.eval_seeds,
-            "warmup": args.warmup, "ms_per_step": learned_ms / max(1, args.eval_seeds), "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": COVER, "scale": sc, "train_seeds": args.train_seeds,
-                       "train_scale": args.train_scale, "eval_seeds": args.eval_seeds,
-                       "train_samples": info["samples"], "positive_rate": info["positive_rate"],
-                       "train_loss": info["loss"], "threshold": tau, "train_recall": info["recall"],
-                       "selected_rate": info["selected_rate"], "trace_s": trace_s, "train_s": train_s,
-                       "rows_processed": rows, "nnz_processed": nnz,
-                       "rounds_mean": {k: float(np.mean(v)) for k, v in rounds.items()},
-                       "parallelism": "single"},
-            "plain": {"full_sweep_ms": plain_ms, "exact_marking_ms": exact_ms,
-                      "speedup_vs_full_sweep": plain_ms / max(learned_ms, 1e-9),
-                      "speedup_vs_exact_marking": exact_ms / max(learned_ms, 1e-9),
-                      "bitexact_with_full_sweep": f"{agree}/{args.eval_seeds}"},
-            "e2e": {"value": float(np.sum(e2e)), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    return {"workload": COVER, "value": ms["learned"], "unit": "ms", "e2e_ms": float(np.sum(e2e)),
+            "scale": sc, "train_seeds": args.train_seeds, "train_scale": args.train_scale,
+            "eval_seeds": args.eval_seeds, "train_samples": info["samples"],
+            "positive_rate": info["positive_rate"], "train_loss": info["loss"], "threshold": tau,
+            "train_recall": info["recall"], "selected_rate": info["selected_rate"], "trace_s": trace_s,
+            "train_s": train_s, "rows_processed": rows, "nnz_processed": nnz,
+            "rounds_mean": {k: float(np.mean(v)) for k, v in rounds.items()},
+            "full_sweep_ms": ms["plain"], "plain_gpu_ms": ms["exact"],
+            "speedup_vs_full_sweep": ms["plain"] / max(ms["learned"], 1e-9),
+            "speedup_vs_plain_gpu": ms["exact"] / max(ms["learned"], 1e-9),
+            "members_bitexact_with_full_sweep": f"{agree}/{args.eval_seeds}",
             "gpu_launches": 2 * args.eval_seeds, "clocks": clk}
+
+
+def run_cover(args, ws, rank, local):
+    r = cover_result(args, local)
+    line = {"metric": "ms-to-fixpoint", "value": r["value"], "unit": "ms", "n_gpus": ws, "steps": args.eval_seeds,
+            "warmup": args.warmup, "ms_per_step": r["value"] / max(1, args.eval_seeds), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {k: v for k, v in r.items() if k not in ("value", "unit", "clocks", "e2e_ms")},
+            "e2e": {"value": r["e2e_ms"], "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": r["gpu_launches"], "clocks": r["clocks"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def main():
-    args = parse()
+def workload_results(args, local) -> dict:
+    """The batched and learned workloads behind the headline line, sized so
+    the default run stays within minutes (sizes and member counts stated in
+    each entry; --workload runs one of them at full size)."""
+    out = {}
+    plans = [
+        ("nodes", dict(workload="nodes", scale=1.0, members=256, learned=False)),
+        ("instances", dict(workload="instances", scale=1.0, members=64, learned=False)),
+        ("cover", dict(workload="cover", scale=1.0, train_seeds=40, eval_seeds=10, train_scale=0.1)),
+        ("chains", dict(workload="chains", scale=0.25, members=32, learned=False)),
+        ("chains_learned", dict(workload="chains", scale=0.25, members=32, learned=True)),
+    ]
+    for name, over in plans:
+        a = copy.copy(args)
+        a.autotune = False
+        a.max_rounds = 0
+        a.full_sweep_baseline = False
+        a.steps = 5
+        a.warmup = 2
+        for k, v in over.items():
+            setattr(a, k, v)
+        t0 = time.perf_counter()
+        try:
+            r = cover_result(a, local) if name == "cover" else batched_result(a, local)
+        except Exception as e:  # report and go on: one workload must not take the headline down
+            r = {"error": f"{type(e).__name__}: {e}"}
+        r["wall_s"] = time.perf_counter() - t0
+        r.pop("clocks", None)
+        out[name] = r
+    # the north star's aggregate: batched (+learned) against the plain GPU path on configs 2-4
+    parts = [out.get(k, {}) for k in ("nodes", "instances", "cover", "chains_learned")]
+    if all("value" in p and "plain_gpu_ms" in p for p in parts):
+        out["aggregate_configs_2_4"] = {
+            "batched_learned_ms": float(sum(p["value"] for p in parts)),
+            "plain_gpu_ms": float(sum(p["plain_gpu_ms"] for p in parts)),
+            "speedup": float(sum(p["plain_gpu_ms"] for p in parts) / sum(p["value"] for p in parts)),
+            "members": "nodes, instances, cover (learned), chains_learned"}
+    return out
+
+
+# ---- the headline: plain propagation of the power-law MIP (config 1) ----------
+def main(argv=None):
+    args = parse(argv)
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
@@ -533,9 +686,11 @@ def main():
     clk = clocks.stop()
     total_ms = ev0.elapsed_time(ev1)
     ms_step = max_over_ranks(ws, total_ms / args.steps)
+    gpu_lb, gpu_ub = d_lb.cpu().numpy(), d_ub.cpu().numpy()  # the fixpoint of the last timed step
+    last = stats[-1]
 
-    rounds = stats[-1]["rounds"]
-    bytes_per_step = stats[-1]["bytes_algorithmic"]
+    rounds = last["rounds"]
+    bytes_per_step = last["bytes_algorithmic"]
     kernel_ms = statistics.median(s["device_ms"] for s in stats)  # megakernel launch duration (events)
     launches = int(sum(s["kernel_launches"] for s in stats))
     peaks = {}
@@ -551,19 +706,28 @@ def main():
     tfile = ROOT / "profiles" / "megakernel_traffic.json"
     if tfile.exists():
         try:
-            tr = json.loads(tfile.read_text())
-            traffic = tr.get("bytes_per_launch")
+            traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
         except (OSError, ValueError):
             traffic = None
 
-    # end to end through the reference-facing C call, host buffers
+    # end to end through the reference-facing C call with host buffers: the
+    # caller's arrays go in, the fixpoint comes back in lbs/ubs
+    lib = gdp.load_library()
+    col, rp, val = np.ascontiguousarray(mip.col, np.int32), np.ascontiguousarray(mip.row_ptr, np.int32), \
+        np.ascontiguousarray(mip.val, np.float64)
+    lhs, rhs, vt = np.ascontiguousarray(mip.lhs), np.ascontiguousarray(mip.rhs), \
+        np.ascontiguousarray(mip.vartype, np.int32)
     e2e_ms = []
     for _ in range(max(1, args.e2e_steps)):
-        lb, ub = list(), list()
+        lbs, ubs = np.array(mip.lb, np.float64), np.array(mip.ub, np.float64)
         t1 = time.perf_counter()
-        lbs, ubs, _ = gdp.propagate(mip, sync_type=sync, max_rounds=args.max_rounds, thread_row_max=args.trm,
-                                    split_tile=args.tile, use_marking=args.marking)
+        rc = lib.propagateConstraintsGPUAtomicDouble(mip.m, mip.n, mip.nnz, gdp._pi(col), gdp._pi(rp),
+                                                     gdp._pd(val), gdp._pd(lhs), gdp._pd(rhs), gdp._pd(lbs),
+                                                     gdp._pd(ubs), gdp._pi(vt), int(sync))
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
+        if rc != gdp.GDP_OKAY:
+            raise RuntimeError(f"propagateConstraintsGPUAtomicDouble failed: {gdp.last_error()}")
+    e2e_same = bool(np.array_equal(lbs, gpu_lb) and np.array_equal(ubs, gpu_ub))
     h2d = (mip.nnz * 12 + (mip.m + 1) * 4 + mip.m * 16 + mip.n * 20)
     d2h = mip.n * 16
 
@@ -571,27 +735,53 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "m": mip.m, "n": mip.n, "nnz": mip.nnz, "rounds": rounds,
-                       "converged": bool(stats[-1]["converged"]), "infeasible": bool(stats[-1]["infeasible"]),
+                       "converged": bool(last["converged"]), "infeasible": bool(last["infeasible"]),
                        "sync": args.sync, "layout": layout, "marking": args.marking,
-                       "rows_processed": stats[-1]["rows_processed"], "nnz_processed": stats[-1]["nnz_processed"], "nnz_exact": stats[-1]["nnz_exact"], "divisions": stats[-1]["divisions"], "rows_exact": stats[-1]["rows_exact"], "rows_go": stats[-1]["rows_go"], "changed_vars": stats[-1]["changed_vars"], "parallelism": "replicas" if ws > 1 else "single",
+                       "rows_processed": last["rows_processed"], "nnz_processed": last["nnz_processed"],
+                       "nnz_exact": last["nnz_exact"], "divisions": last["divisions"],
+                       "rows_exact": last["rows_exact"], "rows_go": last["rows_go"],
+                       "rows_seqmax": last["rows_seqmax"], "changed_vars": last["changed_vars"],
+                       "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (CSR %.0f MB vs 129 MB L2)" % (mip.nnz * 12 / 1e6),
                        "scale": args.scale},
-            "hbm_gbs": achieved, "nnz_per_s": mip.nnz * rounds / (ms_step * 1e-3),
+            "hbm_gbs": achieved, "nnz_per_s": last["nnz_processed"] / (ms_step * 1e-3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "kernel": "k_megakernel", "bytes_per_launch": bytes_per_step,
                          "launch_ms": kernel_ms},
             "e2e": {"value": statistics.median(e2e_ms), "unit": "ms", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "call": "propagateConstraintsGPUAtomicDouble",
+                    "same_fixpoint_as_device_run": e2e_same},
             "gpu_launches": launches, "clocks": clk,
             "setup_s": {"generate": gen_s, "context": ctx_s}}
     if tuned:
         line["config"]["autotune"] = tuned
+    ctx.close()
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(mip, rounds, args.cpu_budget_s, args.max_rounds)
+        import oracle
+        base, seq, omp = cpu_reference(mip, args.cpu_budget_s)
+        line["cpu_baseline"] = base
+        parity = {"vs_cpu_omp": parity_entry(gpu_lb, gpu_ub, last, omp, mip.vartype,
+                                             "Jacobi: the reference's cpu_omp round function (oracle restatement, "
+                                             "left-to-right sums)"),
+                  "vs_cpu_seq": parity_entry(gpu_lb, gpu_ub, last, seq, mip.vartype,
+                                             "Gauss-Seidel: the reference's cpu_seq (oracle restatement)")}
+        # cpu_seq on the same generator without equality rows (rows tight at
+        # the generating point make cpu_seq's result depend on rounding)
+        noeq, _ = make_instance(args, rank, frac_equality=0.0)
+        with gdp.Context(noeq, sync_type=sync, max_rounds=args.max_rounds) as c2:
+            nlb, nub, nst = c2.propagate()
+        nseq = oracle.propagate(noeq, oracle.SEQUENTIAL, max_rounds=args.max_rounds)
+        nomp = oracle.propagate(noeq, oracle.JACOBI, max_rounds=args.max_rounds, nthreads=os.cpu_count() or 1)
+        e = parity_entry(nlb, nub, nst, nseq, noeq.vartype, "Gauss-Seidel (cpu_seq), generator without equality rows")
+        e["cpu_omp_vs_cpu_seq"] = compare(nomp.lb, nomp.ub, nseq, noeq.vartype)
+        e["vs_cpu_omp"] = compare(nlb, nub, nomp, noeq.vartype)
+        parity["no_equality_rows"] = e
+        line["parity"] = parity
+    if rank == 0 and not args.no_workloads:
+        line["workloads"] = workload_results(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                 stats_flush(Pu, mine, lane);  // statistics belong to the item's unit
             }
         }
-        if (!grid_barrier(B.barrier, B.error)) return;
+        if (!grid_barrier(B.barrier, B.error, B.spin_limit)) return;
         // ---- B (plus the resets for round r + 1: its slots were last used in r - 1)
         if (gtid == 0) {
             unsigned *nctr = B.ctr + 4 * (par ^ 1);
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                     push_tile(B.xq, B.tail + 3, B.cap_tiles, B.error, u, t);
                 stats_flush(Pu, mine, lane);
             }
-            if (!grid_barrier(B.barrier, B.error)) return;
+            if (!grid_barrier(B.barrier, B.error, B.spin_limit)) return;
             // ---- C
             const int n_xq = (int)min(*((volatile unsigned *)(B.tail + 3)), B.cap_tiles);
             if (n_xq) {
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                     split_exact(Pu, t, lane, r, &Pu.flags[1 + par].change, &Pu.flags[1 + par].tight, mine);
                     stats_flush(Pu, mine, lane);
                 }
-                if (!grid_barrier(B.barrier, B.error)) return;
+                if (!grid_barrier(B.barrier, B.error, B.spin_limit)) return;
             }
         }
         // ---- F (a row recorded infeasible in round r turns into the unit's
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                 }
             }
         }
-        if (!grid_barrier(B.barrier, B.error)) return;
+        if (!grid_barrier(B.barrier, B.error, B.spin_limit)) return;
         last = r;
         const int nfs = *((volatile int *)B.n_fs);
         const int next = *((volatile int *)(B.fs_prefix + nfs)) +

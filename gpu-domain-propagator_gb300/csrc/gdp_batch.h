@@ -28,6 +28,7 @@ struct BatchDev {
     int *error;
     int *rounds_out;
     int *n_pending;       // learned units that need the next round (learned batches)
+    long long spin_limit; // clock64 cycles one grid-barrier wait may last (the first member's option)
 };
 
 int launch_batch(const BatchDev &B, int grid, const double *lb, const double *ub, double *lb_out,

@@ -168,6 +168,7 @@ GDP_RETCODE Batch::finish_init(int device, int ctas_per_sm) {
     B_.wbase = (const int *)dev(sizeof(int) * (size_t)(n_units + 1));
     B_.total_words = wbase[n_units];
     B_.max_rounds = max_rounds;
+    B_.spin_limit = units_h_[0].spin_limit;
     B_.cap_entries = (unsigned)std::max<long long>(cap_entries, 1);
     B_.entries = (unsigned long long *)dev(sizeof(unsigned long long) * 2 * (size_t)B_.cap_entries);
     B_.cap_tiles = (unsigned)std::max<long long>(cap_tiles, 1);

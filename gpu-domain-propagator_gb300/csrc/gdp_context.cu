@@ -646,6 +646,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.barrier = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 2);
     P.queue = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 8);
     P.max_rounds = opts.max_rounds;
+    P.spin_limit = opts.barrier_wait_kcycles > 0 ? 1000LL * opts.barrier_wait_kcycles : 4000000000LL;
     d_lb = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     d_ub = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.xrow || !P.xctr || !P.mark || !P.bnd || !P.bnd_nxt || !P.bnd32 || !P.chg || !P.flags || !P.barrier || !P.queue ||

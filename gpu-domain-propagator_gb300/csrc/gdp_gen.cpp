@@ -363,7 +363,7 @@ int gdp_gen_cover_knapsack(int n_cover_rows, int n_knap_rows, int n_bin, int n_c
 }
 
 int gdp_gen_chains(int m, int n, int chain_max, double frac_int_vars, double frac_inf_vars,
-                   int make_infeasible, uint64_t seed, gdp_instance *out) {
+                   double frac_equality, int make_infeasible, uint64_t seed, gdp_instance *out) {
     if (m < 4 || n < 4 || chain_max < 1) return -1;
     const int m_chain = m / 2;
     // chains over vars [0, nv_chain): each chain of length L uses L+1 vars and L rows
@@ -387,6 +387,7 @@ int gdp_gen_chains(int m, int n, int chain_max, double frac_int_vars, double fra
     p.n_dense_rows = 0;
     p.frac_int_vars = frac_int_vars;
     p.frac_inf_vars = frac_inf_vars;
+    p.frac_equality = frac_equality;
     p.len_max = std::min(p.len_max, std::max(2, p.n / 4));
     std::vector<int> lens;
     gen_lengths(&p, seed, m_chain, m, p.n, lens);

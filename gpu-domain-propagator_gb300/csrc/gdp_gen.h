@@ -70,11 +70,12 @@ int gdp_gen_cover_knapsack(int n_cover_rows, int n_knap_rows, int n_bin, int n_c
                            uint64_t seed, gdp_instance *out);
 
 /* Chains x_{i+1} - x_i <= c_i (c_i ~ U[0,3], chains up to chain_max long)
- * mixed 50/50 by rows with power-law rows of the large random MIP; when
- * make_infeasible != 0 one chain's end gets a lower bound above what the
- * chain allows, by at least 1. */
+ * mixed 50/50 by rows with power-law rows of the large random MIP (over
+ * other variables; frac_equality of them equality rows, 0.3 in the large
+ * MIP); when make_infeasible != 0 one chain's end gets a lower bound above
+ * what the chain allows, by at least 1. */
 int gdp_gen_chains(int m, int n, int chain_max, double frac_int_vars, double frac_inf_vars,
-                   int make_infeasible, uint64_t seed, gdp_instance *out);
+                   double frac_equality, int make_infeasible, uint64_t seed, gdp_instance *out);
 
 void gdp_gen_free(gdp_instance *inst);
 

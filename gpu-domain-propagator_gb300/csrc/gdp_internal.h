@@ -178,6 +178,7 @@ struct DevProblem {
     unsigned *barrier;     // megakernel grid barrier {count, generation}
     unsigned *queue;       // work counters: [parity * 4 + phase]
     int max_rounds;
+    long long spin_limit;  // clock64 cycles one grid-barrier wait may last (gdp_options.barrier_wait_kcycles)
 };
 
 constexpr int kWarpsPerCta = 8;

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel_learned(DevProble
             const bool full = kind == kRoundFull;
             learned_activity_phase(P, round, kind, q + 0, change, tight, mine, L, lane,
                                    &P.flags[1 + par].rows_deferred);
-            if (!grid_barrier(P.barrier, err)) return;
+            if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 P.flags[1 + (par ^ 1)].change = 0;
                 P.flags[1 + (par ^ 1)].tight = 0u;
@@ -115,10 +115,10 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel_learned(DevProble
             }
             if (P.n_mtiles) {
                 candidate_phase(P, round, !full, q + 1, exact, mine, lane);
-                if (!grid_barrier(P.barrier, err)) return;
+                if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
                 if (*((volatile int *)exact)) {
                     exact_phase(P, round, q + 2, change, tight, mine, lane);
-                    if (!grid_barrier(P.barrier, err)) return;
+                    if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
                 }
             }
             const unsigned t = *((volatile unsigned *)tight);
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel_learned(DevProble
             learned_finalize(P, round, !certified && next != kRoundFull && round < P.max_rounds,
                              blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
             if (blockIdx.x == 0 && threadIdx.x == 0) P.flags[0].rounds = round;
-            if (!grid_barrier(P.barrier, err)) return;
+            if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
             last_change = *((volatile int *)change);
             const int infeasible = *((volatile int *)&P.flags[0].infeasible);
             if (certified || infeasible) break;

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
             int *exact = &P.flags[1 + par].exact;
             unsigned *q = P.queue + 4 * par;
             activity_phase(P, round, marked, q + 0, change, tight, mine, lane, par);
-            if (!grid_barrier(P.barrier, err)) return;
+            if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 P.flags[1 + (par ^ 1)].change = 0;
                 P.flags[1 + (par ^ 1)].tight = 0u;
@@ -145,16 +145,16 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
             if (xrows || P.n_mtiles) {
                 if (xrows) exact_rows_phase(P, par, change, tight, mine, lane);
                 if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, mine, lane);
-                if (!grid_barrier(P.barrier, err)) return;
+                if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
                 if (P.n_mtiles && *((volatile int *)exact)) {
                     exact_phase(P, round, q + 2, change, tight, mine, lane);
-                    if (!grid_barrier(P.barrier, err)) return;
+                    if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
                 }
             }
             marked = next_round_marked(P, *((volatile unsigned *)tight));
             finalize_words(P, round, marked, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
             if (blockIdx.x == 0 && threadIdx.x == 0) P.flags[0].rounds = round;
-            if (!grid_barrier(P.barrier, err)) return;
+            if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
             last_change = *((volatile int *)change);
             const int infeasible = *((volatile int *)&P.flags[0].infeasible);
             if (!last_change || infeasible) break;

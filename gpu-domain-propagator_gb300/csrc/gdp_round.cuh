@@ -1161,10 +1161,10 @@ __device__ __forceinline__ bool next_round_marked(const DevProblem &P, unsigned 
 
 // Grid barrier with a bounded wait: thread 0 of each CTA reads the barrier
 // generation, arrives, and spins until the generation moves. Any CTA that
-// waits longer than kSpinLimitCycles (or sees another CTA's error) records
-// kErrBarrierTimeout and every CTA leaves the round loop at its next barrier.
-constexpr long long kSpinLimitCycles = 4000000000LL;  // about 2 s at 2 GHz
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *error) {
+// waits longer than `limit` clock64 cycles (or sees another CTA's error)
+// records kErrBarrierTimeout and every CTA leaves the round loop at its next
+// barrier. The default limit is 4e9 cycles, about 2 s at 2 GHz.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *error, long long limit) {
     __syncthreads();
     int ok = 1;
     if (threadIdx.x == 0) {
@@ -1180,7 +1180,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *error) {
             const long long t0 = clock64();
             while (*vgen == my_gen) {
                 if (*((volatile int *)error) != kErrNone) { ok = 0; break; }
-                if (clock64() - t0 > kSpinLimitCycles) {
+                if (clock64() - t0 > limit) {
                     atomicExch(error, (int)kErrBarrierTimeout);
                     ok = 0;
                     break;

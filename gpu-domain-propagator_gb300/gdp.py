@@ -57,7 +57,8 @@ class Options(C.Structure):
         ("device", C.c_int),
         ("use_marking", C.c_int),
         ("ctas_per_sm", C.c_int),
-        ("reserved", C.c_int * 6),
+        ("barrier_wait_kcycles", C.c_int),
+        ("reserved", C.c_int * 5),
     ]
 
 
@@ -262,12 +263,13 @@ class Context:
     """Persistent device context: upload once, propagate many bound vectors."""
 
     def __init__(self, mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
-                 split_tile: int = 0, use_marking: int = -1, ctas_per_sm: int = 0):
+                 split_tile: int = 0, use_marking: int = -1, ctas_per_sm: int = 0, barrier_wait_kcycles: int = 0):
         self._lib = load_library()
         self.mip = mip.normalized()
         p = self.mip
         o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
-                            split_tile=split_tile, use_marking=use_marking, ctas_per_sm=ctas_per_sm)
+                            split_tile=split_tile, use_marking=use_marking, ctas_per_sm=ctas_per_sm,
+                            barrier_wait_kcycles=barrier_wait_kcycles)
         h = C.c_void_p()
         rc = self._lib.gdp_context_create(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val),
                                           _pd(p.lhs), _pd(p.rhs), _pi(p.vartype), C.byref(o), C.byref(h))

@@ -48,8 +48,8 @@ def _lib():
         g.gdp_gen_default_params.argtypes = [C.c_int, C.POINTER(GenParams)]
         g.gdp_gen_random_mip.argtypes = [C.POINTER(GenParams), C.POINTER(_Instance)]
         g.gdp_gen_cover_knapsack.argtypes = [C.c_int] * 8 + [C.c_uint64, C.POINTER(_Instance)]
-        g.gdp_gen_chains.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_uint64,
-                                     C.POINTER(_Instance)]
+        g.gdp_gen_chains.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                     C.c_uint64, C.POINTER(_Instance)]
         g.gdp_gen_free.argtypes = [C.POINTER(_Instance)]
         for f in ("gdp_gen_default_params", "gdp_gen_random_mip", "gdp_gen_cover_knapsack", "gdp_gen_chains"):
             getattr(g, f).restype = C.c_int
@@ -113,11 +113,19 @@ def cover_knapsack(n_cover_rows: int = 500_000, n_knap_rows: int = 50_000, n_bin
 
 
 def chains(m: int, n: int | None = None, chain_max: int = 5000, frac_int_vars: float = 0.6,
-           frac_inf_vars: float = 0.15, infeasible: bool = False, seed: int = 0, with_x0: bool = False):
+           frac_inf_vars: float = 0.15, infeasible: bool = False, seed: int = 0, with_x0: bool = False,
+           frac_equality: float = 0.0):
+    """Chain rows x_{i+1} - x_i <= c_i mixed 50/50 with power-law rows of the
+    large random MIP. The power-law rows have no equality rows by default:
+    equality rows tight at the generating point make the verdict depend on
+    rounding (the reference's cpu_seq declares every such instance
+    infeasible within a few rounds, Jacobi rounds about half of them), while
+    without them exactly the members built infeasible (`infeasible`) are
+    infeasible under both schedules."""
     n = int(0.75 * m) if n is None else n
     inst = _Instance()
     rc = _lib().gdp_gen_chains(int(m), int(n), int(chain_max), float(frac_int_vars), float(frac_inf_vars),
-                               int(bool(infeasible)), int(seed), C.byref(inst))
+                               float(frac_equality), int(bool(infeasible)), int(seed), C.byref(inst))
     if rc != 0:
         raise RuntimeError(f"gdp_gen_chains failed ({rc})")
     return _take(inst, with_x0)

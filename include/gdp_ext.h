@@ -41,7 +41,12 @@ typedef struct {
                              2: every round after the first is marked */
     int ctas_per_sm;      /* resident CTAs per SM of the persistent round loop and of the phase
                              kernels; 0 (default) = as many as fit */
-    int reserved[6];      /* must be zero */
+    int barrier_wait_kcycles; /* limit of one grid-barrier wait of the persistent loops (MEGAKERNEL,
+                             learned marking, batches), in thousands of SM clock cycles; a CTA that
+                             waits longer records a device error, every CTA leaves at its next
+                             barrier and the call returns GDP_ERROR. 0 (default) = 4,000,000
+                             (about 2 s at 2 GHz) */
+    int reserved[5];      /* must be zero */
 } gdp_options;
 
 typedef struct {

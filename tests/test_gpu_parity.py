@@ -507,3 +507,21 @@ def test_power_law_vs_reference_semantics():
     ri, rc = _deviation(omp.lb, omp.ub, seq.lb, seq.ub, noeq.vartype)
     assert bi.sum() == 0
     assert not np.any(bc & ~rc), "the GPU differs from cpu_seq where cpu_omp does not"
+
+
+def test_barrier_wait_limit_returns_error_and_library_stays_usable():
+    """A grid-barrier wait that runs out records a device error instead of
+    waiting on: with a limit of 1,000 SM cycles (the first barrier of a round
+    waits for the slowest CTA's phase work, tens of thousands of cycles on
+    this instance) the first CTAs to arrive give up, every CTA leaves at its
+    next barrier, and the call returns GDP_ERROR with the timeout message.
+    The library stays usable: a fresh context then propagates correctly."""
+    mip = gdpgen.random_mip(1, seed=7, m=40_000, n=30_000, len_max=2000, dense_len=5000, n_dense_rows=2)
+    with gdp.Context(mip, sync_type=gdp.MEGAKERNEL, barrier_wait_kcycles=1) as ctx:
+        with pytest.raises(gdp.GDPError, match="grid barrier wait exceeded its limit"):
+            ctx.propagate()
+    ref = oracle.propagate(mip, oracle.JACOBI, split_len=TRM, split_tile=TILE, nthreads=8)
+    with gdp.Context(mip, sync_type=gdp.MEGAKERNEL) as ctx:
+        lb, ub, st = ctx.propagate()
+    assert st["rounds"] == ref.rounds and st["device_error"] == 0
+    assert_bitexact(lb, ub, ref.lb, ref.ub)

@@ -1,8 +1,11 @@
 """MPS reader: every section and bound type on a small hand-written model, a
-round trip through a writer on generated MIPs, and (where the reference's
-sources are mounted) its MPS test instances parsed and propagated by the oracle
-against the reference's own cpu_seq round function."""
+round trip through a writer on generated MIPs (propagated on the GPU as well),
+and, where the reference's sources are available, its MPS test instances
+parsed and propagated by the oracle against the reference's own cpu_seq round
+function. The reference's directory comes from GDP_REFERENCE_DIR, or from the
+note oracle/Makefile's reference-harness recipe leaves in oracle/_ref."""
 import gzip
+import os
 from pathlib import Path
 
 import numpy as np
@@ -145,7 +148,36 @@ def test_errors():
         gdp.parse_mps(b"ROWS\n L R1\nCOLUMNS\n X1 R9 1.0\nENDATA\n")
 
 
-REF_DATA = Path("/root/reference/fileReader/test_data")
+def _reference_dir():
+    d = os.environ.get("GDP_REFERENCE_DIR")
+    note = Path(oracle.__file__).resolve().parent / "_ref" / "refdir.txt"
+    if not d and note.exists():
+        d = note.read_text().strip()
+    return Path(d) if d else None
+
+
+REF_DATA = (_reference_dir() or Path("reference-not-available")) / "fileReader" / "test_data"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_parsed_mps_propagates_on_gpu(seed):
+    """MPS text of generated MIPs (power-law rows, integer and infinite
+    bounds), parsed by gdp_mps_parse and propagated by the CUDA path with the
+    library defaults: bit for bit the oracle's GPU-mode result on the parsed
+    problem, and within the contract's tolerance of the reference's cpu_omp
+    round function on it."""
+    mip = gdpgen.random_mip(1, seed=seed, m=20_000, n=15_000, len_max=2000, dense_len=5000, n_dense_rows=2)
+    p = gdp.parse_mps(_write_mps(mip))
+    lb, ub, st = gdp.propagate(p, sync_type=gdp.MEGAKERNEL)
+    ref = oracle.propagate(p, oracle.JACOBI, split_len=32, split_tile=1024, nthreads=8)
+    assert st["rounds"] == ref.rounds and bool(st["infeasible"]) == ref.infeasible
+    np.testing.assert_array_equal(np.clip(lb, -1e20, 1e20), np.clip(ref.lb, -1e20, 1e20))
+    np.testing.assert_array_equal(np.clip(ub, -1e20, 1e20), np.clip(ref.ub, -1e20, 1e20))
+    omp = oracle.propagate(p, oracle.JACOBI, nthreads=8)
+    assert omp.rounds == st["rounds"]
+    from gdp_testutil import assert_bounds_close
+    assert_bounds_close(lb, ub, omp.lb, omp.ub, p.vartype)
 
 
 @pytest.mark.skipif(not REF_DATA.exists(), reason="reference test data not mounted")
