@@ -353,7 +353,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
                 hist[(size_t)t * W + L] = acc;
                 acc += c;
             }
-            x_elems += (long long)(acc - len_start[L]) * L;
+            x_elems += (long long)(acc - len_start[L]) * ((L + 3) & ~3);  // rows start on 4-element boundaries
         }
         for (int t = 0; t < nt; t++) nsplit[t + 1] += nsplit[t];
         sell_rows.resize(acc);
@@ -540,6 +540,9 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         GDP_CUDA(cudaMemsetAsync(sc, 0, sizeof(int) * n_sell, stream));  // padding slots
         GDP_CUDA(cudaMemsetAsync(sv, 0, sizeof(double) * n_sell, stream));
         GDP_CUDA(cudaMemsetAsync(sa, 0, sizeof(float) * n_sell, stream));
+        GDP_CUDA(cudaMemsetAsync(xc, 0, sizeof(int) * n_x, stream));  // row padding of the copy
+        GDP_CUDA(cudaMemsetAsync(xv, 0, sizeof(double) * n_x, stream));
+        GDP_CUDA(cudaMemsetAsync(xa, 0, sizeof(float) * n_x, stream));
         Arena tmp;  // the row maps, freed when the build is done
         int *dord = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
         int *dspl = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));

@@ -15,7 +15,9 @@
 //    changed in the round.
 //  * a row-contiguous copy of the SELL rows (xcol, xval): the deferred exact
 //    pass reads rows that came from many slices, one row per lane (or group),
-//    so it wants each row's elements next to each other.
+//    so it wants each row's elements next to each other; every row starts on
+//    a 4-element boundary (zero padding), so a lane reads 4 columns or 2
+//    coefficients with one 16-byte load.
 //  * FP32 screen copies of the coefficients (sell_a32, la32) and of the
 //    current bounds (bnd32): the screen streams 8 B per non-zero and gathers
 //    8 B per bound pair; the FP64 arrays are read only by the exact pass.

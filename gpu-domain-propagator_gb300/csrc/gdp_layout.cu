@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256) k_build_positions(LayoutBuild L) {
         L.srow_len_out[p] = len;
         L.srow_lhs_out[p] = L.lhs[i];
         L.srow_rhs_out[p] = L.rhs[i];
-        L.xptr_out[p] = (int)(L.len_base[len] + (long long)(p - L.len_start[len]) * len);
+        L.xptr_out[p] = (int)(L.len_base[len] + (long long)(p - L.len_start[len]) * ((len + 3) & ~3));
     }
     for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < L.n_slices; sl += stride)
         for (int p = L.slice_row0[sl]; p < L.slice_row0[sl + 1]; p++) L.pos_slice_out[p] = sl;

@@ -80,13 +80,19 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         lhs = __ldg(P.srow_lhs + r);
         rhs = __ldg(P.srow_rhs + r);
     }
-    // features (trace rounds and learned marked rounds)
+    // features (trace rounds: every marked row; learned rounds: the rows the
+    // model decides for -- marked, at least learn_min_len long and younger
+    // than the deferral cap; the others are processed whatever their score)
     const bool logged = P.learned == 2 && !full;
     const bool select = P.learned == 1 && kind == kRoundLearned;
+    // a row the model can ever score: its state (features of later rounds) is kept
+    const bool scored_row = P.learned == 2 || len >= P.learn_min_len;
+    const bool decide = select && leader0 && scored_row && round - P.dirty[r] < kMaxDeferRounds;
     __nv_bfloat16 (*feat)[16] = reinterpret_cast<__nv_bfloat16 (*)[16]>(ws.q);
     unsigned trace_idx = 0xffffffffu;
-    if (logged || select) {
-        if (leader0) {
+    const bool any_decide = __any_sync(kFull, decide);  // every lane, outside any condition
+    if (logged || (select && any_decide)) {
+        if (logged ? leader0 : decide) {
             float v[16];
             row_features(P, r, round, len, lhs, rhs, v);
 #pragma unroll
@@ -106,8 +112,7 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         // rows the model decides for: marked, at least learn_min_len long and
         // younger than the deferral cap (the others are processed whatever
         // their score); a 16-row tile without one is not scored
-        const unsigned need = __ballot_sync(kFull, leader0 && len >= P.learn_min_len &&
-                                                       round - P.dirty[r] < kMaxDeferRounds);
+        const unsigned need = __ballot_sync(kFull, decide);
         const int ntiles = ((32 >> lg) + 15) >> 4;
         for (int tile = 0; tile < ntiles; tile++) {
             if (!(need & (lg == 0 ? 0xFFFFu << (16 * tile) : kFull))) continue;  // warp-uniform
@@ -127,8 +132,10 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         // processed too, so that no row is deferred (and scored) round after
         // round while a long propagation never lets a flush happen (L.z of
         // those rows may be stale: their tile may have gone unscored)
-        const bool keep = act && (len < P.learn_min_len || round - P.dirty[r] >= kMaxDeferRounds ||
-                                  L.z[rl] >= P.tau);  // the same for every lane of the row
+        // every lane takes part in the shuffle (a full-mask shuffle that some
+        // lanes skip is undefined), then each row keeps or defers as one
+        const bool row_decided = __shfl_sync(kFull, decide, rl << lg);
+        const bool keep = act && (!row_decided || L.z[rl] >= P.tau);
         const unsigned deferred = __ballot_sync(kFull, leader0 && !keep);
         if (lane == 0 && deferred) atomicAdd(&P.flags[0].rows_deferred, (unsigned long long)__popc(deferred));
         any_deferred = deferred != 0;
@@ -161,7 +168,7 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
     float slack_lo = 0.0f;
     if (leader) {
         exact = !scr_skips(c, len, lhs, rhs);
-        st = screen_stats(c, len, lhs, rhs);
+        if (scored_row) st = screen_stats(c, len, lhs, rhs);
         if (exact) {
             float hi;
             scr_slack(c, len, lhs, rhs, slack_lo, hi);
@@ -180,13 +187,15 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
     if (leader) {
         const bool tightened = L.tight[rl] > 0;
         if (logged && trace_idx < P.trace_cap) P.trace_y[trace_idx] = tightened ? 1.f : 0.f;
-        const unsigned old = P.rinfo[r];
-        const unsigned streak = tightened ? 0u : min(((old >> kRowInfoStreakShift) & 255u) + 1u, 255u);
-        P.rinfo[r] = (unsigned)min(c.minf, 3) | ((unsigned)min(c.maxf, 3) << 2) | ((exact ? 1u : 0u) << 4) |
-                     ((L.go[rl] ? 1u : 0u) << 5) | (streak << kRowInfoStreakShift);
-        P.rstat[r] = st;
-        P.last_proc[r] = round;
-        if (tightened) P.last_tight[r] = round;
+        if (scored_row) {  // rows the model never scores need no feature state
+            const unsigned old = P.rinfo[r];
+            const unsigned streak = tightened ? 0u : min(((old >> kRowInfoStreakShift) & 255u) + 1u, 255u);
+            P.rinfo[r] = (unsigned)min(c.minf, 3) | ((unsigned)min(c.maxf, 3) << 2) | ((exact ? 1u : 0u) << 4) |
+                         ((L.go[rl] ? 1u : 0u) << 5) | (streak << kRowInfoStreakShift);
+            P.rstat[r] = st;
+            P.last_proc[r] = round;
+            if (tightened) P.last_tight[r] = round;
+        }
         P.dirty[r] = 0;
         P.dcount[r] = 0;
     }

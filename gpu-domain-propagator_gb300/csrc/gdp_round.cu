@@ -21,10 +21,13 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_candidates(DevProblem P) {
     __shared__ WarpSmem ws[kWarpsPerCta];
     const int round = P.flags[0].rounds;
     if (P.flags[0].infeasible) return;
-    if (exact_rows_queued(P, 0))
-        exact_rows_phase(P, 0, &P.flags[0].change, &P.flags[0].tight, ws[threadIdx.x >> 5], threadIdx.x & 31);
+    // the multi-tile rows' tiles (1,024 non-zeros each) first, the deferred
+    // exact rows (at most split_tile non-zeros, mostly short) after them: the
+    // heavy items do not end up as the phase's tail
     candidate_phase(P, round, P.flags[0].mark_cur != 0, P.queue + 1, &P.flags[0].exact, ws[threadIdx.x >> 5],
                     threadIdx.x & 31);
+    if (exact_rows_queued(P, 0))
+        exact_rows_phase(P, 0, &P.flags[0].change, &P.flags[0].tight, ws[threadIdx.x >> 5], threadIdx.x & 31);
 }
 
 __global__ void __launch_bounds__(kCtaThreads, 4) k_exact(DevProblem P) {
@@ -143,8 +146,8 @@ __global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
             }
             const bool xrows = exact_rows_queued(P, par);
             if (xrows || P.n_mtiles) {
+                if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, mine, lane);  // heavy items first
                 if (xrows) exact_rows_phase(P, par, change, tight, mine, lane);
-                if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, mine, lane);
                 if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
                 if (P.n_mtiles && *((volatile int *)exact)) {
                     exact_phase(P, round, q + 2, change, tight, mine, lane);

@@ -451,17 +451,39 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
         // (an integer compare of the keys; inf / NaN always pass)
         double m = 0.0;
         const long long kcut = order_key(dbits(slack_lo == slack_lo ? (double)slack_lo : -1e308));
-#pragma unroll 4
-        for (int i = 0; i < cnt1; i++) {
-            const int j = __ldg(col + st * i);
-            const double a = __ldg(val + st * i);
-            const double2 b = load_bnd(P, j);
+        auto elem = [&](int i, double a, double2 b) {
             acc_add_terms(s, a, b.x, b.y);
             const double d = dmul(fabs(a), dsub(b.y, b.x));
             if (eps_gt_fast(d, m)) m = d;
             const long long db = dbits(d);
             if (order_key(db) > kcut || (db & 0x7FF0000000000000LL) == 0x7FF0000000000000LL)
                 cmask |= 1u << (i & 31);
+        };
+        if (st == 1) {
+            // the row-contiguous copy: rows start on 4-element boundaries and
+            // are zero-padded to them, so 4 columns and 4 coefficients come in
+            // three 16-byte loads and the 4 bound gathers go out together
+            for (int i = 0; i < cnt1; i += 4) {
+                const int4 c4 = __ldg(reinterpret_cast<const int4 *>(col + i));
+                const double2 v01 = __ldg(reinterpret_cast<const double2 *>(val + i));
+                const double2 v23 = __ldg(reinterpret_cast<const double2 *>(val + i + 2));
+                const bool k1 = i + 1 < cnt1, k2 = i + 2 < cnt1, k3 = i + 3 < cnt1;
+                const double2 b0 = load_bnd(P, c4.x);
+                double2 b1 = make_double2(0.0, 0.0), b2 = b1, b3 = b1;
+                if (k1) b1 = load_bnd(P, c4.y);
+                if (k2) b2 = load_bnd(P, c4.z);
+                if (k3) b3 = load_bnd(P, c4.w);
+                elem(i, v01.x, b0);
+                if (k1) elem(i + 1, v01.y, b1);
+                if (k2) elem(i + 2, v23.x, b2);
+                if (k3) elem(i + 3, v23.y, b3);
+            }
+        } else {
+#pragma unroll 4
+            for (int i = 0; i < cnt1; i++) {
+                const int j = __ldg(col + st * i);
+                elem(i, __ldg(val + st * i), load_bnd(P, j));
+            }
         }
         if (leader) {
             mn = row_min_slack(s.minact, s.maxact, lhs, rhs);
