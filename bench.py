@@ -654,7 +654,8 @@ def main(argv=None):
     t0 = time.perf_counter()
     ctx = gdp.Context(mip, sync_type=sync, max_rounds=args.max_rounds, thread_row_max=args.trm,
                       split_tile=args.tile, use_marking=args.marking,
-                      ctas_per_sm=tuned["options"]["ctas_per_sm"] if tuned else 0)
+                      ctas_per_sm=tuned["options"]["ctas_per_sm"] if tuned else 0,
+                      cta_threads=tuned["options"]["cta_threads"] if tuned else 0)
     ctx_s = time.perf_counter() - t0
     layout = ctx.layout()
     stream = torch.cuda.current_stream()

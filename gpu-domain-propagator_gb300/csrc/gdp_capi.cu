@@ -210,6 +210,10 @@ GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *col, const 
     });
 }
 
+GDP_RETCODE gdp_autotune_clear_cache(void) {
+    return guarded([&]() -> GDP_RETCODE { return gdp::autotune_clear_cache(); });
+}
+
 GDP_RETCODE gdp_context_destroy(gdp_context *ctx) {
     return guarded([&]() -> GDP_RETCODE {
         delete ctx;

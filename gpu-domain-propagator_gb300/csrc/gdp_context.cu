@@ -208,6 +208,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         set_error("Unknown sync type");
         return GDP_ERROR;
     }
+    if (opts.cta_threads == 0) opts.cta_threads = 256;
+    if (opts.cta_threads != 128 && opts.cta_threads != 256 && opts.cta_threads != 512) {
+        set_error("cta_threads must be 128, 256 or 512");
+        return GDP_ERROR;
+    }
     if (!lhs || !rhs) { set_error("null lhs/rhs"); return GDP_ERROR; }
     if (validate_csr(m, n, nnz, col, row_ptr, val, vartype) != GDP_OKAY) return GDP_ERROR;  // host part
 
@@ -670,17 +675,43 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         P.var_ptr = vp;
         P.var_pos = vpos;
     }
+    if (set_schedule(opts.sync_type, opts.ctas_per_sm, opts.cta_threads) != GDP_OKAY) return GDP_ERROR;
+    GDP_CUDA(cudaStreamSynchronize(stream));
+    return GDP_OKAY;
+}
+
+// Grid sizes of the loop drivers for the schedule (the layout is untouched).
+GDP_RETCODE Context::set_schedule(int sync_type, int ctas_per_sm, int cta_threads) {
+    if (sync_type < CPU_LOOP || sync_type > MEGAKERNEL) {
+        set_error("Unknown sync type");
+        return GDP_ERROR;
+    }
+    if (cta_threads != 128 && cta_threads != 256 && cta_threads != 512) {
+        set_error("cta_threads must be 128, 256 or 512");
+        return GDP_ERROR;
+    }
+    GDP_CUDA(cudaSetDevice(opts.device));
+    const int warps = cta_threads / 32;
     int act_bps = 0, cand_bps = 0, mega_bps = 0;
-    GDP_CUDA(phase_occupancy(&act_bps, &cand_bps, &mega_bps));
-    if (opts.ctas_per_sm > 0) {
-        act_bps = std::min(act_bps, opts.ctas_per_sm);
-        cand_bps = std::min(cand_bps, opts.ctas_per_sm);
-        mega_bps = std::min(mega_bps, opts.ctas_per_sm);
+    GDP_CUDA(phase_occupancy(&act_bps, &cand_bps, &mega_bps, warps));
+    if (ctas_per_sm > 0) {
+        act_bps = std::min(act_bps, ctas_per_sm);
+        cand_bps = std::min(cand_bps, ctas_per_sm);
+        mega_bps = std::min(mega_bps, ctas_per_sm);
     }
     act_blocks = std::max(1, std::min(act_bps * n_sms, (P.n_items + kWarpsPerCta - 1) / kWarpsPerCta));
     cand_blocks = std::max(1, cand_bps * n_sms);  // the exact-rows phase shares this launch
     mega_grid = std::max(1, mega_bps) * n_sms;
-    GDP_CUDA(cudaStreamSynchronize(stream));
+    mega_warps = warps;
+    if (graph_exec && (opts.ctas_per_sm != ctas_per_sm)) {  // the GPU_LOOP graph holds the old grids
+        cudaGraphExecDestroy(graph_exec);
+        cudaGraphDestroy(graph);
+        graph_exec = nullptr;
+        graph = nullptr;
+    }
+    opts.sync_type = sync_type;
+    opts.ctas_per_sm = ctas_per_sm;
+    opts.cta_threads = cta_threads;
     return GDP_OKAY;
 }
 
@@ -775,7 +806,7 @@ GDP_RETCODE Context::rounds_gpu_loop(cudaStream_t s, int *launches) {
 
 // MEGAKERNEL: every round in one persistent cooperative launch.
 GDP_RETCODE Context::rounds_megakernel(cudaStream_t s, int *launches) {
-    GDP_CUDA(launch_megakernel(P, mega_grid, s));
+    GDP_CUDA(launch_megakernel(P, mega_grid, mega_warps, s));
     *launches += 1;
     GDP_CUDA(cudaMemcpyAsync(h_flags, P.flags, sizeof(RoundFlags), cudaMemcpyDeviceToHost, s));
     GDP_CUDA(cudaStreamSynchronize(s));

@@ -38,6 +38,7 @@ GDP_RETCODE autotune(int m, int n, int nnz, const int *col, const int *row_ptr, 
                      const double *lhs, const double *rhs, const double *lbs, const double *ubs,
                      const int *vartype, const gdp_options *base, int repeats, gdp_options *best,
                      double *best_ms, gdp_tune_trial *trials, int max_trials, int *n_trials);
+GDP_RETCODE autotune_clear_cache();
 
 GDP_RETCODE validate_csr(int m, int n, int nnz, const int *col, const int *row_ptr,
                          const double *val, const int *vartype);
@@ -49,6 +50,9 @@ public:
                      const double *lhs, const double *rhs, const int *vartype, const gdp_options *o);
     GDP_RETCODE propagate_host(double *lbs, double *ubs, gdp_stats *st);
     GDP_RETCODE propagate_device(double *d_lbs, double *d_ubs, cudaStream_t s, gdp_stats *st);
+    // Loop driver, resident CTAs per SM (0: as many as fit) and megakernel CTA
+    // size of later propagations; the layout stays.
+    GDP_RETCODE set_schedule(int sync_type, int ctas_per_sm, int cta_threads);
     // Learned marking with model m (NULL: off), logit threshold and the
     // shortest row length the model decides for.
     GDP_RETCODE set_model(const Mlp *m, float threshold, int min_len);
@@ -65,6 +69,7 @@ public:
     DevProblem P{};
     double *d_lb = nullptr, *d_ub = nullptr;  // staging for host bounds
     int n_sms = 0, vec_blocks = 1, act_blocks = 1, cand_blocks = 1, mega_grid = 1, learned_grid = 1;
+    int mega_warps = 8;  // warps per CTA of the megakernel (opts.cta_threads / 32)
     int n_srows = 0, n_slices = 0, n_lrows = 0, n_tiles = 0;
     long long sell_elems = 0;
     // the last propagation converged feasibly: P.bnd is a fixpoint of the problem

@@ -199,8 +199,9 @@ int launch_candidate_phase(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_exact_phase(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_finalize(const DevProblem &P, int blocks, cudaStream_t s);
 int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_t s);
-int launch_megakernel(const DevProblem &P, int grid, cudaStream_t s);
-int phase_occupancy(int *act_blocks_per_sm, int *cand_blocks_per_sm, int *mega_blocks_per_sm);
+// cta_warps: 4, 8 or 16 warps per CTA of the megakernel
+int launch_megakernel(const DevProblem &P, int grid, int cta_warps, cudaStream_t s);
+int phase_occupancy(int *act_blocks_per_sm, int *cand_blocks_per_sm, int *mega_blocks_per_sm, int cta_warps);
 // gdp_layout.cu: element arrays of the layout from the raw CSR (all device pointers)
 struct LayoutBuild {
     const int *col, *row_ptr;  // raw CSR

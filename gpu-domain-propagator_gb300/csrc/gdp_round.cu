@@ -118,8 +118,11 @@ __global__ void __launch_bounds__(256) k_mark_all(DevProblem P) {
 // so that nothing a CTA may still read is cleared: the next round's slots are cleared after the current
 // round's first barrier, which every CTA passes only after finishing the
 // previous round.
-__global__ void __launch_bounds__(kCtaThreads, 3) k_megakernel(DevProblem P) {
-    __shared__ WarpSmem ws[kWarpsPerCta];
+// W warps per CTA; with 24 / W resident CTAs per SM every instance holds about
+// 24 warps per SM under the same register budget.
+template <int W>
+__global__ void __launch_bounds__(32 * W, 24 / W) k_megakernel(DevProblem P) {
+    __shared__ WarpSmem ws[W];
     const int lane = threadIdx.x & 31;
     WarpSmem &mine = ws[threadIdx.x >> 5];
     int *err = &P.flags[0].error;
@@ -235,23 +238,35 @@ int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_
     return (int)cudaGetLastError();
 }
 
-int phase_occupancy(int *act, int *cand, int *mega) {
-    // the megakernel's shared memory (warp queues and row constants, ~29 KB
-    // per CTA, 3 CTAs per SM) is small: prefer a carveout that just holds it,
-    // the rest of the 256 KB per SM serving as L1 for the element streams
-    cudaError_t e = cudaFuncSetAttribute(k_megakernel, cudaFuncAttributePreferredSharedMemoryCarveout, 40);
+namespace {
+const void *megakernel_of(int cta_warps) {
+    switch (cta_warps) {
+        case 4: return (const void *)k_megakernel<4>;
+        case 16: return (const void *)k_megakernel<16>;
+        default: return (const void *)k_megakernel<8>;
+    }
+}
+}  // namespace
+
+int phase_occupancy(int *act, int *cand, int *mega, int cta_warps) {
+    // the megakernel's shared memory (warp queues and row constants, ~3.6 KB
+    // per warp, ~24 warps per SM) is small: prefer a carveout that just holds
+    // it, the rest of the 256 KB per SM serving as L1 for the element streams
+    const void *mk = megakernel_of(cta_warps);
+    cudaError_t e = cudaFuncSetAttribute(mk, cudaFuncAttributePreferredSharedMemoryCarveout, 40);
     if (e != cudaSuccess) return (int)e;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(act, k_activity, kCtaThreads, 0);
     if (e != cudaSuccess) return (int)e;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(cand, k_exact, kCtaThreads, 0);
     if (e != cudaSuccess) return (int)e;
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(mega, k_megakernel, kCtaThreads, 0);
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(mega, mk, 32 * cta_warps, 0);
 }
 
-int launch_megakernel(const DevProblem &P, int grid, cudaStream_t s) {
+int launch_megakernel(const DevProblem &P, int grid, int cta_warps, cudaStream_t s) {
     DevProblem Pc = P;
     void *args[] = {&Pc};
-    return (int)cudaLaunchCooperativeKernel((const void *)k_megakernel, dim3(grid), dim3(kCtaThreads), args, 0, s);
+    return (int)cudaLaunchCooperativeKernel(megakernel_of(cta_warps), dim3(grid), dim3(32 * cta_warps), args, 0,
+                                            s);
 }
 
 }  // namespace gdp

@@ -45,7 +45,7 @@ class MpsProblem(C.Structure):
 
 class TuneTrial(C.Structure):
     _fields_ = [("thread_row_max", C.c_int), ("split_tile", C.c_int), ("sync_type", C.c_int),
-                ("ctas_per_sm", C.c_int), ("rounds", C.c_int), ("pad_", C.c_int), ("ms", C.c_double)]
+                ("ctas_per_sm", C.c_int), ("rounds", C.c_int), ("cta_threads", C.c_int), ("ms", C.c_double)]
 
 
 class Options(C.Structure):
@@ -58,7 +58,8 @@ class Options(C.Structure):
         ("use_marking", C.c_int),
         ("ctas_per_sm", C.c_int),
         ("barrier_wait_kcycles", C.c_int),
-        ("reserved", C.c_int * 5),
+        ("cta_threads", C.c_int),
+        ("reserved", C.c_int * 4),
     ]
 
 
@@ -149,6 +150,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     lib.gdp_autotune.argtypes = _LEGACY_ARGS[:8] + [_P_DBL, _P_DBL, _P_INT, C.POINTER(Options), C.c_int,
                                                     C.POINTER(Options), C.POINTER(C.c_double),
                                                     C.POINTER(TuneTrial), C.c_int, C.POINTER(C.c_int)]
+    lib.gdp_autotune_clear_cache.restype = C.c_int
     lib.gdp_autotune.restype = C.c_int
     lib.gdp_mps_parse.argtypes = [C.c_char_p, C.c_longlong, C.POINTER(MpsProblem)]
     lib.gdp_mps_parse.restype = C.c_int
@@ -263,13 +265,14 @@ class Context:
     """Persistent device context: upload once, propagate many bound vectors."""
 
     def __init__(self, mip: MIP, sync_type: int = CPU_LOOP, max_rounds: int = 0, thread_row_max: int = 0,
-                 split_tile: int = 0, use_marking: int = -1, ctas_per_sm: int = 0, barrier_wait_kcycles: int = 0):
+                 split_tile: int = 0, use_marking: int = -1, ctas_per_sm: int = 0, barrier_wait_kcycles: int = 0,
+                 cta_threads: int = 0):
         self._lib = load_library()
         self.mip = mip.normalized()
         p = self.mip
         o = default_options(sync_type=sync_type, max_rounds=max_rounds, thread_row_max=thread_row_max,
                             split_tile=split_tile, use_marking=use_marking, ctas_per_sm=ctas_per_sm,
-                            barrier_wait_kcycles=barrier_wait_kcycles)
+                            barrier_wait_kcycles=barrier_wait_kcycles, cta_threads=cta_threads)
         h = C.c_void_p()
         rc = self._lib.gdp_context_create(p.m, p.n, p.nnz, _pi(p.col), _pi(p.row_ptr), _pd(p.val),
                                           _pd(p.lhs), _pd(p.rhs), _pi(p.vartype), C.byref(o), C.byref(h))
@@ -370,7 +373,8 @@ def read_mps(path) -> MIP:
 
 def autotune(mip: MIP, repeats: int = 2, max_rounds: int = 0, use_marking: int = -1):
     """gdp_autotune: the fastest (thread_row_max, split_tile, sync_type,
-    ctas_per_sm) for `mip`. Returns (options dict, best ms, list of trials)."""
+    ctas_per_sm, cta_threads) for `mip`, cached per problem shape. Returns
+    (options dict, best ms, list of trials)."""
     lib = load_library()
     p = mip.normalized()
     base = default_options(max_rounds=max_rounds, use_marking=use_marking)
@@ -383,10 +387,13 @@ def autotune(mip: MIP, repeats: int = 2, max_rounds: int = 0, use_marking: int =
                           C.byref(ms), trials, 64, C.byref(k))
     _check(rc, "gdp_autotune")
     opts = {name: getattr(best, name) for name in ("thread_row_max", "split_tile", "sync_type", "ctas_per_sm",
-                                                   "use_marking", "max_rounds")}
-    table = [{name: getattr(trials[i], name) for name, _ in TuneTrial._fields_ if name != "pad_"}
-             for i in range(k.value)]
+                                                   "cta_threads", "use_marking", "max_rounds")}
+    table = [{name: getattr(trials[i], name) for name, _ in TuneTrial._fields_} for i in range(k.value)]
     return opts, ms.value, table
+
+
+def autotune_clear_cache() -> None:
+    _check(load_library().gdp_autotune_clear_cache(), "gdp_autotune_clear_cache")
 
 
 class Batch:
@@ -409,7 +416,9 @@ class Batch:
             big = max(ps, key=lambda p: p.nnz)
             tuned, _, _ = globals()["autotune"](big, repeats=1, max_rounds=max_rounds, use_marking=use_marking)
             thread_row_max, split_tile = tuned["thread_row_max"], tuned["split_tile"]
-            ctas_per_sm = tuned["ctas_per_sm"]
+            # the batch loop runs 256-thread CTAs: the tuned warps per SM, in its CTAs
+            ctas_per_sm = (max(1, tuned["ctas_per_sm"] * tuned["cta_threads"] // 256)
+                           if tuned["ctas_per_sm"] > 0 else 0)
         arr_i = lambda xs: (C.c_int * k)(*xs)
         col = (_P_INT * k)(*[_pi(p.col) for p in ps])
         rp = (_P_INT * k)(*[_pi(p.row_ptr) for p in ps])

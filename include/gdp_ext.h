@@ -46,7 +46,10 @@ typedef struct {
                              waits longer records a device error, every CTA leaves at its next
                              barrier and the call returns GDP_ERROR. 0 (default) = 4,000,000
                              (about 2 s at 2 GHz) */
-    int reserved[5];      /* must be zero */
+    int cta_threads;      /* threads per CTA of the MEGAKERNEL loop: 128, 256 or 512; 0 (default) = 256.
+                             With ctas_per_sm = 0 as many CTAs run per SM as fit (up to 6, 3 and 1,
+                             about 24 warps per SM) */
+    int reserved[4];      /* must be zero */
 } gdp_options;
 
 typedef struct {
@@ -239,19 +242,25 @@ GDP_RETCODE gdp_context_trace(gdp_context *ctx, double *lbs, double *ubs, int ca
                               float *labels, int *n_samples, gdp_stats *stats);
 
 /* ---- autotuner (no counterpart in the reference) ---------------------------
- * Times the propagation of one problem from lbs/ubs (host, not modified) under
- * candidate row bins (thread_row_max in {16, 32, 64} x split_tile in {512,
- * 1024, 2048}) and loop schedules (MEGAKERNEL with 2, 3 or all-fitting CTAs
- * per SM, GPU_LOOP), `repeats` times each (best device time counts), starting
- * from `base` (may be NULL) for every other option. *best receives the
- * fastest options and *best_ms their device time; trials (may be NULL)
- * receives up to max_trials records and *n_trials their count. The layouts
- * only change the summation order of rows longer than thread_row_max (each
- * layout is bit-exact with the oracle's matching GPU mode), so on slowly
- * converging continuous bounds the round count may differ by a round between
- * candidates; the time to the fixpoint is what counts. */
+ * Times the propagation of one problem from lbs/ubs (host, not modified) in
+ * two stages, `repeats` times per candidate (best device time counts),
+ * starting from `base` (may be NULL) for every other option: first the row
+ * bins (thread_row_max in {16, 32, 64} x split_tile in {512, 1024, 2048})
+ * under base's schedule (MEGAKERNEL if base's is CPU_LOOP), then, on the
+ * fastest bins, the loop schedule: MEGAKERNEL with 128-, 256- or 512-thread
+ * CTAs at several CTAs per SM, and GPU_LOOP. *best receives the fastest
+ * options and *best_ms their device time; trials (may be NULL) receives up
+ * to max_trials records and *n_trials their count. The layouts only change
+ * the summation order of rows longer than thread_row_max (each layout is
+ * bit-exact with the oracle's matching GPU mode), so on slowly converging
+ * continuous bounds the round count may differ by a round between
+ * candidates; the time to the fixpoint is what counts.
+ * Results are cached per problem shape (device, m, n, nnz, the histogram of
+ * row lengths in powers of two, base's round cap and marking): a later call
+ * for a problem of the same shape returns the cached options and trials at
+ * once. gdp_autotune_clear_cache empties the cache. */
 typedef struct {
-    int thread_row_max, split_tile, sync_type, ctas_per_sm, rounds, pad_;
+    int thread_row_max, split_tile, sync_type, ctas_per_sm, rounds, cta_threads;
     double ms;
 } gdp_tune_trial;
 GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *csr_col_indices, const int *csr_row_ptrs,
@@ -259,6 +268,7 @@ GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *csr_col_ind
                          const double *ubs, const int *vartypes, const gdp_options *base, int repeats,
                          gdp_options *best, double *best_ms, gdp_tune_trial *trials, int max_trials,
                          int *n_trials);
+GDP_RETCODE gdp_autotune_clear_cache(void);
 
 /* ---- MPS reader (no counterpart in the reference, which reads MPS through
  * python-mip, fileReader/readerInterface.py:52-145) ---------------------------
