@@ -425,7 +425,7 @@ def batched_result(args, local) -> dict:
     # plain: every member alone, device-resident bounds, CUDA-event time of its round loop
     def plain_total(use_marking):
         ctxs = {}
-        total, rounds, n_exact, n_same = 0.0, [], 0, 0
+        total, rounds, n_exact, n_same, per_member = 0.0, [], 0, 0, []
         worst = {"int_mismatches": 0, "cont_beyond_tol": 0, "cont_max_abs": 0.0, "cont_max_rel": 0.0}
         for k, pm in enumerate(plain_mips):
             key = id(pm)
@@ -452,12 +452,15 @@ def batched_result(args, local) -> dict:
                     worst[f] += c[f]
                 for f in ("cont_max_abs", "cont_max_rel"):
                     worst[f] = max(worst[f], c[f])
+                per_member.append(float(c["cont_max_abs"]))
+            else:
+                per_member.append(None)  # a verdict differs, or both infeasible
             n_same += int(same)
         for c in ctxs.values():
             c.close()
-        return total, rounds, n_exact, n_same, worst
+        return total, rounds, n_exact, n_same, worst, per_member
 
-    plain_ms, rounds_plain, exact_plain, same_plain, worst_plain = plain_total(1)
+    plain_ms, rounds_plain, exact_plain, same_plain, worst_plain, member_dev = plain_total(1)
     out = {"workload": BATCH_WORKLOADS[args.workload + ("_learned" if learned_info else "")],
            "value": value, "unit": "ms", "steps": args.steps, "e2e_ms": statistics.median(e2e_ms),
            **sizes, "scale": args.scale, "max_rounds": max_rounds or 100,
@@ -475,11 +478,13 @@ def batched_result(args, local) -> dict:
            "d2h_bytes_per_step": int(16 * sum(len(x) for x in members[0])),
            "gpu_launches": int(tot["kernel_launches"]), "clocks": clk,
            "setup_s": {"generate": gen_s, "build": build_s}}
+    if learned_info is not None:  # each member's largest continuous deviation from its plain fixpoint
+        out["member_max_abs_deviation"] = [None if d is None else float(f"{d:.3g}") for d in member_dev]
     if exact_batch_ms is not None:
         out["exact_marking_batch_ms"] = exact_batch_ms
         out["speedup_vs_exact_marking_batch"] = exact_batch_ms / value
     if args.full_sweep_baseline:
-        full_ms, rounds_full, exact_full, _, _ = plain_total(0)
+        full_ms, rounds_full, exact_full, _, _, _ = plain_total(0)
         out["full_sweep_ms"] = full_ms
         out["speedup_vs_full_sweep"] = full_ms / value
         out["members_bitexact_with_full_sweep"] = f"{exact_full}/{len(plain_mips)}"

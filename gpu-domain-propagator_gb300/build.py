@@ -3,7 +3,11 @@
     libgdp_gb300.so  -- CUDA kernels (sm_103a) + host driver + C-ABI (include/*.h)
     libgdpgen.so     -- seeded synthetic MIP generators (host C++)
 
-Both land in gpu-domain-propagator_gb300/lib/. Translation units compile in
+Both land in gpu-domain-propagator_gb300/lib/. `--phase-timers` builds, beside
+them, libgdp_gb300_timers.so: the same library compiled with
+-DGDP_PHASE_TIMERS, whose megakernel records per-round phase times
+(gdp_phase_timers_read; phase_split.py prints them). It is slower by the
+timers' atomics and is never loaded by default. Translation units compile in
 parallel; one -gencode (compute_103a / sm_103a) keeps the build to about a
 minute.
 """
@@ -60,18 +64,20 @@ def nvcc_flags(extra: list[str] | None = None) -> list[str]:
     ] + (extra or [])
 
 
-def build(verbose: bool = False, force: bool = False) -> dict[str, Path]:
+def build(verbose: bool = False, force: bool = False, phase_timers: bool = False) -> dict[str, Path]:
+    obj_dir = OBJ.with_name(OBJ.name + "_timers") if phase_timers else OBJ
+    defines = ["-DGDP_PHASE_TIMERS"] if phase_timers else []
     LIB.mkdir(parents=True, exist_ok=True)
-    OBJ.mkdir(parents=True, exist_ok=True)
+    obj_dir.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     jobs = []
     objs = []
     for src in CUDA_SOURCES:
-        o = OBJ / (Path(src).stem + ".o")
+        o = obj_dir / (Path(src).stem + ".o")
         objs.append(o)
         if force or _stale(o, [CSRC / src] + headers):
-            jobs.append([nvcc, *nvcc_flags(), "-c", str(CSRC / src), "-o", str(o)])
+            jobs.append([nvcc, *nvcc_flags(defines), "-c", str(CSRC / src), "-o", str(o)])
     gen_so = LIB / "libgdpgen.so"
     gen_job = None
     if force or _stale(gen_so, [CSRC / "gdp_gen.cpp", CSRC / "gdp_gen.h"]):
@@ -83,7 +89,7 @@ def build(verbose: bool = False, force: bool = False) -> dict[str, Path]:
             futs.append(ex.submit(_run, gen_job, verbose))
         for f in futs:
             f.result()
-    so = LIB / "libgdp_gb300.so"
+    so = LIB / ("libgdp_gb300_timers.so" if phase_timers else "libgdp_gb300.so")
     if force or jobs or not so.exists():
         _run([nvcc, *ARCH, "-shared", "-o", str(so), *map(str, objs), "-Xcompiler", "-fopenmp",
               "-lgomp"], verbose)
@@ -91,6 +97,6 @@ def build(verbose: bool = False, force: bool = False) -> dict[str, Path]:
 
 
 if __name__ == "__main__":
-    out = build(verbose="-v" in sys.argv, force="-f" in sys.argv)
+    out = build(verbose="-v" in sys.argv, force="-f" in sys.argv, phase_timers="--phase-timers" in sys.argv)
     for k, v in out.items():
         print(k, v)

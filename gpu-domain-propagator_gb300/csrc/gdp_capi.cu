@@ -214,6 +214,29 @@ GDP_RETCODE gdp_autotune_clear_cache(void) {
     return guarded([&]() -> GDP_RETCODE { return gdp::autotune_clear_cache(); });
 }
 
+namespace {
+GDP_RETCODE timer_status(int e) {
+    if (e == -1) {
+        gdp::set_error("phase timers are compiled only into a library built with GDP_PHASE_TIMERS");
+        return GDP_NOTIMPLEMENTED;
+    }
+    if (e != 0) {
+        gdp::set_error(std::string("phase timers: ") + cudaGetErrorString((cudaError_t)e));
+        return GDP_ERROR;
+    }
+    return GDP_OKAY;
+}
+}  // namespace
+
+GDP_RETCODE gdp_phase_timers_clear(void) {
+    return guarded([&]() -> GDP_RETCODE { return timer_status(gdp::phase_timers_clear()); });
+}
+
+GDP_RETCODE gdp_phase_timers_read(unsigned long long *wall, unsigned long long *busy, unsigned long long *pass,
+                                  int rounds) {
+    return guarded([&]() -> GDP_RETCODE { return timer_status(gdp::phase_timers_read(wall, busy, pass, rounds)); });
+}
+
 GDP_RETCODE gdp_context_destroy(gdp_context *ctx) {
     return guarded([&]() -> GDP_RETCODE {
         delete ctx;

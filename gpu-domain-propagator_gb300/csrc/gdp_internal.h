@@ -202,6 +202,10 @@ int launch_condition(const DevProblem &P, unsigned long long handle, cudaStream_
 // cta_warps: 4, 8 or 16 warps per CTA of the megakernel
 int launch_megakernel(const DevProblem &P, int grid, int cta_warps, cudaStream_t s);
 int phase_occupancy(int *act_blocks_per_sm, int *cand_blocks_per_sm, int *mega_blocks_per_sm, int cta_warps);
+// Phase timers of the megakernel (a library built with GDP_PHASE_TIMERS):
+// 0 or a CUDA error; -1 when the library was built without them.
+int phase_timers_clear();
+int phase_timers_read(unsigned long long *wall, unsigned long long *busy, unsigned long long *pass, int rounds);
 // gdp_layout.cu: element arrays of the layout from the raw CSR (all device pointers)
 struct LayoutBuild {
     const int *col, *row_ptr;  // raw CSR

@@ -2,6 +2,8 @@
 // (CPU_LOOP and GPU_LOOP drivers) and as a persistent cooperative megakernel
 // that runs every round in one launch (MEGAKERNEL driver). The round's device
 // functions live in gdp_round.cuh.
+#include <algorithm>
+
 #include "gdp_round.cuh"
 
 namespace gdp {
@@ -112,6 +114,30 @@ __global__ void __launch_bounds__(256) k_mark_all(DevProblem P) {
 }
 
 // ---- megakernel -----------------------------------------------------------
+#ifdef GDP_PHASE_TIMERS
+// Stamp k of round r by one thread (0: round start, 1: after phase A's
+// barrier, 2: after B's, 3: after C's, 4: after F's, with the cumulative
+// processed rows, non-zeros and exact non-zeros in slots 5-7).
+__device__ __forceinline__ void timer_stamp(const DevProblem &P, int round, int k) {
+    if (blockIdx.x != 0 || threadIdx.x != 0 || round >= kTimerRounds) return;
+    unsigned long long *w = g_timer_wall + round * kTimerSlots;
+    w[k] = timer_now();
+    if (k == 4) {
+        w[5] = *((volatile unsigned long long *)&P.flags[0].rows_proc);
+        w[6] = *((volatile unsigned long long *)&P.flags[0].nnz_proc);
+        w[7] = *((volatile unsigned long long *)&P.flags[0].nnz_exact);
+    }
+}
+// adds the warp's time in phase k of round r since t0 (0: A, 1: B multi-tile
+// rows, 2: B deferred exact rows, 3: C, 4: F)
+__device__ __forceinline__ void timer_busy(int lane, int round, int k, unsigned long long t0) {
+    if (lane == 0 && round < kTimerRounds) atomicAdd(&g_timer_busy[round * kTimerSlots + k], timer_now() - t0);
+}
+#else
+__device__ __forceinline__ void timer_stamp(const DevProblem &, int, int) {}
+__device__ __forceinline__ void timer_busy(int, int, int, unsigned long long) {}
+#endif
+
 // Round loop on the device. flags[0] holds the sticky state; flags[1 + (round
 // & 1)] the per-round change flag, tightening and exact-row counts, and
 // queue[4 * (round & 1) + phase] the per-round work counters, double-buffered
@@ -135,8 +161,12 @@ __global__ void __launch_bounds__(32 * W, 24 / W) k_megakernel(DevProblem P) {
             unsigned *tight = &P.flags[1 + par].tight;
             int *exact = &P.flags[1 + par].exact;
             unsigned *q = P.queue + 4 * par;
+            timer_stamp(P, round, 0);
+            unsigned long long t0 = timer_now();
             activity_phase(P, round, marked, q + 0, change, tight, mine, lane, par);
+            timer_busy(lane, round, 0, t0);
             if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
+            timer_stamp(P, round, 1);
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 P.flags[1 + (par ^ 1)].change = 0;
                 P.flags[1 + (par ^ 1)].tight = 0u;
@@ -149,18 +179,29 @@ __global__ void __launch_bounds__(32 * W, 24 / W) k_megakernel(DevProblem P) {
             }
             const bool xrows = exact_rows_queued(P, par);
             if (xrows || P.n_mtiles) {
+                t0 = timer_now();
                 if (P.n_mtiles) candidate_phase(P, round, marked, q + 1, exact, mine, lane);  // heavy items first
+                timer_busy(lane, round, 1, t0);
+                t0 = timer_now();
                 if (xrows) exact_rows_phase(P, par, change, tight, mine, lane);
+                timer_busy(lane, round, 2, t0);
                 if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
+                timer_stamp(P, round, 2);
                 if (P.n_mtiles && *((volatile int *)exact)) {
+                    t0 = timer_now();
                     exact_phase(P, round, q + 2, change, tight, mine, lane);
+                    timer_busy(lane, round, 3, t0);
                     if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
+                    timer_stamp(P, round, 3);
                 }
             }
             marked = next_round_marked(P, *((volatile unsigned *)tight));
+            t0 = timer_now();
             finalize_words(P, round, marked, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+            timer_busy(lane, round, 4, t0);
             if (blockIdx.x == 0 && threadIdx.x == 0) P.flags[0].rounds = round;
             if (!grid_barrier(P.barrier, err, P.spin_limit)) return;
+            timer_stamp(P, round, 4);
             last_change = *((volatile int *)change);
             const int infeasible = *((volatile int *)&P.flags[0].infeasible);
             if (!last_change || infeasible) break;
@@ -173,6 +214,34 @@ __global__ void __launch_bounds__(32 * W, 24 / W) k_megakernel(DevProblem P) {
 }
 
 }  // namespace
+
+// ---- phase timers ---------------------------------------------------------
+
+int phase_timers_clear() {
+#ifdef GDP_PHASE_TIMERS
+    static const unsigned long long zero[kTimerRounds * kTimerSlots] = {};
+    cudaError_t e = cudaMemcpyToSymbol(g_timer_wall, zero, sizeof(zero));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_timer_busy, zero, sizeof(zero));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_timer_pass, zero, sizeof(unsigned long long) * kTimerPass);
+    return (int)e;
+#else
+    return -1;
+#endif
+}
+
+int phase_timers_read(unsigned long long *wall, unsigned long long *busy, unsigned long long *pass, int rounds) {
+#ifdef GDP_PHASE_TIMERS
+    const size_t k = sizeof(unsigned long long) * kTimerSlots * (size_t)std::min(std::max(rounds, 0), kTimerRounds);
+    cudaError_t e = cudaSuccess;
+    if (wall) e = cudaMemcpyFromSymbol(wall, g_timer_wall, k);
+    if (busy && e == cudaSuccess) e = cudaMemcpyFromSymbol(busy, g_timer_busy, k);
+    if (pass && e == cudaSuccess) e = cudaMemcpyFromSymbol(pass, g_timer_pass, sizeof(unsigned long long) * kTimerPass);
+    return (int)e;
+#else
+    (void)wall, (void)busy, (void)pass, (void)rounds;
+    return -1;
+#endif
+}
 
 // ---- launchers ------------------------------------------------------------
 

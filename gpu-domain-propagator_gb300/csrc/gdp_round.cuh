@@ -38,6 +38,37 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kQueueCap = 128;  // >= 31 pending + 64 pushed per step
 
+// Phase timers, compiled only into a library built with -DGDP_PHASE_TIMERS
+// (build.py --phase-timers): the megakernel stamps %globaltimer at the start of
+// each round and after each of its grid barriers, every warp adds the time it
+// spends in each phase, and the exact pass of SELL rows adds its two passes'
+// warp time by lane-group size. In the plain build timer_now() is 0 and the
+// recording calls are empty.
+constexpr int kTimerRounds = 1024;  // rounds recorded (later rounds are not)
+constexpr int kTimerSlots = 8;      // per round: 5 stamps + 3 work counters; 5 phase busy sums
+constexpr int kTimerPass = 16;      // 2 passes x lane-group sizes 1..32
+#ifdef GDP_PHASE_TIMERS
+__device__ unsigned long long g_timer_wall[kTimerRounds * kTimerSlots];
+__device__ unsigned long long g_timer_busy[kTimerRounds * kTimerSlots];
+__device__ unsigned long long g_timer_pass[kTimerPass];
+__device__ __forceinline__ unsigned long long timer_now() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// warp time of the exact pass's pass 1 [t0, t1) and pass 2 [t1, now)
+__device__ __forceinline__ void timer_pass(int lane, int lg, unsigned long long t0, unsigned long long t1) {
+    if (lane == 0) {
+        const unsigned long long t2 = timer_now();
+        atomicAdd(&g_timer_pass[2 * lg], t1 - t0);
+        atomicAdd(&g_timer_pass[2 * lg + 1], t2 - t1);
+    }
+}
+#else
+__device__ __forceinline__ unsigned long long timer_now() { return 0ull; }
+__device__ __forceinline__ void timer_pass(int, int, unsigned long long, unsigned long long) {}
+#endif
+
 __device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
     atomicOr(P.chg + (j >> 5), 1u << (j & 31));
 }
@@ -429,6 +460,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
                                                 int *change,
                                                 unsigned *tight_ctr, WarpSmem &ws, int *row_tight = nullptr,
                                                 int *row_go = nullptr) {
+    const unsigned long long t_pass0 = timer_now();
     const int g = 1 << lg;
     const int rl = lane >> lg, sub = lane & (g - 1);
     const bool leader = exact && sub == 0;
@@ -526,6 +558,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
         const unsigned bx = __ballot_sync(kFull, leader);
         if (lane == 0) ws.st_xrows += __popc(bx);
     }
+    const unsigned long long t_pass1 = timer_now();
     int tight = 0;
     const bool go = __shfl_sync(kFull, dec, rl << lg) == 1 && exact;
     if (row_go && leader) row_go[rl] = go ? 1 : 0;
@@ -610,6 +643,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
         queue_drain(Q, lane, true, run);
         if (lane == 0) ws.st_div += (unsigned long long)Q.pushed;
     }
+    timer_pass(lane, lg, t_pass0, t_pass1);
     report_tight(tight, lane, change, tight_ctr);
 }
 

@@ -98,8 +98,10 @@ _P_DBL = C.POINTER(C.c_double)
 _LEGACY_ARGS = [C.c_int, C.c_int, C.c_int, _P_INT, _P_INT, _P_DBL, _P_DBL, _P_DBL, _P_DBL, _P_DBL, _P_INT]
 
 
-def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
-    """Loads libgdp_gb300.so (once) and declares the C signatures."""
+def load_library(path: Optional[os.PathLike] = None, make_default: bool = False) -> C.CDLL:
+    """Loads libgdp_gb300.so (once) and declares the C signatures. A library
+    at another path (the phase-timer build) is loaded as given, and becomes the
+    one every later call of this module uses with make_default=True."""
     global _lib
     if _lib is not None and path is None:
         return _lib
@@ -156,6 +158,11 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     lib.gdp_mps_parse.restype = C.c_int
     lib.gdp_mps_free.argtypes = [C.POINTER(MpsProblem)]
     lib.gdp_mps_free.restype = None
+    _P_U64 = C.POINTER(C.c_ulonglong)
+    lib.gdp_phase_timers_read.argtypes = [_P_U64, _P_U64, _P_U64, C.c_int]
+    lib.gdp_phase_timers_read.restype = C.c_int
+    lib.gdp_phase_timers_clear.argtypes = []
+    lib.gdp_phase_timers_clear.restype = C.c_int
     lib.gdp_context_trace.argtypes = [C.c_void_p, _P_DBL, _P_DBL, C.c_int, _P_F, _P_F, C.POINTER(C.c_int),
                                       C.POINTER(Stats)]
     for name in ("gdp_mlp_create", "gdp_mlp_destroy", "gdp_mlp_get_params", "gdp_mlp_set_params",
@@ -167,7 +174,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
                  "gdp_propagate_once", "propagateConstraintsGPUAtomicDouble",
                  "propagateConstraintsGPUReductionDouble"):
         getattr(lib, name).restype = C.c_int
-    if path is None:
+    if path is None or make_default:
         _lib = lib
     return lib
 

@@ -270,6 +270,25 @@ GDP_RETCODE gdp_autotune(int n_cons, int n_vars, int nnz, const int *csr_col_ind
                          int *n_trials);
 GDP_RETCODE gdp_autotune_clear_cache(void);
 
+/* ---- phase timers (no counterpart in the reference) ----------------------
+ * Where a MEGAKERNEL propagation spends its time, from a library built with
+ * GDP_PHASE_TIMERS (build.py --phase-timers, libgdp_gb300_timers.so; the plain
+ * library returns GDP_NOTIMPLEMENTED). Per round r (0 <= r < rounds, at most
+ * 1024; round numbers start at 1), 8 values each:
+ *   wall[8r + k]: %globaltimer ns at the round's start (k = 0) and after the
+ *     grid barriers of phase A (1), B (2), C (3, rounds with exact tiles) and
+ *     F (4); k = 5..7: rows, non-zeros and exact non-zeros processed so far;
+ *   busy[8r + k]: warp ns summed over all warps in phase A (0), B multi-tile
+ *     rows (1), B deferred exact rows (2), C (3), F (4);
+ *   pass[2 lg + i] (16 values, all rounds): warp ns of the exact pass of rows
+ *     summed by 2^lg lanes, pass 1 (i = 0, activities and row test) and pass 2
+ *     (i = 1, candidates).
+ * Any output may be NULL. The timers accumulate over propagations until
+ * gdp_phase_timers_clear; they are device globals of the current device. */
+GDP_RETCODE gdp_phase_timers_clear(void);
+GDP_RETCODE gdp_phase_timers_read(unsigned long long *wall, unsigned long long *busy, unsigned long long *pass,
+                                  int rounds);
+
 /* ---- MPS reader (no counterpart in the reference, which reads MPS through
  * python-mip, fileReader/readerInterface.py:52-145) ---------------------------
  * Parses free-format MPS text (decompress .gz first) into the reference's CSR

@@ -72,6 +72,15 @@ def test_float_and_cpu_entry_points_not_implemented():
     assert "not implemented" in gdp.last_error()
 
 
+def test_phase_timers_only_in_the_timer_build():
+    """The plain library compiles no phase timers: both calls refuse without
+    touching the device."""
+    lib = gdp.load_library()
+    assert lib.gdp_phase_timers_clear() == gdp.GDP_NOTIMPLEMENTED
+    assert "GDP_PHASE_TIMERS" in gdp.last_error()
+    assert lib.gdp_phase_timers_read(None, None, None, 4) == gdp.GDP_NOTIMPLEMENTED
+
+
 def test_empty_problem_is_noop():
     # reference src/propagators/GPU_propagator.cuh:113-116
     lb, ub = gdp.propagateGPUAtomic(2, 0, 0, [], [0], [], [], [], [1.0, 2.0], [3.0, 4.0], [3, 3])

@@ -83,9 +83,13 @@ def test_learned_infeasible_detected():
 
 
 def test_train_on_traces_and_gain():
-    """Trace -> train on the GPU -> learned marking on a held-out seed: the same
-    certified fixpoint as plain, with fewer non-zeros processed than exact
-    marking (the method without the model) needs."""
+    """Trace -> train on the GPU -> learned marking on a held-out seed: the
+    same certified fixpoint as plain propagation (bit for bit on this
+    all-integer chain MIP), with less than half the non-zeros of the plain
+    full sweep every round (the reference's GPU schedule). Against exact
+    marking (the engine's own marking without the model) the learned rounds
+    process about as many non-zeros on such chains: that comparison is
+    printed, not asserted (bench.py reports it on the chain workload)."""
     import marking
     x, y = marking.collect_traces(gdpgen.chains(60_000, chain_max=90, seed=100 + s, frac_int_vars=1.0) for s in range(4))
     assert len(y) > 1000 and 0 < y.mean() < 1
