@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                 bits &= bits - 1;
                 const double2 b = Pu.bnd_nxt[j];
                 Pu.bnd[j] = b;
-                Pu.bnd32[j] = bnd_screen(b);
+                Pu.bnd32[j] = bnd_record(b, r);
                 if (var_infeasible(b.x, b.y)) {
                     Pu.flags[0].infeasible = 1;
                     atomicMin(&Pu.flags[0].infeasible_var, j);
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(256) k_batch_init(BatchDev B, const double *lb
         const double2 b = make_double2(lb[vb + j], ub[vb + j]);
         Pu.bnd[j] = b;
         Pu.bnd_nxt[j] = b;
-        Pu.bnd32[j] = bnd_screen(b);
+        Pu.bnd32[j] = bnd_record(b, 0);
         if (var_infeasible(b.x, b.y)) {
             Pu.flags[0].infeasible = 1;
             atomicMin(&Pu.flags[0].infeasible_var, j);

@@ -57,6 +57,17 @@ struct XRow {
 struct TileScr {
     float mn, mx, S, U;
     int minf, maxf;
+    int chg;  // a variable of the tile changed at the end of the previous round
+    int pad;
+};
+
+// The FP32 screen copy of a variable's bounds (bnd_screen) with the round at
+// whose end they were last committed (0: the input bounds), in one 16-byte
+// record: the screen's gather of the bounds brings the stamp in the same sector.
+struct __align__(16) BndScr {
+    float lb, ub;
+    int round;
+    int pad;
 };
 
 // Device-written round status. [0] is read by the host (CPU_LOOP), by the
@@ -163,16 +174,19 @@ struct DevProblem {
     unsigned *trace_n;
     unsigned trace_cap;
     int *mark;             // round in which the position is processed next (0: none)
-    // batched engine only (null otherwise): slice of each SELL row position and
-    // the round in which each slice was last queued
-    const int *pos_slice;  // n_srows
+    const int *pos_slice;  // n_srows: slice of each SELL row position
+    // batched engine only (null otherwise): the round in which each slice was last queued
     int *slice_stamp;      // n_slices
     const int *var_ptr;    // n + 1
     const int *var_pos;    // positions of each variable's rows
     // bounds
     double2 *bnd;          // current (lb, ub); read-only while a round runs
     double2 *bnd_nxt;      // next: FP64 min/max atomics
-    float2 *bnd32;         // FP32 screen copies of bnd (bnd_screen), refreshed with it
+    BndScr *bnd32;         // FP32 screen copies of bnd with their round stamps, refreshed with it
+    // 1: a row none of whose variables changed at the end of the previous round
+    // skips the exact pass (valid where every row with a changed variable is
+    // processed in the next round: full sweeps and exact marking, not deferral)
+    int pull_skip;
     const unsigned char *is_cont;
     unsigned *chg;         // changed-variable bitmap, n_chg_words words
     int n_chg_words;

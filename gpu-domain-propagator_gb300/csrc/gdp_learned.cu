@@ -70,7 +70,7 @@ __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round,
             bits &= bits - 1;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
-            P.bnd32[j] = bnd_screen(b);
+            P.bnd32[j] = bnd_record(b, round);
             if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_interleave(DevProblem P, const double *
         const double2 b = make_double2(lb[j], ub[j]);
         P.bnd[j] = b;
         P.bnd_nxt[j] = b;
-        P.bnd32[j] = bnd_screen(b);
+        P.bnd32[j] = bnd_record(b, 0);
     }
 }
 
@@ -129,9 +129,14 @@ __device__ __forceinline__ void timer_stamp(const DevProblem &P, int round, int 
     }
 }
 // adds the warp's time in phase k of round r since t0 (0: A, 1: B multi-tile
-// rows, 2: B deferred exact rows, 3: C, 4: F)
+// rows, 2: B deferred exact rows, 3: C, 4: F), and keeps the longest single
+// warp's time of the phase group in slot 5 (A), 6 (B) or 7 (C and F)
 __device__ __forceinline__ void timer_busy(int lane, int round, int k, unsigned long long t0) {
-    if (lane == 0 && round < kTimerRounds) atomicAdd(&g_timer_busy[round * kTimerSlots + k], timer_now() - t0);
+    if (lane == 0 && round < kTimerRounds) {
+        const unsigned long long dt = timer_now() - t0;
+        atomicAdd(&g_timer_busy[round * kTimerSlots + k], dt);
+        atomicMax(&g_timer_busy[round * kTimerSlots + (k == 0 ? 5 : k <= 2 ? 6 : 7)], dt);
+    }
 }
 #else
 __device__ __forceinline__ void timer_stamp(const DevProblem &, int, int) {}

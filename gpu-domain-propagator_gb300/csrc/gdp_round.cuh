@@ -76,7 +76,34 @@ __device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
 // Bounds are written by the finalize phase of the same megakernel launch, so
 // they are read with coherent loads (never the read-only path).
 __device__ __forceinline__ double2 load_bnd(const DevProblem &P, int j) { return P.bnd[j]; }
-__device__ __forceinline__ float2 load_bnd32(const DevProblem &P, int j) { return P.bnd32[j]; }
+__device__ __forceinline__ float2 load_bnd32(const DevProblem &P, int j) {
+    return *reinterpret_cast<const float2 *>(P.bnd32 + j);
+}
+// The screen copy of variable j's bounds, with chg set when the variable was
+// committed at the end of the round before `round` (one 16-byte load).
+__device__ __forceinline__ float2 load_bnd32_chg(const DevProblem &P, int j, int round, int &chg) {
+    const float4 v = *reinterpret_cast<const float4 *>(P.bnd32 + j);
+    chg |= __float_as_int(v.z) == round - 1 ? 1 : 0;
+    return make_float2(v.x, v.y);
+}
+__device__ __forceinline__ BndScr bnd_record(double2 b, int round) {
+    const float2 f = bnd_screen(b);
+    BndScr r;
+    r.lb = f.x;
+    r.ub = f.y;
+    r.round = round;
+    r.pad = 0;
+    return r;
+}
+// Whether a row the screen cannot skip takes the exact pass in `round`: a row
+// none of whose variables changed at the end of the previous round (chg == 0)
+// was last processed with the same bounds, so its activities and candidates
+// are those of that processing -- applied then, or not EPS-better than bounds
+// that have not moved since -- and it can neither tighten a bound nor turn
+// infeasible. Round 1 processes every row.
+__device__ __forceinline__ bool row_due(const DevProblem &P, int round, int chg) {
+    return chg != 0 || round <= 1 || !P.pull_skip || P.learned != 0;
+}
 
 // Row constants of tightenVariable (src/propagation_methods.cuh:223-276), with
 // float thresholds that decide most per-element EPS tests without FP64:
@@ -678,17 +705,21 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         const float *val = P.sell_a32 + base;
         Scr c;
         scr_init(c);
+        int chg = 0;
 #pragma unroll 4
         for (int i = 0; i < cnt; i++) {
             const int j = __ldcs(col + 32 * i);
             const float a = __ldcs(val + 32 * i);
-            scr_add(c, a, load_bnd32(P, j));
+            scr_add(c, a, load_bnd32_chg(P, j, round, chg));
         }
-        if (g > 1) scr_group_reduce(c, g);
+        if (g > 1) {
+            scr_group_reduce(c, g);
+            for (int off = g >> 1; off > 0; off >>= 1) chg |= __shfl_xor_sync(kFull, chg, off);
+        }
         if (leader) {
             lhs = __ldg(P.srow_lhs + r);
             rhs = __ldg(P.srow_rhs + r);
-            exact = !scr_skips(c, len, lhs, rhs);
+            exact = !scr_skips(c, len, lhs, rhs) && row_due(P, round, chg);
             if (exact) {
                 float hi;
                 scr_slack(c, len, lhs, rhs, slack_lo, hi);
@@ -746,8 +777,12 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
         mx = max(mx, len[k]);
     }
     Scr c[K];
+    int chg[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) scr_init(c[k]);
+    for (int k = 0; k < K; k++) {
+        scr_init(c[k]);
+        chg[k] = 0;
+    }
 #pragma unroll 2
     for (int i = 0; i < mx; i++) {
 #pragma unroll
@@ -755,7 +790,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
             if (i < len[k]) {
                 const int j = __ldcs(P.sell_col + base[k] + 32 * i);
                 const float a = __ldcs(P.sell_a32 + base[k] + 32 * i);
-                scr_add(c[k], a, load_bnd32(P, j));
+                scr_add(c[k], a, load_bnd32_chg(P, j, round, chg[k]));
             }
         }
     }
@@ -774,7 +809,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
     unsigned bal[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        exact[k] = act[k] && !scr_skips(c[k], len[k], lhs[k], rhs[k]);
+        exact[k] = act[k] && !scr_skips(c[k], len[k], lhs[k], rhs[k]) && row_due(P, round, chg[k]);
         slo[k] = 0.0f;
         if (exact[k]) {
             float hi;
@@ -810,8 +845,13 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
         const int g = 1 << lg, per = 32 >> lg;
         const int rl = lane >> lg, sub = lane & (g - 1);
         for (;;) {
+            // claims only grow: a class already claimed to its end is left
+            // without an atomic (every warp of the grid passes each class)
             unsigned k0 = 0;
-            if (lane == 0) k0 = atomicAdd(P.xctr + 16 * par + 8 + lg, (unsigned)per);
+            if (lane == 0) {
+                k0 = *((volatile unsigned *)(P.xctr + 16 * par + 8 + lg));
+                if (k0 < (unsigned)n) k0 = atomicAdd(P.xctr + 16 * par + 8 + lg, (unsigned)per);
+            }
             const int k = (int)__shfl_sync(kFull, k0, 0) + rl;
             if (k - rl >= n) break;
             const bool exact = k < n;
@@ -979,13 +1019,15 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
     Scr c;
     scr_init(c);
+    int chg = 0;
 #pragma unroll 4
     for (int k = b + lane; k < e; k += 32) {
         const int j = __ldcs(P.lcol + k);
         const float a = __ldcs(P.la32 + k);
-        scr_add(c, a, load_bnd32(P, j));
+        scr_add(c, a, load_bnd32_chg(P, j, round, chg));
     }
     scr_shfl_reduce(c);
+    chg = __any_sync(kFull, chg) ? 1 : 0;
     const int t0 = __ldg(P.lrow_tile0 + row);
     const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
     int exact = 0;
@@ -993,11 +1035,14 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
         ws.st_nnz += (unsigned long long)(e - b);
         if (t == t0) ws.st_rows += 1ULL;
         if (single) {
-            exact = !scr_skips(c, e - b, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+            exact = !scr_skips(c, e - b, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) &&
+                    row_due(P, round, chg);
             if (exact) ws.st_exact += (unsigned long long)(e - b);
         } else {
             TileScr ts;
             ts.mn = c.mn; ts.mx = c.mx; ts.S = c.S; ts.U = c.U; ts.minf = c.minf; ts.maxf = c.maxf;
+            ts.chg = chg;
+            ts.pad = 0;
             P.tile_scr[t] = ts;
         }
     }
@@ -1020,17 +1065,20 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
     const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
     Scr c;
     scr_init(c);
+    int chg = 0;
     for (int u = t0 + lane; u < t1; u += 32) {
         const TileScr p = P.tile_scr[u];
         Scr o;
         o.mn = p.mn; o.mx = p.mx; o.S = p.S; o.U = p.U; o.minf = p.minf; o.maxf = p.maxf;
         scr_combine(c, o);
+        chg |= p.chg;
     }
     scr_shfl_reduce(c);
+    chg = __any_sync(kFull, chg) ? 1 : 0;
     int exact = 0;
     if (lane == 0) {
         const int n_row = __ldg(P.tile_end + t1 - 1) - __ldg(P.tile_begin + t0);
-        exact = !scr_skips(c, n_row, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row));
+        exact = !scr_skips(c, n_row, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) && row_due(P, round, chg);
     }
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
@@ -1109,7 +1157,7 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
             const int j = w * 32 + lane;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
-            P.bnd32[j] = bnd_screen(b);
+            P.bnd32[j] = bnd_record(b, round);
             if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);
@@ -1179,24 +1227,52 @@ __device__ __forceinline__ void activity_phase(const DevProblem &P, int round, b
     stats_flush(P, ws, lane);
 }
 
+// The grid's warps: this warp's index and their number.
+__device__ __forceinline__ int grid_warp() { return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
+__device__ __forceinline__ int grid_warps() { return (int)((gridDim.x * blockDim.x) >> 5); }
+
+// Candidate phase over the tiles of multi-tile rows: warp w takes the tiles
+// w, w + W, ... (W warps), one per lane per step, and runs those whose row is
+// due (every tile in an unmarked round, the tiles of marked rows otherwise).
+// The tiles hold at most split_tile non-zeros each and the deferred exact rows
+// that follow in the same phase are claimed dynamically, so a static
+// assignment costs no balance and saves a contended claim per tile.
 __device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, bool marked, unsigned *ctr,
                                                 int *exact_ctr, WarpSmem &ws, int lane) {
+    (void)ctr;
     stats_zero(ws, lane);
-    for (;;) {
-        const int i = warp_next(ctr, lane);
-        if (i >= P.n_mtiles) break;
-        split_cand(P, __ldg(P.mtiles + i), lane, round, marked, exact_ctr, ws);
+    const int nw = grid_warps();
+    for (int i0 = grid_warp(); i0 < P.n_mtiles; i0 += 32 * nw) {
+        const int i = i0 + lane * nw;
+        int t = 0;
+        bool live = false;
+        if (i < P.n_mtiles) {
+            t = __ldg(P.mtiles + i);
+            live = !marked || P.mark[P.n_srows + __ldg(P.tile_row + t)] == round;
+        }
+        for (unsigned bal = __ballot_sync(kFull, live); bal; bal &= bal - 1)
+            split_cand(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, false, exact_ctr, ws);
     }
     stats_flush(P, ws, lane);
 }
 
+// Exact phase over the tiles of the multi-tile rows flagged this round, with
+// the same static assignment as the candidate phase.
 __device__ __forceinline__ void exact_phase(const DevProblem &P, int round, unsigned *ctr, int *change,
                                             unsigned *tight_ctr, WarpSmem &ws, int lane) {
+    (void)ctr;
     stats_zero(ws, lane);
-    for (;;) {
-        const int i = warp_next(ctr, lane);
-        if (i >= P.n_mtiles) break;
-        split_exact(P, __ldg(P.mtiles + i), lane, round, change, tight_ctr, ws);
+    const int nw = grid_warps();
+    for (int i0 = grid_warp(); i0 < P.n_mtiles; i0 += 32 * nw) {
+        const int i = i0 + lane * nw;
+        int t = 0;
+        bool live = false;
+        if (i < P.n_mtiles) {
+            t = __ldg(P.mtiles + i);
+            live = P.row_exact[__ldg(P.tile_row + t)] == round;
+        }
+        for (unsigned bal = __ballot_sync(kFull, live); bal; bal &= bal - 1)
+            split_exact(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, change, tight_ctr, ws);
     }
     stats_flush(P, ws, lane);
 }

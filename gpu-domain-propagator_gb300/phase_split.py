@@ -12,7 +12,9 @@ n = 1,500,000 variables, Zipf(1.8) row lengths in [2, 20000] plus 32 rows of
     the number of warps), which shows how full each phase keeps the GPU;
   * warp time of the two passes of the exact pass of SELL rows by lane-group
     size (pass 1: FP64 activities and the row test; pass 2: candidates);
-  * with --per-round, one line per round with the work it processed.
+  * with --per-round, one line per round with the work it processed and, per
+    phase group, the average warp's busy time and the longest single warp's
+    (a long pole shows as a maximum near the phase's wall time).
 
     python gpu-domain-propagator_gb300/phase_split.py [--scale 1.0] [--per-round]
 
@@ -59,11 +61,11 @@ def read_timers(lib, rounds: int):
 
 
 def split(scale: float = 1.0, seed: int = 1000, warmup: int = 3, per_round: bool = False,
-          cta_threads: int = 256, keep_bounds: bool = False) -> dict:
+          cta_threads: int = 256, keep_bounds: bool = False, use_marking: int = -1) -> dict:
     so = _build.build(phase_timers=True)["gdp"]
     lib = gdp.load_library(so, make_default=True)
     mip = workload(scale, seed)
-    ctx = gdp.Context(mip, sync_type=gdp.MEGAKERNEL, cta_threads=cta_threads)
+    ctx = gdp.Context(mip, sync_type=gdp.MEGAKERNEL, cta_threads=cta_threads, use_marking=use_marking)
     ms = [ctx.propagate()[2]["device_ms"] for _ in range(warmup)]
     if lib.gdp_phase_timers_clear() != gdp.GDP_OKAY:
         raise gdp.GDPError(gdp.last_error())
@@ -75,6 +77,10 @@ def split(scale: float = 1.0, seed: int = 1000, warmup: int = 3, per_round: bool
     b = wall[:, 2] - wall[:, 1]
     cf = wall[:, 4] - wall[:, 2]  # C (when present) and F
     busy_ms = {k: float(busy[:, i].sum()) / warps / 1e6 for i, k in enumerate(PHASES)}
+    # per round: the average warp's busy time and the longest single warp's, by phase group
+    avg_a = busy[:, 0] / warps
+    avg_b = (busy[:, 1] + busy[:, 2]) / warps
+    avg_cf = (busy[:, 3] + busy[:, 4]) / warps
     total_busy = sum(busy_ms.values())
     out = {
         "workload": f"power-law MIP m={mip.m} n={mip.n} nnz={mip.nnz} seed={seed}",
@@ -96,7 +102,10 @@ def split(scale: float = 1.0, seed: int = 1000, warmup: int = 3, per_round: bool
             d = wall[r, 5:8] - prev
             prev = wall[r, 5:8]
             lines.append({"round": r + 1, "A_us": a[r] / 1e3, "B_us": b[r] / 1e3, "CF_us": cf[r] / 1e3,
-                          "rows": int(d[0]), "nnz": int(d[1]), "nnz_exact": int(d[2])})
+                          "rows": int(d[0]), "nnz": int(d[1]), "nnz_exact": int(d[2]),
+                          "A_avg_us": avg_a[r] / 1e3, "A_max_us": busy[r, 5] / 1e3,
+                          "B_avg_us": avg_b[r] / 1e3, "B_max_us": busy[r, 6] / 1e3,
+                          "CF_avg_us": avg_cf[r] / 1e3, "CF_max_us": busy[r, 7] / 1e3})
         out["per_round"] = lines
     if keep_bounds:
         out["lb"], out["ub"] = lb, ub
@@ -110,13 +119,17 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--per-round", action="store_true")
     ap.add_argument("--cta-threads", type=int, default=256, choices=[128, 256, 512])
+    ap.add_argument("--marking", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="-1: library default; 0: full sweeps; 1: adaptive; 2: marked rows every round")
     args = ap.parse_args(argv)
-    res = split(args.scale, args.seed, args.warmup, args.per_round, args.cta_threads)
+    res = split(args.scale, args.seed, args.warmup, args.per_round, args.cta_threads, use_marking=args.marking)
     rounds = res.pop("per_round", None)
     print(json.dumps(res, indent=1))
     for r in rounds or []:
         print(f"round {r['round']:4d}  A {r['A_us']:8.1f} us  B {r['B_us']:8.1f} us  C+F {r['CF_us']:7.1f} us  "
-              f"rows {r['rows']:9d}  nnz {r['nnz']:11d}  exact nnz {r['nnz_exact']:10d}")
+              f"rows {r['rows']:9d}  nnz {r['nnz']:11d}  exact nnz {r['nnz_exact']:10d}  "
+              f"warp avg/max: A {r['A_avg_us']:6.1f}/{r['A_max_us']:6.1f}  B {r['B_avg_us']:6.1f}/{r['B_max_us']:6.1f}  "
+              f"C+F {r['CF_avg_us']:5.1f}/{r['CF_max_us']:5.1f}")
     return 0
 
 

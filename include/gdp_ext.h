@@ -279,7 +279,8 @@ GDP_RETCODE gdp_autotune_clear_cache(void);
  *     grid barriers of phase A (1), B (2), C (3, rounds with exact tiles) and
  *     F (4); k = 5..7: rows, non-zeros and exact non-zeros processed so far;
  *   busy[8r + k]: warp ns summed over all warps in phase A (0), B multi-tile
- *     rows (1), B deferred exact rows (2), C (3), F (4);
+ *     rows (1), B deferred exact rows (2), C (3), F (4); k = 5..7: the longest
+ *     time of one warp in one of A (5), B's two parts (6), C or F (7);
  *   pass[2 lg + i] (16 values, all rounds): warp ns of the exact pass of rows
  *     summed by 2^lg lanes, pass 1 (i = 0, activities and row test) and pass 2
  *     (i = 1, candidates).
