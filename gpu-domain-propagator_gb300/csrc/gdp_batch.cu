@@ -258,19 +258,19 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                     if (it >= 0) {
                         if (lane == 0) L.marked = 0;
                         __syncwarp();
-                        const bool deferred = sell_slice_learned(Pu, it, lane, r, kind, change, tight, mine, L);
+                        const bool deferred = sell_slice_learned<0>(Pu, it, lane, r, kind, change, tight, mine, L);
                         if (lane == 0) {
                             if (L.marked) atomicAdd(&Pu.flags[1 + par].rows_deferred, L.marked);
                             if (deferred && r < B.max_rounds && atomicExch(Pu.slice_stamp + it, r + 1) != r + 1)
                                 push_entry(B, par ^ 1, u, it);
                         }
-                    } else if (split_partial(Pu, -it - 1, lane, r, kind != kRoundFull, change, tight, mine) &&
+                    } else if (split_partial<0>(Pu, -it - 1, lane, r, kind != kRoundFull, change, tight, mine) &&
                                lane == 0) {
                         push_tile(B.cq, B.tail + 2, B.cap_tiles, B.error, u, -it - 1);
                     }
                 } else if (it >= 0) {
-                    sell_slice(Pu, it, lane, r, marked, change, tight, mine);
-                } else if (split_partial(Pu, -it - 1, lane, r, marked, change, tight, mine) && lane == 0) {
+                    sell_slice<0>(Pu, it, lane, r, marked, change, tight, mine);
+                } else if (split_partial<0>(Pu, -it - 1, lane, r, marked, change, tight, mine) && lane == 0) {
                     push_tile(B.cq, B.tail + 2, B.cap_tiles, B.error, u, -it - 1);
                 }
                 stats_flush(Pu, mine, lane);  // statistics belong to the item's unit
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                 const unsigned long long e = B.cq[i];
                 const int u = (int)(e >> 32), t = (int)(unsigned)e;
                 const DevProblem &Pu = B.units[u];
-                if (split_cand(Pu, t, lane, r, false, &Pu.flags[1 + par].exact, mine) && lane == 0)
+                if (split_cand<0>(Pu, t, lane, r, false, &Pu.flags[1 + par].exact, mine) && lane == 0)
                     push_tile(B.xq, B.tail + 3, B.cap_tiles, B.error, u, t);
                 stats_flush(Pu, mine, lane);
             }
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                     const unsigned long long e = B.xq[i];
                     const int u = (int)(e >> 32), t = (int)(unsigned)e;
                     const DevProblem &Pu = B.units[u];
-                    split_exact(Pu, t, lane, r, &Pu.flags[1 + par].change, &Pu.flags[1 + par].tight, mine);
+                    split_exact<0>(Pu, t, lane, r, &Pu.flags[1 + par].change, &Pu.flags[1 + par].tight, mine);
                     stats_flush(Pu, mine, lane);
                 }
                 if (!grid_barrier(B.barrier, B.error, B.spin_limit)) return;
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) k_batch_loop(BatchDev B) {
                 bits &= bits - 1;
                 const double2 b = Pu.bnd_nxt[j];
                 Pu.bnd[j] = b;
-                Pu.bnd32[j] = bnd_record(b, r);
+                store_bnd32<0>(Pu, j, b, r);
                 if (var_infeasible(b.x, b.y)) {
                     Pu.flags[0].infeasible = 1;
                     atomicMin(&Pu.flags[0].infeasible_var, j);
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(256) k_batch_init(BatchDev B, const double *lb
         const double2 b = make_double2(lb[vb + j], ub[vb + j]);
         Pu.bnd[j] = b;
         Pu.bnd_nxt[j] = b;
-        Pu.bnd32[j] = bnd_record(b, 0);
+        store_bnd32<0>(Pu, j, b, 0);
         if (var_infeasible(b.x, b.y)) {
             Pu.flags[0].infeasible = 1;
             atomicMin(&Pu.flags[0].infeasible_var, j);

@@ -69,7 +69,6 @@ GDP_RETCODE Batch::init_instances(int n_inst, const int *n_cons, const int *n_va
     for (int u = 0; u < n_units; u++) {
         units_h_[u] = inst_[u]->P;
         units_h_[u].defer_exact = 0;  // the batch loop runs exact passes in place
-        units_h_[u].pull_skip = 0;    // members are processed as their own schedule has it
     }
     // per-unit batch state: slice stamps
     for (int u = 0; u < n_units; u++) {
@@ -96,15 +95,12 @@ GDP_RETCODE Batch::init_nodes(Context *ctx, int n_nodes) {
     const DevProblem &S = ctx->P;
     const int n = std::max(S.n, 1), npos = std::max(S.n_srows + S.n_lrows, 1);
     units_h_.assign(n_units, S);
-    for (int u = 0; u < n_units; u++) {
-        units_h_[u].defer_exact = 0;  // exact passes run in place
-        units_h_[u].pull_skip = 0;
-    }
+    for (int u = 0; u < n_units; u++) units_h_[u].defer_exact = 0;  // exact passes run in place
     for (int u = 0; u < n_units; u++) {
         DevProblem &Q = units_h_[u];
         Q.bnd = (double2 *)arena_.alloc_bytes(sizeof(double2) * (size_t)n);
         Q.bnd_nxt = (double2 *)arena_.alloc_bytes(sizeof(double2) * (size_t)n);
-        Q.bnd32 = (BndScr *)arena_.alloc_bytes(sizeof(BndScr) * (size_t)n);
+        Q.bnd32 = (float2 *)arena_.alloc_bytes(sizeof(float2) * (size_t)n);  // 8-byte copies
         Q.chg = (unsigned *)arena_.alloc_bytes(sizeof(unsigned) * (size_t)std::max(S.n_chg_words, 1));
         Q.mark = (int *)arena_.alloc_bytes(sizeof(int) * (size_t)npos);
         Q.slice_stamp = (int *)arena_.alloc_bytes(sizeof(int) * (size_t)std::max(S.n_slices, 1));

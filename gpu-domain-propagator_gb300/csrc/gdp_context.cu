@@ -647,8 +647,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);
     P.bnd = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
     P.bnd_nxt = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
-    P.bnd32 = (BndScr *)arena.alloc_bytes(sizeof(BndScr) * (size_t)std::max(n, 1));
-    P.pull_skip = 1;
+    P.bnd32 = (float2 *)arena.alloc_bytes(sizeof(BndScr) * (size_t)std::max(n, 1));  // stamped records
     P.chg = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * (size_t)std::max(n_words, 1));
     P.n_chg_words = n_words;
     P.flags = (RoundFlags *)arena.alloc_bytes(sizeof(RoundFlags) * 3);

@@ -64,6 +64,7 @@ struct TileScr {
 // The FP32 screen copy of a variable's bounds (bnd_screen) with the round at
 // whose end they were last committed (0: the input bounds), in one 16-byte
 // record: the screen's gather of the bounds brings the stamp in the same sector.
+// Batch members keep the 8-byte copies alone.
 struct __align__(16) BndScr {
     float lb, ub;
     int round;
@@ -182,11 +183,10 @@ struct DevProblem {
     // bounds
     double2 *bnd;          // current (lb, ub); read-only while a round runs
     double2 *bnd_nxt;      // next: FP64 min/max atomics
-    BndScr *bnd32;         // FP32 screen copies of bnd with their round stamps, refreshed with it
-    // 1: a row none of whose variables changed at the end of the previous round
-    // skips the exact pass (valid where every row with a changed variable is
-    // processed in the next round: full sweeps and exact marking, not deferral)
-    int pull_skip;
+    // FP32 screen copies of bnd, refreshed with it: BndScr records (bounds and
+    // round stamp, 16 bytes) in single-problem contexts, float2 copies (8
+    // bytes) in batch members
+    float2 *bnd32;
     const unsigned char *is_cont;
     unsigned *chg;         // changed-variable bitmap, n_chg_words words
     int n_chg_words;

@@ -46,8 +46,8 @@ __device__ __forceinline__ void learned_activity_phase(const DevProblem &P, int 
         const int i = cur.next(lane);
         if (i >= P.n_items) break;
         const int it = __ldg(P.items + i);
-        if (it >= 0) sell_slice_learned(P, it, lane, round, kind, change, tight_ctr, ws, L);
-        else split_partial(P, -it - 1, lane, round, kind != kRoundFull, change, tight_ctr, ws);
+        if (it >= 0) sell_slice_learned<1>(P, it, lane, round, kind, change, tight_ctr, ws, L);
+        else split_partial<1>(P, -it - 1, lane, round, kind != kRoundFull, change, tight_ctr, ws);
     }
     stats_flush(P, ws, lane);
     if (lane == 0 && L.marked) atomicAdd(marked_ctr, L.marked);
@@ -70,7 +70,7 @@ __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round,
             bits &= bits - 1;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
-            P.bnd32[j] = bnd_record(b, round);
+            store_bnd32<1>(P, j, b, round);
             if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);

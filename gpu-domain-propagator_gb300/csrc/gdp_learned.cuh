@@ -56,6 +56,7 @@ enum RoundKind : int { kRoundFull = 0, kRoundLearned = 1, kRoundFlush = 2 };
 
 // One SELL-g slice in a round of the given kind. Returns true when the model
 // deferred marked rows of the slice (they stay dirty for a later round).
+template <int kRec>  // the bnd32 layout (load_bnd32): 1 in contexts, 0 in batch members
 __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slice, int lane, int round, int kind,
                                                    int *change, unsigned *tight_ctr, WarpSmem &ws,
                                                    LearnSmem &L) {
@@ -159,7 +160,7 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
         for (int i = 0; i < cnt; i++) {
             const int j = __ldcs(col + 32 * i);
             const float a = __ldcs(val + 32 * i);
-            scr_add(c, a, load_bnd32(P, j));
+            scr_add(c, a, load_bnd32<kRec>(P, j));
         }
     }
     if (g > 1) scr_group_reduce(c, g);
@@ -180,7 +181,7 @@ __device__ __forceinline__ bool sell_slice_learned(const DevProblem &P, int slic
     if (__any_sync(kFull, exact)) {
         ws.base[lane] = base;
         __syncwarp();
-        sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, r, slack_lo, change, tight_ctr, ws,
+        sell_rows_exact<kRec>(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, r, slack_lo, change, tight_ctr, ws,
                         L.tight, L.go);
     }
     __syncwarp();

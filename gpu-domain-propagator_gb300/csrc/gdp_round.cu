@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_interleave(DevProblem P, const double *
         const double2 b = make_double2(lb[j], ub[j]);
         P.bnd[j] = b;
         P.bnd_nxt[j] = b;
-        P.bnd32[j] = bnd_record(b, 0);
+        store_bnd32<1>(P, j, b, 0);
     }
 }
 

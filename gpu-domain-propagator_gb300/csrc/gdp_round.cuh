@@ -76,33 +76,43 @@ __device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
 // Bounds are written by the finalize phase of the same megakernel launch, so
 // they are read with coherent loads (never the read-only path).
 __device__ __forceinline__ double2 load_bnd(const DevProblem &P, int j) { return P.bnd[j]; }
+// The layout of bnd32 is fixed per kernel: kRec = 1, the stamped 16-byte
+// records (BndScr) of single-problem contexts -- the round loops of the
+// megakernel, the phase kernels and learned marking; kRec = 0, the 8-byte
+// copies of batch members.
+// Variable j's screen copy of its bounds.
+template <int kRec>
 __device__ __forceinline__ float2 load_bnd32(const DevProblem &P, int j) {
-    return *reinterpret_cast<const float2 *>(P.bnd32 + j);
+    return P.bnd32[kRec ? 2 * (long long)j : j];
 }
 // The screen copy of variable j's bounds, with chg set when the variable was
-// committed at the end of the round before `round` (one 16-byte load).
+// committed at the end of the round before `round` (one 16-byte load of the
+// stamped record; copies without stamps leave chg alone).
+template <int kRec>
 __device__ __forceinline__ float2 load_bnd32_chg(const DevProblem &P, int j, int round, int &chg) {
-    const float4 v = *reinterpret_cast<const float4 *>(P.bnd32 + j);
+    if (!kRec) return P.bnd32[j];
+    const float4 v = reinterpret_cast<const float4 *>(P.bnd32)[j];
     chg |= __float_as_int(v.z) == round - 1 ? 1 : 0;
     return make_float2(v.x, v.y);
 }
-__device__ __forceinline__ BndScr bnd_record(double2 b, int round) {
+// Stores variable j's screen copy of bounds b committed at the end of `round`.
+template <int kRec>
+__device__ __forceinline__ void store_bnd32(const DevProblem &P, int j, double2 b, int round) {
     const float2 f = bnd_screen(b);
-    BndScr r;
-    r.lb = f.x;
-    r.ub = f.y;
-    r.round = round;
-    r.pad = 0;
-    return r;
+    if (kRec) reinterpret_cast<float4 *>(P.bnd32)[j] = make_float4(f.x, f.y, __int_as_float(round), 0.0f);
+    else P.bnd32[j] = f;
 }
 // Whether a row the screen cannot skip takes the exact pass in `round`: a row
 // none of whose variables changed at the end of the previous round (chg == 0)
 // was last processed with the same bounds, so its activities and candidates
 // are those of that processing -- applied then, or not EPS-better than bounds
 // that have not moved since -- and it can neither tighten a bound nor turn
-// infeasible. Round 1 processes every row.
+// infeasible. Round 1 processes every row. Valid where every row with a
+// changed variable is processed in the next round (full sweeps and exact
+// marking): not under learned deferral, and only with stamped records.
+template <int kRec>
 __device__ __forceinline__ bool row_due(const DevProblem &P, int round, int chg) {
-    return chg != 0 || round <= 1 || !P.pull_skip || P.learned != 0;
+    return chg != 0 || round <= 1 || !kRec || P.learned != 0;
 }
 
 // Row constants of tightenVariable (src/propagation_methods.cuh:223-276), with
@@ -481,6 +491,7 @@ __device__ __forceinline__ ElemView sell_view(const DevProblem &P) {
 //           reference's row test, and every row is checked for row-side
 //           infeasibility.
 //   pass 2: candidates through the warp division queue.
+template <int kRec>
 __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemView ev, int lg, int lane,
                                                 bool exact, int len,
                                                 int cnt, double lhs, double rhs, int pos, float slack_lo,
@@ -625,7 +636,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
             float2 b1 = make_float2(0.0f, 0.0f);
             if (rem) { i1 = __ffs(rem) - 1; rem &= rem - 1; j1 = __ldg(col + st * i1); a1 = __ldg(a32 + st * i1); }
             if (rem) { i2 = __ffs(rem) - 1; rem &= rem - 1; j2 = __ldg(col + st * i2); a2 = __ldg(a32 + st * i2); }
-            if (i1 >= 0) b1 = load_bnd32(P, j1);
+            if (i1 >= 0) b1 = load_bnd32<kRec>(P, j1);
             for (int t = 0; t < nvis; t++) {
                 const int i = i1, j = j1;
                 const float a = a1;
@@ -633,7 +644,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
                 i1 = i2; j1 = j2; a1 = a2;
                 i2 = -1;
                 if (rem) { i2 = __ffs(rem) - 1; rem &= rem - 1; j2 = __ldg(col + st * i2); a2 = __ldg(a32 + st * i2); }
-                if (i1 >= 0) b1 = load_bnd32(P, j1);
+                if (i1 >= 0) b1 = load_bnd32<kRec>(P, j1);
                 int sides = i >= 0 ? candidate_sides32(ws.rc[rl], a, b) : 0;
                 if (sides & 4) {
                     const double2 bd = load_bnd(P, j);
@@ -649,7 +660,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
             float2 b1 = make_float2(0.0f, 0.0f);
             if (ce > 0) { j1 = __ldg(col); a1 = __ldg(a32); }
             if (ce > 1) { j2 = __ldg(col + st); a2 = __ldg(a32 + st); }
-            if (ce > 0) b1 = load_bnd32(P, j1);
+            if (ce > 0) b1 = load_bnd32<kRec>(P, j1);
             for (int i = 0; i < maxcnt; i++) {
                 const int j = j1;
                 const float a = a1;
@@ -657,7 +668,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
                 j1 = j2;
                 a1 = a2;
                 if (i + 2 < ce) { j2 = __ldg(col + st * (i + 2)); a2 = __ldg(a32 + st * (i + 2)); }
-                if (i + 1 < ce) b1 = load_bnd32(P, j1);
+                if (i + 1 < ce) b1 = load_bnd32<kRec>(P, j1);
                 int sides = i < ce ? candidate_sides32(ws.rc[rl], a, b) : 0;
                 if (sides & 4) {
                     const double2 bd = load_bnd(P, j);
@@ -679,6 +690,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
 // column-major (step i of lane l at slice_ptr[slice] + 32 i + l).
 // The FP32 screen runs here; rows it cannot skip take the exact pass in place
 // or, with P.defer_exact, are queued for the exact-rows phase.
+template <int kRec>
 __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int lane, int round, bool marked,
                                            int *change, unsigned *tight_ctr, WarpSmem &ws, int par = 0) {
     const int lg = __ldg(P.slice_lg + slice);
@@ -710,7 +722,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         for (int i = 0; i < cnt; i++) {
             const int j = __ldcs(col + 32 * i);
             const float a = __ldcs(val + 32 * i);
-            scr_add(c, a, load_bnd32_chg(P, j, round, chg));
+            scr_add(c, a, load_bnd32_chg<kRec>(P, j, round, chg));
         }
         if (g > 1) {
             scr_group_reduce(c, g);
@@ -719,7 +731,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
         if (leader) {
             lhs = __ldg(P.srow_lhs + r);
             rhs = __ldg(P.srow_rhs + r);
-            exact = !scr_skips(c, len, lhs, rhs) && row_due(P, round, chg);
+            exact = !scr_skips(c, len, lhs, rhs) && row_due<kRec>(P, round, chg);
             if (exact) {
                 float hi;
                 scr_slack(c, len, lhs, rhs, slack_lo, hi);
@@ -740,7 +752,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
     if (!__any_sync(kFull, exact)) return;
     ws.base[lane] = base;
     __syncwarp();
-    sell_rows_exact(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, r, slack_lo, change, tight_ctr, ws);
+    sell_rows_exact<kRec>(P, sell_view(P), lg, lane, exact, len, cnt, lhs, rhs, r, slack_lo, change, tight_ctr, ws);
 }
 
 // K slices of one-lane rows (g = 1) screened together in the deferred-exact
@@ -750,7 +762,7 @@ __device__ __forceinline__ void sell_slice(const DevProblem &P, int slice, int l
 // waiting), and the exact rows of all K slices are queued with one counter
 // update. Decisions and queue contents equal those of K sell_slice calls.
 constexpr int kScreenGroup = 2;
-template <int K>
+template <int K, int kRec>
 __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&sl)[K], int lane, int round,
                                                bool marked, WarpSmem &ws, int par) {
     int r[K], len[K];
@@ -790,7 +802,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
             if (i < len[k]) {
                 const int j = __ldcs(P.sell_col + base[k] + 32 * i);
                 const float a = __ldcs(P.sell_a32 + base[k] + 32 * i);
-                scr_add(c[k], a, load_bnd32_chg(P, j, round, chg[k]));
+                scr_add(c[k], a, load_bnd32_chg<kRec>(P, j, round, chg[k]));
             }
         }
     }
@@ -809,7 +821,7 @@ __device__ __forceinline__ void sell_slices_g1(const DevProblem &P, const int (&
     unsigned bal[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        exact[k] = act[k] && !scr_skips(c[k], len[k], lhs[k], rhs[k]) && row_due(P, round, chg[k]);
+        exact[k] = act[k] && !scr_skips(c[k], len[k], lhs[k], rhs[k]) && row_due<kRec>(P, round, chg[k]);
         slo[k] = 0.0f;
         if (exact[k]) {
             float hi;
@@ -874,7 +886,7 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
             }
             ws.base[lane] = base;
             __syncwarp();
-            sell_rows_exact(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, pos,
+            sell_rows_exact<1>(P, ElemView{P.xcol, P.xval, P.xa32, g}, lg, lane, exact, len, cnt, lhs, rhs, pos,
                             slack_lo, change, tight_ctr, ws);
             __syncwarp();
         }
@@ -902,6 +914,7 @@ __device__ __forceinline__ void acc_shfl_reduce(Acc &s) {
 // [b, e) of one tile, from the row's complete activities and first maximum
 // held by lane 0; the warp queues the divisions. The row's first tile also
 // checks it for row-side infeasibility.
+template <int kRec>
 __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int row, int b, int e, const Acc &s0,
                                                      int lane, int *change, unsigned *tight_ctr, WarpSmem &ws) {
     RowC c;
@@ -952,7 +965,7 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
     float2 b1 = make_float2(0.0f, 0.0f);
     if (b + lane < e) { j1 = __ldg(P.lcol + b + lane); a1 = __ldg(P.la32 + b + lane); }
     if (b + 32 + lane < e) { j2 = __ldg(P.lcol + b + 32 + lane); a2 = __ldg(P.la32 + b + 32 + lane); }
-    if (b + lane < e) b1 = load_bnd32(P, j1);
+    if (b + lane < e) b1 = load_bnd32<kRec>(P, j1);
     for (int k0 = b; k0 < e; k0 += 32) {
         const int k = k0 + lane;
         const int j = j1;
@@ -961,7 +974,7 @@ __device__ __forceinline__ void split_row_candidates(const DevProblem &P, int ro
         j1 = j2;
         a1 = a2;
         if (k + 64 < e) { j2 = __ldg(P.lcol + k + 64); a2 = __ldg(P.la32 + k + 64); }
-        if (k + 32 < e) b1 = load_bnd32(P, j1);
+        if (k + 32 < e) b1 = load_bnd32<kRec>(P, j1);
         int sides = k < e ? candidate_sides32(c, a, bb) : 0;
         if (sides & 4) {
             const double2 bd = load_bnd(P, j);
@@ -1012,6 +1025,7 @@ __device__ __forceinline__ Acc tile_exact(const DevProblem &P, int b, int e, int
 // fits in one tile is finished here (screen decision, exact pass, candidates);
 // tiles of longer rows store their screen partial for the candidate phase
 // (returns true for those).
+template <int kRec>
 __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int lane, int round, bool marked,
                                               int *change, unsigned *tight_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
@@ -1024,7 +1038,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     for (int k = b + lane; k < e; k += 32) {
         const int j = __ldcs(P.lcol + k);
         const float a = __ldcs(P.la32 + k);
-        scr_add(c, a, load_bnd32_chg(P, j, round, chg));
+        scr_add(c, a, load_bnd32_chg<kRec>(P, j, round, chg));
     }
     scr_shfl_reduce(c);
     chg = __any_sync(kFull, chg) ? 1 : 0;
@@ -1036,7 +1050,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
         if (t == t0) ws.st_rows += 1ULL;
         if (single) {
             exact = !scr_skips(c, e - b, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) &&
-                    row_due(P, round, chg);
+                    row_due<kRec>(P, round, chg);
             if (exact) ws.st_exact += (unsigned long long)(e - b);
         } else {
             TileScr ts;
@@ -1049,7 +1063,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     if (!single) return true;
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const Acc s = tile_exact(P, b, e, b, lane);
-    split_row_candidates(P, row, b, e, s, lane, change, tight_ctr, ws);
+    split_row_candidates<kRec>(P, row, b, e, s, lane, change, tight_ctr, ws);
     return false;
 }
 
@@ -1058,6 +1072,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
 // reaches the same decision); a row the screen cannot skip gets this tile's
 // exact FP64 partial, and its first tile flags the row for the exact phase
 // (returns true when the tile computed its exact partial).
+template <int kRec>
 __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane, int round, bool marked,
                                            int *exact_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
@@ -1078,7 +1093,7 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
     int exact = 0;
     if (lane == 0) {
         const int n_row = __ldg(P.tile_end + t1 - 1) - __ldg(P.tile_begin + t0);
-        exact = !scr_skips(c, n_row, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) && row_due(P, round, chg);
+        exact = !scr_skips(c, n_row, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) && row_due<kRec>(P, round, chg);
     }
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
@@ -1100,6 +1115,7 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
 
 // Exact phase, tile t of a multi-tile row flagged this round: the row's exact
 // partials combined in tile order, then the decision and this tile's candidates.
+template <int kRec>
 __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane, int round, int *change,
                                             unsigned *tight_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
@@ -1126,7 +1142,7 @@ __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane
             }
         }
     }
-    split_row_candidates(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, ws);
+    split_row_candidates<kRec>(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, ws);
 }
 
 // Adds a thread's committed-change count to the round flags, one atomic per warp.
@@ -1157,7 +1173,7 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
             const int j = w * 32 + lane;
             const double2 b = P.bnd_nxt[j];
             P.bnd[j] = b;
-            P.bnd32[j] = bnd_record(b, round);
+            store_bnd32<1>(P, j, b, round);
             if (var_infeasible(b.x, b.y)) {
                 P.flags[0].infeasible = 1;
                 atomicMin(&P.flags[0].infeasible_var, j);
@@ -1188,8 +1204,8 @@ __device__ __forceinline__ int warp_next(unsigned *ctr, int lane) {
 
 __device__ __forceinline__ void activity_item(const DevProblem &P, int it, int lane, int round, bool marked,
                                               int *change, unsigned *tight_ctr, WarpSmem &ws, int par) {
-    if (it >= 0) sell_slice(P, it, lane, round, marked, change, tight_ctr, ws, par);
-    else split_partial(P, -it - 1, lane, round, marked, change, tight_ctr, ws);
+    if (it >= 0) sell_slice<1>(P, it, lane, round, marked, change, tight_ctr, ws, par);
+    else split_partial<1>(P, -it - 1, lane, round, marked, change, tight_ctr, ws);
 }
 
 // Items are claimed kScreenGroup at a time; a claim of one-lane-row slices
@@ -1217,7 +1233,7 @@ __device__ __forceinline__ void activity_phase(const DevProblem &P, int round, b
             for (int k = 0; k < K; k++) group = group && __ldg(P.slice_lg + it[k]) == 0;
         }
         if (group) {
-            sell_slices_g1<K>(P, it, lane, round, marked, ws, par);
+            sell_slices_g1<K, 1>(P, it, lane, round, marked, ws, par);
         } else {
 #pragma unroll 1
             for (int k = 0; k < K && i + k < P.n_items; k++)
@@ -1251,7 +1267,7 @@ __device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, 
             live = !marked || P.mark[P.n_srows + __ldg(P.tile_row + t)] == round;
         }
         for (unsigned bal = __ballot_sync(kFull, live); bal; bal &= bal - 1)
-            split_cand(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, false, exact_ctr, ws);
+            split_cand<1>(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, false, exact_ctr, ws);
     }
     stats_flush(P, ws, lane);
 }
@@ -1272,7 +1288,7 @@ __device__ __forceinline__ void exact_phase(const DevProblem &P, int round, unsi
             live = P.row_exact[__ldg(P.tile_row + t)] == round;
         }
         for (unsigned bal = __ballot_sync(kFull, live); bal; bal &= bal - 1)
-            split_exact(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, change, tight_ctr, ws);
+            split_exact<1>(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, change, tight_ctr, ws);
     }
     stats_flush(P, ws, lane);
 }
