@@ -46,7 +46,7 @@ constexpr int kQueueCap = 128;  // >= 31 pending + 64 pushed per step
 // recording calls are empty.
 constexpr int kTimerRounds = 1024;  // rounds recorded (later rounds are not)
 constexpr int kTimerSlots = 8;      // per round: 5 stamps + 3 work counters; 5 phase busy sums
-constexpr int kTimerPass = 16;      // 2 passes x lane-group sizes 1..32
+constexpr int kTimerPass = 16;      // 2 passes x lane-group sizes 1..32, then one-lane row work
 #ifdef GDP_PHASE_TIMERS
 __device__ unsigned long long g_timer_wall[kTimerRounds * kTimerSlots];
 __device__ unsigned long long g_timer_busy[kTimerRounds * kTimerSlots];
@@ -64,9 +64,25 @@ __device__ __forceinline__ void timer_pass(int lane, int lg, unsigned long long 
         atomicAdd(&g_timer_pass[2 * lg + 1], t2 - t1);
     }
 }
+// one-lane rows of an exact-pass warp: their elements (slot 12) against 32 x
+// the longest (slot 13), the lane utilisation of the row loops
+__device__ __forceinline__ void timer_lanes(int lane, int lg, int cnt) {
+    if (lg != 0) return;
+    int sum = cnt, mx = cnt;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, off);
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) {
+        atomicAdd(&g_timer_pass[12], (unsigned long long)sum);
+        atomicAdd(&g_timer_pass[13], 32ull * (unsigned long long)mx);
+    }
+}
 #else
 __device__ __forceinline__ unsigned long long timer_now() { return 0ull; }
 __device__ __forceinline__ void timer_pass(int, int, unsigned long long, unsigned long long) {}
+__device__ __forceinline__ void timer_lanes(int, int, int) {}
 #endif
 
 __device__ __forceinline__ void mark_changed(const DevProblem &P, int j) {
@@ -507,6 +523,7 @@ __device__ __forceinline__ void sell_rows_exact(const DevProblem &P, const ElemV
     const double *val = ev.val + base;
     const int st = ev.stride;
     const int cnt1 = exact ? cnt : 0;
+    timer_lanes(lane, lg, cnt1);
     Acc s;
     acc_init(s);
     double mn = 0.0;
@@ -1117,7 +1134,7 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
 // partials combined in tile order, then the decision and this tile's candidates.
 template <int kRec>
 __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane, int round, int *change,
-                                            unsigned *tight_ctr, WarpSmem &ws) {
+                                            unsigned *tight_ctr, WarpSmem &ws, int part = 0, int parts = 1) {
     const int row = __ldg(P.tile_row + t);
     if (P.row_exact[row] != round) return;
     // lanes load 32 partials at a time; lane 0 folds them in tile order
@@ -1142,7 +1159,11 @@ __device__ __forceinline__ void split_exact(const DevProblem &P, int t, int lane
             }
         }
     }
-    split_row_candidates<kRec>(P, row, __ldg(P.tile_begin + t), __ldg(P.tile_end + t), s, lane, change, tight_ctr, ws);
+    // this item's part of the tile: parts of whole warp steps
+    const int tb = __ldg(P.tile_begin + t), te = __ldg(P.tile_end + t);
+    const int step = ((te - tb + parts - 1) / parts + 31) & ~31;
+    const int pb = min(te, tb + part * step), pe = min(te, pb + step);
+    if (pb < pe) split_row_candidates<kRec>(P, row, pb, pe, s, lane, change, tight_ctr, ws);
 }
 
 // Adds a thread's committed-change count to the round flags, one atomic per warp.
@@ -1273,22 +1294,30 @@ __device__ __forceinline__ void candidate_phase(const DevProblem &P, int round, 
 }
 
 // Exact phase over the tiles of the multi-tile rows flagged this round, with
-// the same static assignment as the candidate phase.
+// the same static assignment as the candidate phase, each tile's candidates in
+// quarters (a warp per quarter): the row test is the same for every quarter,
+// and a tile's 1,024 candidate tests and divisions on one warp were the
+// phase's long pole while the rest of the grid waited at its barrier.
 __device__ __forceinline__ void exact_phase(const DevProblem &P, int round, unsigned *ctr, int *change,
                                             unsigned *tight_ctr, WarpSmem &ws, int lane) {
     (void)ctr;
     stats_zero(ws, lane);
+    constexpr int kParts = 4;  // candidates of a tile in quarters: a long tile is no phase's long pole
     const int nw = grid_warps();
-    for (int i0 = grid_warp(); i0 < P.n_mtiles; i0 += 32 * nw) {
+    const int n_items = P.n_mtiles * kParts;
+    for (int i0 = grid_warp(); i0 < n_items; i0 += 32 * nw) {
         const int i = i0 + lane * nw;
         int t = 0;
         bool live = false;
-        if (i < P.n_mtiles) {
-            t = __ldg(P.mtiles + i);
+        if (i < n_items) {
+            t = __ldg(P.mtiles + i / kParts);
             live = P.row_exact[__ldg(P.tile_row + t)] == round;
         }
-        for (unsigned bal = __ballot_sync(kFull, live); bal; bal &= bal - 1)
-            split_exact<1>(P, __shfl_sync(kFull, t, __ffs(bal) - 1), lane, round, change, tight_ctr, ws);
+        for (unsigned bal = __ballot_sync(kFull, live); bal; bal &= bal - 1) {
+            const int src = __ffs(bal) - 1;
+            split_exact<1>(P, __shfl_sync(kFull, t, src), lane, round, change, tight_ctr, ws,
+                           (i0 + src * nw) % kParts, kParts);
+        }
     }
     stats_flush(P, ws, lane);
 }

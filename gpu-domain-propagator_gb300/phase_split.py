@@ -92,6 +92,8 @@ def split(scale: float = 1.0, seed: int = 1000, warmup: int = 3, per_round: bool
         "busy_share": {k: v / total_busy for k, v in busy_ms.items()} if total_busy else {},
         "exact_pass_ms_per_warp": {f"g{1 << lg}": [float(passes[2 * lg]) / warps / 1e6,
                                                      float(passes[2 * lg + 1]) / warps / 1e6] for lg in range(6)},
+        # one-lane exact rows: elements against 32 x the longest row of each warp
+        "one_lane_row_utilisation": float(passes[12]) / float(passes[13]) if passes[13] else None,
         "stats": {k: st[k] for k in ("rows_processed", "nnz_processed", "nnz_exact", "rows_exact", "rows_go",
                                      "divisions", "changed_vars")},
     }

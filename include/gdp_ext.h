@@ -283,7 +283,8 @@ GDP_RETCODE gdp_autotune_clear_cache(void);
  *     time of one warp in one of A (5), B's two parts (6), C or F (7);
  *   pass[2 lg + i] (16 values, all rounds): warp ns of the exact pass of rows
  *     summed by 2^lg lanes, pass 1 (i = 0, activities and row test) and pass 2
- *     (i = 1, candidates).
+ *     (i = 1, candidates); pass[12]: elements of the one-lane rows through the
+ *     exact pass, pass[13]: 32 x the longest such row of each warp, summed.
  * Any output may be NULL. The timers accumulate over propagations until
  * gdp_phase_timers_clear; they are device globals of the current device. */
 GDP_RETCODE gdp_phase_timers_clear(void);
