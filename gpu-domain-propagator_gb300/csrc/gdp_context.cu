@@ -523,6 +523,19 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.srow_rhs = d_srow_rhs;
     P.n_lrows = n_lrows;
     P.n_tiles = n_tiles;
+    GDP_UP(P.lrow_lhs, const double, lrow_lhs);
+    GDP_UP(P.lrow_rhs, const double, lrow_rhs);
+    GDP_UP(P.lrow_tile0, const int, lrow_tile0);
+    if (tile_row.empty()) { tile_row.push_back(0); tile_begin.push_back(0); tile_end.push_back(0); }
+    GDP_UP(P.tile_row, const int, tile_row);
+    GDP_UP(P.tile_begin, const int, tile_begin);
+    GDP_UP(P.tile_end, const int, tile_end);
+    // The device builds the layout and then the marking index while this
+    // thread prepares the rest (row origins, work lists, variable types) and
+    // sends it up on the helper's stream; one synchronisation at the end, then
+    // the element checks' verdict.
+    Arena tmp;  // the row maps, freed when the build is done
+    int *hbad = reinterpret_cast<int *>(h_flags);  // pinned: the checks' verdict comes back asynchronously
     {  // element arrays: the raw CSR goes up once and the device places every
        // element (SELL slots, row-contiguous copy, split rows) together with
        // its FP32 screen copy
@@ -548,7 +561,6 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         GDP_CUDA(cudaMemsetAsync(xc, 0, sizeof(int) * n_x, stream));  // row padding of the copy
         GDP_CUDA(cudaMemsetAsync(xv, 0, sizeof(double) * n_x, stream));
         GDP_CUDA(cudaMemsetAsync(xa, 0, sizeof(float) * n_x, stream));
-        Arena tmp;  // the row maps, freed when the build is done
         int *dord = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
         int *dspl = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
         long long *dlrp = (long long *)tmp.alloc_bytes(sizeof(long long) * ((size_t)n_lrows + 1));
@@ -588,49 +600,62 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         L.lhs = dlhs; L.rhs = drhs; L.len_start = dls; L.len_base = dlb; L.n_slices = n_slices;
         L.srow_len_out = d_srow_len; L.xptr_out = d_xptr; L.pos_slice_out = d_pos_slice;
         L.srow_lhs_out = d_srow_lhs; L.srow_rhs_out = d_srow_rhs;
-        // nothing up to the marking index uses a column as an index, so the
-        // build runs before the element checks' result is read
+        // nothing in the layout build uses a column as an index, and the
+        // marking index skips columns out of range, so both run before the
+        // element checks' verdict is read
         GDP_CUDA(build_layout_positions(L, 8 * n_sms, stream));
         GDP_CUDA(build_layout_elements(L, 8 * n_sms, stream));
-        int bad[2];
-        GDP_CUDA(cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, stream));
-        GDP_CUDA(cudaStreamSynchronize(stream));  // before the raw CSR is freed
-        raw.release();
-        if (element_error(bad) != GDP_OKAY) return GDP_ERROR;
+        GDP_CUDA(cudaMemcpyAsync(hbad, dbad, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
         P.sell_col = sc; P.sell_val = sv; P.sell_a32 = sa;
         P.xcol = xc; P.xval = xv; P.xa32 = xa;
         P.lcol = lc; P.lval = lv; P.la32 = la;
     }
-    {  // original row of every position (row-side infeasibility names it)
-        std::vector<int> pos_row((size_t)std::max(ns + n_lrows, 1), 0);
-        std::copy(order.begin(), order.end(), pos_row.begin());
-        std::copy(split_rows.begin(), split_rows.end(), pos_row.begin() + ns);
-        GDP_UP(P.pos_row, const int, pos_row);
+    vec_blocks = std::max(1, std::min((std::max(n, std::max(ns + n_lrows, 1)) + 255) / 256, 8 * n_sms));
+    // marking index (variable -> row positions), built on the device from the
+    // layout (also used by node batches when this context's rounds never mark)
+    {
+        int *vp = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1));
+        int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
+        int *scratch = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)(n + 1 + (n + 1 + 1023) / 1024 + 1));
+        if (!vp || !vpos || !scratch) { set_error("device allocation failed (marking index)"); return GDP_ERROR; }
+        GDP_CUDA(build_marking_index(P, vp, vpos, scratch, 8 * n_sms, stream));
+        P.var_ptr = vp;
+        P.var_pos = vpos;
     }
-    GDP_UP(P.lrow_lhs, const double, lrow_lhs);
-    GDP_UP(P.lrow_rhs, const double, lrow_rhs);
-    GDP_UP(P.lrow_tile0, const int, lrow_tile0);
-    if (tile_row.empty()) { tile_row.push_back(0); tile_begin.push_back(0); tile_end.push_back(0); }
-    GDP_UP(P.tile_row, const int, tile_row);
-    GDP_UP(P.tile_begin, const int, tile_begin);
-    GDP_UP(P.tile_end, const int, tile_end);
+    // the rest goes up on the helper's stream while the device builds
+    auto up_aux = [&](const void *src, size_t bytes) -> void * {
+        void *d = arena.alloc_bytes(bytes);
+        if (!d) return nullptr;
+        if (bytes && cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, ups.s) != cudaSuccess) return nullptr;
+        return d;
+    };
+#define GDP_UP_AUX(dst, T, vec)                                                                     \
+    do {                                                                                           \
+        dst = (T *)up_aux((vec).data(), sizeof((vec)[0]) * (vec).size());                          \
+        if (!dst) { set_error("device allocation/upload failed for " #vec); return GDP_ERROR; }     \
+    } while (0)
+    std::vector<int> pos_row((size_t)std::max(ns + n_lrows, 1), 0);  // row-side infeasibility names it
+    std::copy(order.begin(), order.end(), pos_row.begin());
+    std::copy(split_rows.begin(), split_rows.end(), pos_row.begin() + ns);
+    GDP_UP_AUX(P.pos_row, const int, pos_row);
     std::vector<int> mtiles;
     for (int r = 0; r < n_lrows; r++)
         if (lrow_tile0[r + 1] - lrow_tile0[r] > 1)
             for (int t = lrow_tile0[r]; t < lrow_tile0[r + 1]; t++) mtiles.push_back(t);
     P.n_mtiles = (int)mtiles.size();
     if (mtiles.empty()) mtiles.push_back(0);
-    GDP_UP(P.mtiles, const int, mtiles);
+    GDP_UP_AUX(P.mtiles, const int, mtiles);
     P.n_items = (int)items.size();
     if (items.empty()) items.push_back(0);
-    GDP_UP(P.items, const int, items);
+    GDP_UP_AUX(P.items, const int, items);
     P.use_marking = opts.use_marking < 0 ? 1 : (opts.use_marking > 2 ? 2 : opts.use_marking);
     // adaptive marking: mark when a round tightened fewer bounds than 1/16 of the variables
     P.mark_threshold = (unsigned)std::max(1, n / 16);
     std::vector<unsigned char> is_cont(std::max(n, 1), 0);
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < n; j++) is_cont[j] = vartype[j] == GDP_CONTINUOUS ? 1 : 0;
-    GDP_UP(P.is_cont, const unsigned char, is_cont);
+    GDP_UP_AUX(P.is_cont, const unsigned char, is_cont);
+#undef GDP_UP_AUX
 #undef GDP_UP
     const int npos = std::max(ns + n_lrows, 1);
     const int n_words = (n + 31) / 32;
@@ -663,21 +688,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         return GDP_ERROR;
     }
 
-    vec_blocks = std::max(1, std::min((std::max(n, npos) + 255) / 256, 8 * n_sms));
-    // marking index (variable -> row positions), built on the device from the
-    // layout (also used by node batches when this context's rounds never mark)
-    {
-        int *vp = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1));
-        int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
-        int *scratch = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1 + (n + 1 + 1023) / 1024 + 1));
-        if (!vp || !vpos || !scratch) { set_error("device allocation failed (marking index)"); return GDP_ERROR; }
-        GDP_CUDA(build_marking_index(P, vp, vpos, scratch, 8 * n_sms, stream));
-        P.var_ptr = vp;
-        P.var_pos = vpos;
-    }
     if (set_schedule(opts.sync_type, opts.ctas_per_sm, opts.cta_threads) != GDP_OKAY) return GDP_ERROR;
-    GDP_CUDA(cudaStreamSynchronize(stream));
-    return GDP_OKAY;
+    GDP_CUDA(cudaStreamSynchronize(ups.s));
+    GDP_CUDA(cudaStreamSynchronize(stream));  // before the raw CSR is freed and the verdict is read
+    raw.release();
+    return element_error(hbad);
 }
 
 // Grid sizes of the loop drivers for the schedule (the layout is untouched).

@@ -46,13 +46,19 @@ __device__ __forceinline__ void for_each_element(const DevProblem &P, F &&f) {
     }
 }
 
+// Columns out of range are skipped: the index is built before the element
+// checks' verdict is read (the context is then rejected, the index unused).
 __global__ void k_count_cols(DevProblem P, int *cnt) {
-    for_each_element(P, [&](int j, int) { atomicAdd(cnt + j, 1); });
+    for_each_element(P, [&](int j, int) {
+        if ((unsigned)j < (unsigned)P.n) atomicAdd(cnt + j, 1);
+    });
 }
 
 // fill[j] starts at var_ptr[j] and hands out the slots of column j
 __global__ void k_fill_cols(DevProblem P, int *fill, int *pos_out) {
-    for_each_element(P, [&](int j, int pos) { pos_out[atomicAdd(fill + j, 1)] = pos; });
+    for_each_element(P, [&](int j, int pos) {
+        if ((unsigned)j < (unsigned)P.n) pos_out[atomicAdd(fill + j, 1)] = pos;
+    });
 }
 
 // Block-level exclusive scan (Hillis-Steele in shared memory; counts fit int).
