@@ -33,6 +33,30 @@ namespace gdp {
 
 namespace {
 thread_local std::string g_last_error;
+
+// Allocator that leaves the elements of a resized vector uninitialised: the
+// layout's per-row host arrays are written in full by parallel loops, and
+// zero-filling them first cost a serial pass over megabytes.
+template <class T>
+struct NoInit : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInit<U>;
+    };
+    NoInit() = default;
+    template <class U>
+    NoInit(const NoInit<U> &) {}
+    template <class U>
+    void construct(U *p) {
+        ::new ((void *)p) U;
+    }
+    template <class U, class... A>
+    void construct(U *p, A &&...a) {
+        ::new ((void *)p) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using RawVec = std::vector<T, NoInit<T>>;
 }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
@@ -319,12 +343,16 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // this is a counting sort by length, longest first -- run in parallel over
     // contiguous row chunks (per-chunk histograms keep it stable). Split rows
     // (longer than Ls) are collected in row order and sorted by length.
-    std::vector<int> sell_rows, split_rows;
+    // pos_row: the original row of every position -- SELL positions first (the
+    // row order the layout is built from), then the split rows; uploaded as is
+    RawVec<int> pos_row((size_t)std::max(m, 1));
+    std::vector<int> split_rows;
     // per SELL row length L: first position, and first element of the
     // row-contiguous copy (rows of one length are consecutive positions)
     std::vector<int> len_start((size_t)lmax + 1, 0);
     std::vector<long long> len_base((size_t)lmax + 1, 0);
     long long x_elems = 0;  // elements of the row-contiguous copy
+    int n_sell_rows = 0;
     {
 #ifdef _OPENMP
         const int nt = lmax <= (1 << 16) ? std::min(host_threads, 64) : 1;
@@ -361,7 +389,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             x_elems += (long long)(acc - len_start[L]) * ((L + 3) & ~3);  // rows start on 4-element boundaries
         }
         for (int t = 0; t < nt; t++) nsplit[t + 1] += nsplit[t];
-        sell_rows.resize(acc);
+        n_sell_rows = acc;
         split_rows.resize(nsplit[nt]);
 #pragma omp parallel num_threads(nt)
         {
@@ -375,13 +403,13 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             int sp = nsplit[t];
             for (int i = i0; i < i1; i++) {
                 if (len[i] > Ls) split_rows[sp++] = i;
-                else if (len[i] > 0) sell_rows[h[len[i]]++] = i;
+                else if (len[i] > 0) pos_row[h[len[i]]++] = i;
             }
         }
     }
     std::stable_sort(split_rows.begin(), split_rows.end(), [&](int a, int b) { return len[a] > len[b]; });
-    const int ns = (int)sell_rows.size();
-    const std::vector<int> &order = sell_rows;  // row position -> original row
+    const int ns = n_sell_rows;
+    const int *order = pos_row.data();  // row position -> original row
 
     n_srows = ns;
     // slices: the rows of one lanes-per-row class are consecutive positions;
@@ -443,20 +471,30 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     std::vector<int> lrow_tile0(n_lrows + 1, 0);
     std::vector<double> lrow_lhs(std::max(n_lrows, 1)), lrow_rhs(std::max(n_lrows, 1));
     std::vector<int> tile_row, tile_begin, tile_end;
-    for (int r = 0; r < n_lrows; r++) {
-        const int i = split_rows[r];
-        lrow_ptr[r + 1] = lrow_ptr[r] + len[i];
-        lrow_lhs[r] = lhs[i];
-        lrow_rhs[r] = rhs[i];
-        lrow_tile0[r] = (int)tile_row.size();
-        for (long long b = lrow_ptr[r]; b < lrow_ptr[r + 1]; b += opts.split_tile) {
-            tile_row.push_back(r);
-            tile_begin.push_back((int)b);
-            tile_end.push_back((int)std::min(b + opts.split_tile, lrow_ptr[r + 1]));
+    {  // element and tile offsets (prefix sums), then the row sides and tiles in parallel
+        const long long tl = opts.split_tile;
+        for (int r = 0; r < n_lrows; r++) {
+            const int L = len[split_rows[r]];
+            lrow_ptr[r + 1] = lrow_ptr[r] + L;
+            lrow_tile0[r + 1] = lrow_tile0[r] + (int)((L + tl - 1) / tl);
+        }
+        n_tiles = lrow_tile0[n_lrows];
+        tile_row.resize(n_tiles);
+        tile_begin.resize(n_tiles);
+        tile_end.resize(n_tiles);
+#pragma omp parallel for schedule(static) num_threads(host_threads)
+        for (int r = 0; r < n_lrows; r++) {
+            const int i = split_rows[r];
+            lrow_lhs[r] = lhs[i];
+            lrow_rhs[r] = rhs[i];
+            int t = lrow_tile0[r];
+            for (long long b = lrow_ptr[r]; b < lrow_ptr[r + 1]; b += tl, t++) {
+                tile_row[t] = r;
+                tile_begin[t] = (int)b;
+                tile_end[t] = (int)std::min(b + tl, lrow_ptr[r + 1]);
+            }
         }
     }
-    lrow_tile0[n_lrows] = (int)tile_row.size();
-    n_tiles = (int)tile_row.size();
     const long long lnnz = lrow_ptr[n_lrows];
     // work items of the activity phase, heaviest first (slices: 32 x width non-zeros)
     std::vector<int> items;
@@ -577,7 +615,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             return GDP_ERROR;
         }
         GDP_CUDA(cudaStreamWaitEvent(stream, ups.done, 0));
-        if (ns) GDP_CUDA(cudaMemcpyAsync(dord, order.data(), sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, stream));
+        if (ns) GDP_CUDA(cudaMemcpyAsync(dord, order, sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, stream));
         if (n_lrows)
             GDP_CUDA(cudaMemcpyAsync(dspl, split_rows.data(), sizeof(int) * (size_t)n_lrows, cudaMemcpyHostToDevice,
                                      stream));
@@ -634,10 +672,12 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         dst = (T *)up_aux((vec).data(), sizeof((vec)[0]) * (vec).size());                          \
         if (!dst) { set_error("device allocation/upload failed for " #vec); return GDP_ERROR; }     \
     } while (0)
-    std::vector<int> pos_row((size_t)std::max(ns + n_lrows, 1), 0);  // row-side infeasibility names it
-    std::copy(order.begin(), order.end(), pos_row.begin());
+    // row-side infeasibility names a position's original row: the split rows
+    // follow the SELL positions (the row order uploaded above is staged already)
     std::copy(split_rows.begin(), split_rows.end(), pos_row.begin() + ns);
-    GDP_UP_AUX(P.pos_row, const int, pos_row);
+    if (ns + n_lrows == 0) pos_row[0] = 0;
+    P.pos_row = (const int *)up_aux(pos_row.data(), sizeof(int) * (size_t)std::max(ns + n_lrows, 1));
+    if (!P.pos_row) { set_error("device allocation/upload failed for pos_row"); return GDP_ERROR; }
     std::vector<int> mtiles;
     for (int r = 0; r < n_lrows; r++)
         if (lrow_tile0[r + 1] - lrow_tile0[r] > 1)
@@ -651,7 +691,8 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.use_marking = opts.use_marking < 0 ? 1 : (opts.use_marking > 2 ? 2 : opts.use_marking);
     // adaptive marking: mark when a round tightened fewer bounds than 1/16 of the variables
     P.mark_threshold = (unsigned)std::max(1, n / 16);
-    std::vector<unsigned char> is_cont(std::max(n, 1), 0);
+    RawVec<unsigned char> is_cont((size_t)std::max(n, 1));
+    is_cont[0] = 0;
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < n; j++) is_cont[j] = vartype[j] == GDP_CONTINUOUS ? 1 : 0;
     GDP_UP_AUX(P.is_cont, const unsigned char, is_cont);
