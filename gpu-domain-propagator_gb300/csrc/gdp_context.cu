@@ -654,11 +654,13 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     {
         int *vp = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1));
         int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
+        float *vac = (float *)arena.alloc_bytes(sizeof(float) * (size_t)std::max(nnz, 1));
         int *scratch = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)(n + 1 + (n + 1 + 1023) / 1024 + 1));
-        if (!vp || !vpos || !scratch) { set_error("device allocation failed (marking index)"); return GDP_ERROR; }
-        GDP_CUDA(build_marking_index(P, vp, vpos, scratch, 8 * n_sms, stream));
+        if (!vp || !vpos || !vac || !scratch) { set_error("device allocation failed (marking index)"); return GDP_ERROR; }
+        GDP_CUDA(build_marking_index(P, vp, vpos, vac, scratch, 8 * n_sms, stream));
         P.var_ptr = vp;
         P.var_pos = vpos;
+        P.var_acoef = vac;
     }
     // the rest goes up on the helper's stream while the device builds
     auto up_aux = [&](const void *src, size_t bytes) -> void * {
@@ -710,6 +712,9 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.xrow = (XRow *)arena.alloc_bytes(sizeof(XRow) * (size_t)std::max(ns, 1));
     P.xctr = (unsigned *)arena.alloc_bytes(sizeof(unsigned) * 32);
     P.row_exact = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
+    P.lrow_margin = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n_lrows, 1));
+    P.lrow_drift = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n_lrows, 1));
+    P.lrow_skip = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(n_lrows, 1));
     P.mark = (int *)arena.alloc_bytes(sizeof(int) * (size_t)npos);
     P.bnd = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
     P.bnd_nxt = (double2 *)arena.alloc_bytes(sizeof(double2) * (size_t)std::max(n, 1));
@@ -723,7 +728,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     P.spin_limit = opts.barrier_wait_kcycles > 0 ? 1000LL * opts.barrier_wait_kcycles : 4000000000LL;
     d_lb = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
     d_ub = (double *)arena.alloc_bytes(sizeof(double) * (size_t)std::max(n, 1));
-    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.xrow || !P.xctr || !P.mark || !P.bnd || !P.bnd_nxt || !P.bnd32 || !P.chg || !P.flags || !P.barrier || !P.queue ||
+    if (!P.tile_part || !P.tile_scr || !P.row_exact || !P.lrow_margin || !P.lrow_drift || !P.lrow_skip || !P.xrow || !P.xctr || !P.mark || !P.bnd || !P.bnd_nxt || !P.bnd32 || !P.chg || !P.flags || !P.barrier || !P.queue ||
         !d_lb || !d_ub) {
         set_error("device allocation failed");
         return GDP_ERROR;

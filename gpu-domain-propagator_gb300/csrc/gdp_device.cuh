@@ -503,6 +503,28 @@ __device__ __forceinline__ bool scr_skips(const Scr &c, int n, double lhs, doubl
     return mn_hi < kInfF32Dn && __fmul_ru(scr_u_bound(c), kUMargin) <= mn_lo;
 }
 
+// The certified margin of a row the screen skips (scr_skips): how far the
+// row's FP64 slacks may still fall, whatever order they are summed in, before
+// that skip's certificate fails -- every |a| (ub - lb) only shrinks as bounds
+// tighten, so the certificate u <= slack needs the slacks alone. It is mn_lo -
+// u (u = fl_ru(U kUMargin)), less 2^-30 S for the FP64 summation errors of
+// the certifying and of a later evaluation (n <= 2^20 terms, 2^-33 S each,
+// with S grown by the drift at most), 2^-50 |mn_lo| for the rounding of the
+// slack itself and 2^-80, rounded down. A row skipped on its infinite
+// contributions keeps its skip until a bound becomes finite (an infinite
+// drift): margin DBL_MAX. -1 when the screen does not skip the row.
+__device__ __forceinline__ double scr_margin(const Scr &c, int n, double lhs, double rhs) {
+    if (c.minf > 1 && c.maxf > 1) return 1.7976931348623157e308;
+    float lo, hi;
+    scr_slack(c, n, lhs, rhs, lo, hi);
+    const float u = __fmul_ru(scr_u_bound(c), kUMargin);
+    if (!(hi < kInfF32Dn && u <= lo)) return -1.0;
+    double m = __dsub_rd((double)lo, (double)u);
+    m = __dsub_rd(m, __dmul_ru((double)c.S, 0x1p-30));
+    m = __dsub_rd(m, __dmul_ru(fabs((double)lo), 0x1p-50));
+    return __dsub_rd(m, 0x1p-80);
+}
+
 // The project's infeasibility rule (the reference detects none).
 __device__ __forceinline__ bool var_infeasible(double lb, double ub) {
     double s = fmax(fabs(lb), fabs(ub));

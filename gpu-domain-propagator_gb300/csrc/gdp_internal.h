@@ -180,6 +180,13 @@ struct DevProblem {
     int *slice_stamp;      // n_slices
     const int *var_ptr;    // n + 1
     const int *var_pos;    // positions of each variable's rows
+    const float *var_acoef;  // |a| of each entry of var_pos, rounded up (drift bound)
+    // drift bound of split rows (single-problem plain rounds): the certified
+    // margin of the row's last screen skip (< 0: none), an upper bound of how
+    // far its FP64 slack can have moved since (variables tightened), and the
+    // round in which the screen skipped the row on that bound
+    double *lrow_margin, *lrow_drift;
+    int *lrow_skip;
     // bounds
     double2 *bnd;          // current (lb, ub); read-only while a round runs
     double2 *bnd_nxt;      // next: FP64 min/max atomics
@@ -258,6 +265,8 @@ int build_layout_elements(const LayoutBuild &L, int blocks, cudaStream_t s);
 // caller sets to INT_MAX before.
 int check_csr_elements(const int *col, const double *val, int nnz, int n, int *bad, int blocks, cudaStream_t s);
 // gdp_layout.cu: variable -> row-position index for marking (scratch: n + 2 + (n+1)/1024 ints)
-int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s);
+// var_acoef (may be null): |a| of every entry, rounded up, for the drift bound
+int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, float *var_acoef, int *scratch, int blocks,
+                        cudaStream_t s);
 
 }  // namespace gdp

@@ -36,28 +36,37 @@ __device__ __forceinline__ void for_each_element(const DevProblem &P, F &&f) {
         const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
         const long long base = P.slice_ptr[s] + lane;
 #pragma unroll 4
-        for (int i = 0; i < cnt; i++) f(__ldg(P.sell_col + base + 32LL * i), row0 + rl);
+        for (int i = 0; i < cnt; i++) f(__ldg(P.sell_col + base + 32LL * i), row0 + rl, __ldg(P.sell_a32 + base + 32LL * i));
     }
     for (int t = warp; t < P.n_tiles; t += nwarps) {
         const int pos = P.n_srows + P.tile_row[t];
         const int e = P.tile_end[t];
 #pragma unroll 4
-        for (int k = P.tile_begin[t] + lane; k < e; k += 32) f(__ldg(P.lcol + k), pos);
+        for (int k = P.tile_begin[t] + lane; k < e; k += 32) f(__ldg(P.lcol + k), pos, __ldg(P.la32 + k));
     }
 }
 
 // Columns out of range are skipped: the index is built before the element
 // checks' verdict is read (the context is then rejected, the index unused).
 __global__ void k_count_cols(DevProblem P, int *cnt) {
-    for_each_element(P, [&](int j, int) {
+    for_each_element(P, [&](int j, int, float) {
         if ((unsigned)j < (unsigned)P.n) atomicAdd(cnt + j, 1);
     });
 }
 
-// fill[j] starts at var_ptr[j] and hands out the slots of column j
-__global__ void k_fill_cols(DevProblem P, int *fill, int *pos_out) {
-    for_each_element(P, [&](int j, int pos) {
-        if ((unsigned)j < (unsigned)P.n) pos_out[atomicAdd(fill + j, 1)] = pos;
+// fill[j] starts at var_ptr[j] and hands out the slots of column j; with
+// acoef, each slot also gets |a| rounded up: the FP32 copy is round-to-nearest,
+// so one step up bounds |a| (infinite and NaN copies stay so)
+__global__ void k_fill_cols(DevProblem P, int *fill, int *pos_out, float *acoef) {
+    for_each_element(P, [&](int j, int pos, float a32) {
+        if ((unsigned)j < (unsigned)P.n) {
+            const int slot = atomicAdd(fill + j, 1);
+            pos_out[slot] = pos;
+            if (acoef) {
+                const float m = fabsf(a32);
+                acoef[slot] = m < kF32Inf ? __int_as_float(__float_as_int(m) + 1) : m;
+            }
+        }
     });
 }
 
@@ -111,7 +120,8 @@ __global__ void k_add_offsets(int *out, const int *block_sums, int n) {
 
 // Builds var_ptr (n + 1) and var_pos (nnz) on the device. scratch: n + 1 +
 // ceil((n + 1) / 1024) ints. Returns the cudaError_t of the launches.
-int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *scratch, int blocks, cudaStream_t s) {
+int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, float *var_acoef, int *scratch, int blocks,
+                        cudaStream_t s) {
     const int n1 = P.n + 1;
     const int nb = (n1 + kScanBlock - 1) / kScanBlock;
     int *cnt = scratch;        // n + 1 counts, then the fill cursors
@@ -124,7 +134,7 @@ int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, int *sc
     k_add_offsets<<<nb, kScanBlock, 0, s>>>(var_ptr, sums, n1);
     e = cudaMemcpyAsync(cnt, var_ptr, sizeof(int) * (size_t)n1, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return (int)e;
-    k_fill_cols<<<blocks, 256, 0, s>>>(P, cnt, var_pos);
+    k_fill_cols<<<blocks, 256, 0, s>>>(P, cnt, var_pos, var_acoef);
     return (int)cudaGetLastError();
 }
 

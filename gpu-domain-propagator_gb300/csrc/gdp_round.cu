@@ -111,6 +111,12 @@ __global__ void __launch_bounds__(256) k_copy_out(const double *lb, const double
 __global__ void __launch_bounds__(256) k_mark_all(DevProblem P) {
     const int npos = P.n_srows + P.n_lrows;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npos; p += gridDim.x * blockDim.x) P.mark[p] = 0;
+    if (P.lrow_margin)  // no drift bound carried over from an earlier propagation
+        for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < P.n_lrows; r += gridDim.x * blockDim.x) {
+            P.lrow_margin[r] = -1.0;
+            P.lrow_drift[r] = 0.0;
+            P.lrow_skip[r] = 0;
+        }
 }
 
 // ---- megakernel -----------------------------------------------------------

@@ -912,6 +912,30 @@ __device__ __forceinline__ void exact_rows_phase(const DevProblem &P, int par, i
 }
 
 // ---- split rows: one warp per tile ----------------------------------------
+// Drift bound (single-problem plain rounds; marked rounds use it): a split row
+// the screen skipped with certified margin m (scr_margin) stays skippable while
+// the bound D of how far its slack has fallen since -- finalize adds |a|
+// (lb' - lb + ub - ub') rounded up for every tightening of one of its
+// variables, infinite when an infinite bound becomes finite -- satisfies
+// D (1 + 2^-22) <= m: the factor covers D's own rounding (an FP64 sum of
+// rounded-up terms, up to 2^28 of them) and |a| against its FP32 copy. Such a
+// row tightens nothing and is feasible, exactly as its screen would decide.
+// Its work is counted as screened, so the statistics equal a full screen's.
+template <int kRec>
+__device__ __forceinline__ bool drift_active(const DevProblem &P) {
+    return kRec != 0 && P.learned == 0 && P.lrow_margin != nullptr;
+}
+__device__ __forceinline__ bool drift_skips(const DevProblem &P, int row) {
+    const double m = P.lrow_margin[row];
+    if (!(m >= 0.0)) return false;
+    return __dmul_ru(P.lrow_drift[row], 1.0 + 0x1p-22) <= m;  // false for NaN and inf drifts
+}
+// A screen of split row `row` refreshes its certificate (one writer per row).
+__device__ __forceinline__ void drift_reset(const DevProblem &P, int row, const Scr &c, int n, double lhs,
+                                            double rhs) {
+    P.lrow_margin[row] = scr_margin(c, n, lhs, rhs);
+    P.lrow_drift[row] = 0.0;
+}
 __device__ __forceinline__ void acc_shfl_reduce(Acc &s) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -1048,6 +1072,16 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     const int row = __ldg(P.tile_row + t);
     if (marked && P.mark[P.n_srows + row] != round) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
+    const int t0 = __ldg(P.lrow_tile0 + row);
+    const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
+    if (marked && drift_active<kRec>(P) && drift_skips(P, row)) {  // the same values for every lane
+        if (lane == 0) {
+            ws.st_nnz += (unsigned long long)(e - b);
+            if (t == t0) ws.st_rows += 1ULL;
+            if (!single) P.lrow_skip[row] = round;  // the candidate phase skips the row too
+        }
+        return false;
+    }
     Scr c;
     scr_init(c);
     int chg = 0;
@@ -1059,15 +1093,14 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     }
     scr_shfl_reduce(c);
     chg = __any_sync(kFull, chg) ? 1 : 0;
-    const int t0 = __ldg(P.lrow_tile0 + row);
-    const bool single = __ldg(P.lrow_tile0 + row + 1) - t0 == 1;
     int exact = 0;
     if (lane == 0) {
         ws.st_nnz += (unsigned long long)(e - b);
         if (t == t0) ws.st_rows += 1ULL;
         if (single) {
-            exact = !scr_skips(c, e - b, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) &&
-                    row_due<kRec>(P, round, chg);
+            const double lhs = __ldg(P.lrow_lhs + row), rhs = __ldg(P.lrow_rhs + row);
+            exact = !scr_skips(c, e - b, lhs, rhs) && row_due<kRec>(P, round, chg);
+            if (drift_active<kRec>(P)) drift_reset(P, row, c, e - b, lhs, rhs);
             if (exact) ws.st_exact += (unsigned long long)(e - b);
         } else {
             TileScr ts;
@@ -1094,6 +1127,7 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
                                            int *exact_ctr, WarpSmem &ws) {
     const int row = __ldg(P.tile_row + t);
     if (marked && P.mark[P.n_srows + row] != round) return false;
+    if (drift_active<kRec>(P) && P.lrow_skip[row] == round) return false;  // skipped on its drift bound
     const int t0 = __ldg(P.lrow_tile0 + row), t1 = __ldg(P.lrow_tile0 + row + 1);
     Scr c;
     scr_init(c);
@@ -1110,7 +1144,9 @@ __device__ __forceinline__ bool split_cand(const DevProblem &P, int t, int lane,
     int exact = 0;
     if (lane == 0) {
         const int n_row = __ldg(P.tile_end + t1 - 1) - __ldg(P.tile_begin + t0);
-        exact = !scr_skips(c, n_row, __ldg(P.lrow_lhs + row), __ldg(P.lrow_rhs + row)) && row_due<kRec>(P, round, chg);
+        const double lhs = __ldg(P.lrow_lhs + row), rhs = __ldg(P.lrow_rhs + row);
+        exact = !scr_skips(c, n_row, lhs, rhs) && row_due<kRec>(P, round, chg);
+        if (drift_active<kRec>(P) && t == t0) drift_reset(P, row, c, n_row, lhs, rhs);
     }
     if (!__shfl_sync(kFull, exact, 0)) return false;
     const int b = __ldg(P.tile_begin + t), e = __ldg(P.tile_end + t);
@@ -1190,9 +1226,14 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
     for (int w = tid >> 5; w < P.n_chg_words; w += nthreads >> 5) {
         const unsigned bits = P.chg[w];
         if (!bits) continue;  // warp-uniform
+        double delta = 0.0;  // upper bound of (lb' - lb) + (ub - ub') of my variable
         if ((bits >> lane) & 1u) {
             const int j = w * 32 + lane;
             const double2 b = P.bnd_nxt[j];
+            const double2 o = P.bnd[j];
+            delta = (neginf_bits(dbits(o.x)) || posinf_bits(dbits(o.y)))
+                            ? __longlong_as_double(0x7FF0000000000000LL)  // an infinite bound became finite
+                            : __dadd_ru(__dsub_ru(b.x, o.x), __dsub_ru(o.y, b.y));
             P.bnd[j] = b;
             store_bnd32<1>(P, j, b, round);
             if (var_infeasible(b.x, b.y)) {
@@ -1207,9 +1248,16 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
         }
         if (!push_marks) continue;
         for (unsigned rem = bits; rem; rem &= rem - 1) {
-            const int j = w * 32 + __ffs(rem) - 1;
-            for (int p = __ldg(P.var_ptr + j) + lane; p < __ldg(P.var_ptr + j + 1); p += 32)
-                P.mark[__ldg(P.var_pos + p)] = round + 1;
+            const int bit = __ffs(rem) - 1;
+            const int j = w * 32 + bit;
+            const double dj = __shfl_sync(kFull, delta, bit);
+            for (int p = __ldg(P.var_ptr + j) + lane; p < __ldg(P.var_ptr + j + 1); p += 32) {
+                const int pos = __ldg(P.var_pos + p);
+                P.mark[pos] = round + 1;
+                // a split row's slack moves by at most |a| (lb' - lb + ub - ub')
+                if (pos >= P.n_srows && P.lrow_drift)
+                    atomicAdd(P.lrow_drift + (pos - P.n_srows), __dmul_ru((double)__ldg(P.var_acoef + p), dj));
+            }
         }
     }
     flush_changed(P, changed);
