@@ -275,6 +275,18 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             if (s) cudaStreamDestroy(s);
         }
     } ups;
+    // marking index (variable -> row positions, |a| rounded up): the helper
+    // counts the columns as soon as they are up; the layout kernels fill it
+    const size_t n1 = (size_t)n + 1;
+    int *vp = (int *)arena.alloc_bytes(sizeof(int) * n1);
+    int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
+    float *vac = (float *)arena.alloc_bytes(sizeof(float) * (size_t)std::max(nnz, 1));
+    int *vcur = (int *)raw.alloc_bytes(sizeof(int) * n1);
+    int *vscan = (int *)raw.alloc_bytes(sizeof(int) * ((n1 + 1023) / 1024 + 1));
+    if (!vp || !vpos || !vac || !vcur || !vscan) {
+        set_error("device allocation failed (marking index)");
+        return GDP_ERROR;
+    }
     struct Joined {
         std::thread t;
         ~Joined() {
@@ -310,6 +322,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             e = cudaMemcpyAsync(drp, row_ptr, sizeof(int) * ((size_t)m + 1), cudaMemcpyHostToDevice, us);
         if (e == cudaSuccess && m) e = cudaMemcpyAsync(dlhs, lhs, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, us);
         if (e == cudaSuccess && m) e = cudaMemcpyAsync(drhs, rhs, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess) e = (cudaError_t)build_marking_counts(dcol, nnz, n, vp, vcur, vscan, us);
         if (e == cudaSuccess) e = cudaEventRecord(ups.done, us);
         if (e != cudaSuccess) fail("raw CSR upload", e);
     });
@@ -638,8 +651,9 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         L.lhs = dlhs; L.rhs = drhs; L.len_start = dls; L.len_base = dlb; L.n_slices = n_slices;
         L.srow_len_out = d_srow_len; L.xptr_out = d_xptr; L.pos_slice_out = d_pos_slice;
         L.srow_lhs_out = d_srow_lhs; L.srow_rhs_out = d_srow_rhs;
-        // nothing in the layout build uses a column as an index, and the
-        // marking index skips columns out of range, so both run before the
+        L.idx_cursor = vcur; L.var_pos = vpos; L.var_acoef = vac; L.n = n;
+        // the layout build uses columns as indices only for the marking
+        // index, which skips columns out of range, so it runs before the
         // element checks' verdict is read
         GDP_CUDA(build_layout_positions(L, 8 * n_sms, stream));
         GDP_CUDA(build_layout_elements(L, 8 * n_sms, stream));
@@ -649,19 +663,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         P.lcol = lc; P.lval = lv; P.la32 = la;
     }
     vec_blocks = std::max(1, std::min((std::max(n, std::max(ns + n_lrows, 1)) + 255) / 256, 8 * n_sms));
-    // marking index (variable -> row positions), built on the device from the
-    // layout (also used by node batches when this context's rounds never mark)
-    {
-        int *vp = (int *)arena.alloc_bytes(sizeof(int) * (size_t)(n + 1));
-        int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
-        float *vac = (float *)arena.alloc_bytes(sizeof(float) * (size_t)std::max(nnz, 1));
-        int *scratch = (int *)tmp.alloc_bytes(sizeof(int) * (size_t)(n + 1 + (n + 1 + 1023) / 1024 + 1));
-        if (!vp || !vpos || !vac || !scratch) { set_error("device allocation failed (marking index)"); return GDP_ERROR; }
-        GDP_CUDA(build_marking_index(P, vp, vpos, vac, scratch, 8 * n_sms, stream));
-        P.var_ptr = vp;
-        P.var_pos = vpos;
-        P.var_acoef = vac;
-    }
+    // the marking index (also used by node batches when this context's rounds
+    // never mark) was filled with the layout
+    P.var_ptr = vp;
+    P.var_pos = vpos;
+    P.var_acoef = vac;
     // the rest goes up on the helper's stream while the device builds
     auto up_aux = [&](const void *src, size_t bytes) -> void * {
         void *d = arena.alloc_bytes(bytes);

@@ -245,6 +245,13 @@ struct LayoutBuild {
     int *lcol;
     double *lval;
     float *la32;
+    // marking index, filled while the elements are placed: idx_cursor (n) hands
+    // out each column's next slot of var_pos (row position) and var_acoef (|a|
+    // rounded up); columns out of range are skipped (n: the variable count)
+    int *idx_cursor;
+    int *var_pos;
+    float *var_acoef;
+    int n;
     // row positions, built before the elements: SELL rows are sorted by
     // length, longest first, so the rows of one length L are the consecutive
     // positions from len_start[L] and their row-contiguous copies start at
@@ -265,8 +272,10 @@ int build_layout_elements(const LayoutBuild &L, int blocks, cudaStream_t s);
 // caller sets to INT_MAX before.
 int check_csr_elements(const int *col, const double *val, int nnz, int n, int *bad, int blocks, cudaStream_t s);
 // gdp_layout.cu: variable -> row-position index for marking (scratch: n + 2 + (n+1)/1024 ints)
-// var_acoef (may be null): |a| of every entry, rounded up, for the drift bound
-int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, float *var_acoef, int *scratch, int blocks,
-                        cudaStream_t s);
+// Column counts of the marking index from the raw CSR columns (out-of-range
+// columns skipped): var_ptr (n + 1) gets their exclusive prefix sums and
+// cursor (n + 1) a copy of it, from which the layout kernels hand out slots.
+// scratch: (n + 1 + 1023) / 1024 + 1 ints.
+int build_marking_counts(const int *col, int nnz, int n, int *var_ptr, int *cursor, int *scratch, cudaStream_t s);
 
 }  // namespace gdp

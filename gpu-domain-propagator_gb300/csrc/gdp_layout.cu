@@ -1,14 +1,16 @@
 // gdp_layout.cu -- device-side construction of the layout's element arrays
 // from the raw CSR (below), and of the marking index: for every
 // variable, the row positions (SELL slot or split-row slot) of the rows it
-// appears in. This is the transpose (CSR -> CSC pattern) that the reference
-// computes with cuSPARSE csr2csc on every call (src/kernels/util_kernels.cuh:92-229)
-// and uses to mark constraints (src/propagation_methods.cu:3-13).
+// appears in, with |a| rounded up (the drift bound's coefficients). This is
+// the transpose (CSR -> CSC pattern) that the reference computes with
+// cuSPARSE csr2csc on every call (src/kernels/util_kernels.cuh:92-229) and
+// uses to mark constraints (src/propagation_methods.cu:3-13).
 //
-// Three steps over the context's own layout: count the non-zeros of every
-// column (warp per slice / per split tile), exclusive scan of the counts,
-// scatter the positions. The order of positions inside a column is not
-// defined (it does not matter for marking).
+// The column counts and their exclusive scan come from the raw columns
+// alone, so they run while the host still bins the rows; the kernels that
+// place the elements scatter each one's position into its column's next slot.
+// The order of positions inside a column is not defined (it does not matter
+// for marking or for the drift sums).
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -21,53 +23,12 @@ namespace {
 
 constexpr int kScanBlock = 1024;
 
-// For every element of the layout, calls f(col, position). Warp per slice
-// (lane = row) or per split tile; items are visited through the grid stride.
-template <class F>
-__device__ __forceinline__ void for_each_element(const DevProblem &P, F &&f) {
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int s = warp; s < P.n_slices; s += nwarps) {
-        const int lg = P.slice_lg[s], g = 1 << lg;
-        const int row0 = P.slice_row0[s], nrows = P.slice_row0[s + 1] - row0;
-        const int rl = lane >> lg, sub = lane & (g - 1);
-        const int len = rl < nrows ? P.srow_len[row0 + rl] : 0;
-        const int cnt = len > sub ? (len - sub + g - 1) >> lg : 0;
-        const long long base = P.slice_ptr[s] + lane;
-#pragma unroll 4
-        for (int i = 0; i < cnt; i++) f(__ldg(P.sell_col + base + 32LL * i), row0 + rl, __ldg(P.sell_a32 + base + 32LL * i));
+// Counts the raw columns (out-of-range ones skipped: the element checks report them).
+__global__ void k_count_raw(const int *__restrict__ col, int nnz, int n, int *cnt) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += gridDim.x * blockDim.x) {
+        const int j = __ldcs(col + k);
+        if ((unsigned)j < (unsigned)n) atomicAdd(cnt + j, 1);
     }
-    for (int t = warp; t < P.n_tiles; t += nwarps) {
-        const int pos = P.n_srows + P.tile_row[t];
-        const int e = P.tile_end[t];
-#pragma unroll 4
-        for (int k = P.tile_begin[t] + lane; k < e; k += 32) f(__ldg(P.lcol + k), pos, __ldg(P.la32 + k));
-    }
-}
-
-// Columns out of range are skipped: the index is built before the element
-// checks' verdict is read (the context is then rejected, the index unused).
-__global__ void k_count_cols(DevProblem P, int *cnt) {
-    for_each_element(P, [&](int j, int, float) {
-        if ((unsigned)j < (unsigned)P.n) atomicAdd(cnt + j, 1);
-    });
-}
-
-// fill[j] starts at var_ptr[j] and hands out the slots of column j; with
-// acoef, each slot also gets |a| rounded up: the FP32 copy is round-to-nearest,
-// so one step up bounds |a| (infinite and NaN copies stay so)
-__global__ void k_fill_cols(DevProblem P, int *fill, int *pos_out, float *acoef) {
-    for_each_element(P, [&](int j, int pos, float a32) {
-        if ((unsigned)j < (unsigned)P.n) {
-            const int slot = atomicAdd(fill + j, 1);
-            pos_out[slot] = pos;
-            if (acoef) {
-                const float m = fabsf(a32);
-                acoef[slot] = m < kF32Inf ? __int_as_float(__float_as_int(m) + 1) : m;
-            }
-        }
-    });
 }
 
 // Block-level exclusive scan (Hillis-Steele in shared memory; counts fit int).
@@ -118,23 +79,17 @@ __global__ void k_add_offsets(int *out, const int *block_sums, int n) {
 
 }  // namespace
 
-// Builds var_ptr (n + 1) and var_pos (nnz) on the device. scratch: n + 1 +
-// ceil((n + 1) / 1024) ints. Returns the cudaError_t of the launches.
-int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, float *var_acoef, int *scratch, int blocks,
-                        cudaStream_t s) {
-    const int n1 = P.n + 1;
+int build_marking_counts(const int *col, int nnz, int n, int *var_ptr, int *cursor, int *scratch, cudaStream_t s) {
+    const int n1 = n + 1;
     const int nb = (n1 + kScanBlock - 1) / kScanBlock;
-    int *cnt = scratch;        // n + 1 counts, then the fill cursors
-    int *sums = scratch + n1;  // nb block sums
-    cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n1, s);
+    cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)n1, s);
     if (e != cudaSuccess) return (int)e;
-    k_count_cols<<<blocks, 256, 0, s>>>(P, cnt);
-    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(cnt, var_ptr, sums, n1);
-    k_scan_sums<<<1, kScanBlock, 0, s>>>(sums, nb);
-    k_add_offsets<<<nb, kScanBlock, 0, s>>>(var_ptr, sums, n1);
-    e = cudaMemcpyAsync(cnt, var_ptr, sizeof(int) * (size_t)n1, cudaMemcpyDeviceToDevice, s);
+    if (nnz > 0) k_count_raw<<<1024, 256, 0, s>>>(col, nnz, n, cursor);
+    k_scan_blocks<<<nb, kScanBlock, 0, s>>>(cursor, var_ptr, scratch, n1);
+    k_scan_sums<<<1, kScanBlock, 0, s>>>(scratch, nb);
+    k_add_offsets<<<nb, kScanBlock, 0, s>>>(var_ptr, scratch, n1);
+    e = cudaMemcpyAsync(cursor, var_ptr, sizeof(int) * (size_t)n1, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return (int)e;
-    k_fill_cols<<<blocks, 256, 0, s>>>(P, cnt, var_pos, var_acoef);
     return (int)cudaGetLastError();
 }
 
@@ -146,6 +101,14 @@ int build_marking_index(const DevProblem &P, int *var_ptr, int *var_pos, float *
 // row-contiguous copy, split-row arrays (block per split row). Padding slots
 // of the SELL arrays stay as cleared before.
 namespace {
+// Element (column c, coefficient v) of row position p into the marking index.
+__device__ __forceinline__ void index_element(const LayoutBuild &L, int c, double v, int p) {
+    if ((unsigned)c >= (unsigned)L.n) return;  // reported by the element checks
+    const int slot = atomicAdd(L.idx_cursor + c, 1);
+    L.var_pos[slot] = p;
+    L.var_acoef[slot] = __double2float_ru(fabs(v));
+}
+
 // Places the elements of SELL row positions, each with its FP32 screen copy
 // (coef_screen) in both layouts. One-lane rows (positions from g1_begin) go
 // thread per row: the threads of a warp hold consecutive rows of one slice,
@@ -171,6 +134,7 @@ __global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
             L.xcol[xb + k] = c;
             L.xval[xb + k] = v;
             L.xa32[xb + k] = a;
+            index_element(L, c, v, p);
         }
     }
     const int lane = threadIdx.x & 31;
@@ -194,6 +158,7 @@ __global__ void __launch_bounds__(256) k_build_sell(LayoutBuild L) {
             L.xcol[xb + k] = c;
             L.xval[xb + k] = v;
             L.xa32[xb + k] = a;
+            index_element(L, c, v, p);
         }
     }
 }
@@ -240,9 +205,11 @@ __global__ void __launch_bounds__(256) k_build_split(LayoutBuild L) {
 #pragma unroll 4
         for (int k = threadIdx.x; k < len; k += blockDim.x) {
             const double v = __ldg(L.val + b + k);
-            L.lcol[o + k] = __ldg(L.col + b + k);
+            const int c = __ldg(L.col + b + k);
+            L.lcol[o + k] = c;
             L.lval[o + k] = v;
             L.la32[o + k] = coef_screen(v);
+            index_element(L, c, v, L.n_srows + r);
         }
     }
 }
