@@ -96,6 +96,7 @@ struct RoundFlags {
     unsigned long long rows_exact;    // SELL rows through the exact FP64 pass
     unsigned long long rows_go;       // ... of which had their candidates computed
     unsigned long long rows_seqmax;   // rows whose row test needed the sequential EPS-max (seq_eps_max)
+    unsigned long long rows_drift;    // split rows skipped on their drift bound (counted once per row)
 };
 
 enum DeviceError : int {

@@ -85,6 +85,7 @@ class Stats(C.Structure):
         ("rows_exact", C.c_longlong),
         ("rows_go", C.c_longlong),
         ("rows_seqmax", C.c_longlong),
+        ("rows_drift", C.c_longlong),
     ]
 
     def as_dict(self) -> dict:

@@ -79,6 +79,9 @@ typedef struct {
     long long rows_go;      /* ... of which passed the row test (candidates computed) */
     long long rows_seqmax;  /* row tests that needed the reference's sequential EPS-max of |a|(ub-lb)
                                (the FP64 maximum exceeded the slack by EPS to 2.00001e-9) */
+    long long rows_drift;   /* marked split rows (longer than split_tile) left unread because their
+                               last screen's certified margin still covers every tightening of their
+                               variables since (counted in rows_processed / nnz_processed as screened) */
 } gdp_stats;
 
 /* Fills *opts with the defaults. */

@@ -509,6 +509,25 @@ def test_power_law_vs_reference_semantics():
     assert not np.any(bc & ~rc), "the GPU differs from cpu_seq where cpu_omp does not"
 
 
+def test_drift_bound_skips_split_rows_bitexact():
+    """Marked rounds leave a split row unread while the certified margin of its
+    last screen covers every tightening of its variables since (the drift
+    bound): on a power-law MIP with long rows such skips happen, and with
+    marking on every round the result, the round count and the work counters
+    (rows and non-zeros screened, rows through the row test) equal the
+    oracle's, which screens every marked row."""
+    mip = gdpgen.random_mip(1, seed=3, m=200_000, n=150_000, len_max=5000, dense_len=20_000, n_dense_rows=4)
+    for sync in SYNCS:
+        st = check_vs_oracle(mip, sync, trm=32, tile=1024, marking=2)
+        assert st["rows_drift"] > 0, sync
+    # the library defaults (adaptive marking) against the reference's cpu_omp semantics
+    lb, ub, st = gpu(mip, gdp.MEGAKERNEL)
+    omp = oracle.propagate(mip, oracle.JACOBI, nthreads=8)
+    assert st["rounds"] == omp.rounds and st["rows_drift"] > 0
+    bi, bc = _deviation(lb, ub, omp.lb, omp.ub, mip.vartype)
+    assert bi.sum() == 0 and bc.sum() == 0
+
+
 def test_barrier_wait_limit_returns_error_and_library_stays_usable():
     """A grid-barrier wait that runs out records a device error instead of
     waiting on: with a limit of 1,000 SM cycles (the first barrier of a round
