@@ -398,6 +398,7 @@ GDP_RETCODE Batch::propagate(const double *const *lbs_in, const double *const *u
         st.rows_go = (long long)f.rows_go;
         st.rows_seqmax = (long long)f.rows_seqmax;
         st.rows_drift = (long long)f.rows_drift;
+        st.nnz_drift = (long long)f.nnz_drift;
         st.full_rounds = f.full_rounds;
         st.bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc +
                                36.0 * (double)(var_base_[u + 1] - var_base_[u]) * (double)f.rounds;
@@ -417,6 +418,7 @@ GDP_RETCODE Batch::propagate(const double *const *lbs_in, const double *const *u
         tot.rows_go += st.rows_go;
         tot.rows_seqmax += st.rows_seqmax;
         tot.rows_drift += st.rows_drift;
+        tot.nnz_drift += st.nnz_drift;
         tot.full_rounds = std::max(tot.full_rounds, st.full_rounds);
         tot.bytes_algorithmic += st.bytes_algorithmic;
     }

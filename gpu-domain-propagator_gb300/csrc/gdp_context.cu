@@ -940,8 +940,11 @@ GDP_RETCODE Context::run(const double *lb_in, const double *ub_in, double *lb_ou
         st->rows_go = (long long)f.rows_go;
         st->rows_seqmax = (long long)f.rows_seqmax;
         st->rows_drift = (long long)f.rows_drift;
+        st->nnz_drift = (long long)f.nnz_drift;
         st->full_rounds = f.full_rounds;
-        st->bytes_algorithmic = 12.0 * (double)f.nnz_proc + 20.0 * (double)f.rows_proc + 36.0 * n * (double)f.rounds;
+        // the rows read: without those left unread on their drift bound
+        st->bytes_algorithmic = 12.0 * (double)(f.nnz_proc - f.nnz_drift) + 20.0 * (double)(f.rows_proc - f.rows_drift) +
+                                36.0 * n * (double)f.rounds;
         st->device_ms = ms;
     }
     return GDP_OKAY;

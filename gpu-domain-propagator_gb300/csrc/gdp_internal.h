@@ -97,6 +97,7 @@ struct RoundFlags {
     unsigned long long rows_go;       // ... of which had their candidates computed
     unsigned long long rows_seqmax;   // rows whose row test needed the sequential EPS-max (seq_eps_max)
     unsigned long long rows_drift;    // split rows skipped on their drift bound (counted once per row)
+    unsigned long long nnz_drift;     // their non-zeros
 };
 
 enum DeviceError : int {

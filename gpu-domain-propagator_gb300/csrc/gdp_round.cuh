@@ -302,13 +302,13 @@ struct WarpSmem {
     // work statistics of this warp, written by lane 0 and flushed to the
     // round flags once per phase (not once per item: same-address atomics
     // from every warp for every item would serialise in L2)
-    unsigned long long st_rows, st_nnz, st_exact, st_div, st_xrows, st_go, st_seq, st_drift;
+    unsigned long long st_rows, st_nnz, st_exact, st_div, st_xrows, st_go, st_seq, st_drift, st_drift_nnz;
 };
 
 __device__ __forceinline__ void stats_zero(WarpSmem &ws, int lane) {
     if (lane == 0) {
         ws.st_rows = 0; ws.st_nnz = 0; ws.st_exact = 0; ws.st_div = 0;
-        ws.st_xrows = 0; ws.st_go = 0; ws.st_seq = 0; ws.st_drift = 0;
+        ws.st_xrows = 0; ws.st_go = 0; ws.st_seq = 0; ws.st_drift = 0; ws.st_drift_nnz = 0;
     }
 }
 __device__ __forceinline__ void stats_flush(const DevProblem &P, WarpSmem &ws, int lane) {
@@ -321,8 +321,9 @@ __device__ __forceinline__ void stats_flush(const DevProblem &P, WarpSmem &ws, i
         if (ws.st_go) atomicAdd(&P.flags[0].rows_go, ws.st_go);
         if (ws.st_seq) atomicAdd(&P.flags[0].rows_seqmax, ws.st_seq);
         if (ws.st_drift) atomicAdd(&P.flags[0].rows_drift, ws.st_drift);
+        if (ws.st_drift_nnz) atomicAdd(&P.flags[0].nnz_drift, ws.st_drift_nnz);
         ws.st_rows = 0; ws.st_nnz = 0; ws.st_exact = 0; ws.st_div = 0;
-        ws.st_xrows = 0; ws.st_go = 0; ws.st_seq = 0; ws.st_drift = 0;
+        ws.st_xrows = 0; ws.st_go = 0; ws.st_seq = 0; ws.st_drift = 0; ws.st_drift_nnz = 0;
     }
 }
 
@@ -1078,6 +1079,7 @@ __device__ __forceinline__ bool split_partial(const DevProblem &P, int t, int la
     if (marked && drift_active<kRec>(P) && drift_skips(P, row)) {  // the same values for every lane
         if (lane == 0) {
             ws.st_nnz += (unsigned long long)(e - b);
+            ws.st_drift_nnz += (unsigned long long)(e - b);
             if (t == t0) {
                 ws.st_rows += 1ULL;
                 ws.st_drift += 1ULL;

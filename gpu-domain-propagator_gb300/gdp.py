@@ -86,6 +86,7 @@ class Stats(C.Structure):
         ("rows_go", C.c_longlong),
         ("rows_seqmax", C.c_longlong),
         ("rows_drift", C.c_longlong),
+        ("nnz_drift", C.c_longlong),
     ]
 
     def as_dict(self) -> dict:

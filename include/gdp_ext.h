@@ -65,8 +65,9 @@ typedef struct {
     long long changed_vars; /* variable bound changes committed, summed over rounds */
     long long rows_processed;  /* rows swept, summed over rounds */
     long long nnz_processed;   /* their non-zeros */
-    double bytes_algorithmic;  /* sum over rounds of 12*nnz + 20*rows + 36*n
-                                  (CSR col+val, row_ptr+lhs+rhs, lb/ub read+write and vartype) */
+    double bytes_algorithmic;  /* sum over rounds of 12*nnz + 20*rows + 36*n (CSR col+val,
+                                  row_ptr+lhs+rhs, lb/ub read+write and vartype), rows and non-zeros
+                                  counted as read: without those left unread on their drift bound */
     double device_ms;       /* device time of the round loop (CUDA events) */
     double total_ms;        /* host wall time of the call */
     long long nnz_exact;    /* non-zeros of the rows that the FP32 screen could not skip and that
@@ -82,6 +83,7 @@ typedef struct {
     long long rows_drift;   /* marked split rows (longer than split_tile) left unread because their
                                last screen's certified margin still covers every tightening of their
                                variables since (counted in rows_processed / nnz_processed as screened) */
+    long long nnz_drift;    /* their non-zeros */
 } gdp_stats;
 
 /* Fills *opts with the defaults. */

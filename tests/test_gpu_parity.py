@@ -342,8 +342,9 @@ def test_stats_accounting():
     assert st["bytes_algorithmic"] == st["rounds"] * (12.0 * mip.nnz + 20.0 * mip.m + 36.0 * mip.n)
     assert st["device_ms"] > 0 and st["kernel_launches"] >= 2
     _, _, sm = gpu(mip, gdp.MEGAKERNEL, marking=2)
-    assert sm["bytes_algorithmic"] == 12.0 * sm["nnz_processed"] + 20.0 * sm["rows_processed"] + \
-        36.0 * mip.n * sm["rounds"]
+    # bytes of the rows read: split rows left unread on their drift bound are not
+    assert sm["bytes_algorithmic"] == 12.0 * (sm["nnz_processed"] - sm["nnz_drift"]) + \
+        20.0 * (sm["rows_processed"] - sm["rows_drift"]) + 36.0 * mip.n * sm["rounds"]
 
 
 def test_gpu_loop_graph_reused_and_cap_changes():
@@ -519,7 +520,7 @@ def test_drift_bound_skips_split_rows_bitexact():
     mip = gdpgen.random_mip(1, seed=3, m=200_000, n=150_000, len_max=5000, dense_len=20_000, n_dense_rows=4)
     for sync in SYNCS:
         st = check_vs_oracle(mip, sync, trm=32, tile=1024, marking=2)
-        assert st["rows_drift"] > 0, sync
+        assert st["rows_drift"] > 0 and st["nnz_drift"] > 1024 * st["rows_drift"], sync
     # the library defaults (adaptive marking) against the reference's cpu_omp semantics
     lb, ub, st = gpu(mip, gdp.MEGAKERNEL)
     omp = oracle.propagate(mip, oracle.JACOBI, nthreads=8)
