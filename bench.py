@@ -621,14 +621,28 @@ def workload_results(args, local) -> dict:
         r["wall_s"] = time.perf_counter() - t0
         r.pop("clocks", None)
         out[name] = r
-    # the benchmark spec's aggregate: batched (+learned) against the plain GPU path on configs 2-4
-    parts = [out.get(k, {}) for k in ("nodes", "instances", "cover", "chains_learned")]
-    if all("value" in p and "plain_gpu_ms" in p for p in parts):
-        out["aggregate_configs_2_4"] = {
-            "batched_learned_ms": float(sum(p["value"] for p in parts)),
-            "plain_gpu_ms": float(sum(p["plain_gpu_ms"] for p in parts)),
-            "speedup": float(sum(p["plain_gpu_ms"] for p in parts) / sum(p["value"] for p in parts)),
-            "members": "nodes, instances, cover (learned), chains_learned"}
+    # batched (+learned) against the plain GPU path on configs 2-4, counting only
+    # results that meet the parity contract: the learned chain batch stops its
+    # limit-converging continuous bounds up to 1e-6 away from the plain fixpoint,
+    # so the exact-marking chain batch (bit-exact) stands for config 4, and the
+    # learned figure is reported beside it
+    def aggregate(keys):
+        parts = [out.get(k, {}) for k in keys]
+        if not all("value" in p and "plain_gpu_ms" in p for p in parts):
+            return None
+        return {"batched_ms": float(sum(p["value"] for p in parts)),
+                "plain_gpu_ms": float(sum(p["plain_gpu_ms"] for p in parts)),
+                "speedup": float(sum(p["plain_gpu_ms"] for p in parts) / sum(p["value"] for p in parts)),
+                "members": ", ".join(keys)}
+    agg = aggregate(("nodes", "instances", "cover", "chains"))
+    if agg is not None:
+        agg["parity"] = "every member within the contract (integer bounds bit-exact, continuous 1e-9 / 1e-12)"
+        out["aggregate_configs_2_4"] = agg
+    agg = aggregate(("nodes", "instances", "cover", "chains_learned"))
+    if agg is not None:
+        agg["parity"] = ("not within the contract: learned chain members keep integer bounds exact, continuous "
+                         "bounds within 1.2e-6 absolute")
+        out["aggregate_configs_2_4_with_learned_chains"] = agg
     return out
 
 
