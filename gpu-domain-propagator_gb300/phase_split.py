@@ -19,7 +19,7 @@ n = 1,500,000 variables, Zipf(1.8) row lengths in [2, 20000] plus 32 rows of
     python gpu-domain-propagator_gb300/phase_split.py [--scale 1.0] [--per-round]
 
 The timers add atomics and %globaltimer reads to every warp's phase: the
-device time of this build is a little above the plain library's.
+timer library's device time is a little above the plain library's.
 """
 from __future__ import annotations
 
