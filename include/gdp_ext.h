@@ -328,7 +328,9 @@ void gdp_mps_free(gdp_mps_problem *p);
  *     library holds it until the process exits. n_vars above the limit returns
  *     GDP_ERROR.
  *   - The first call on a device looks up that array's device address (once per
- *     device); make that first call before any stream capture.
+ *     device).
+ *   - The host reads the round flags after every round: the call synchronizes
+ *     its stream once per round.
  *   - Calls share the array: calls that overlap on the GPU race and must be
  *     serialized by the caller. Each call re-initializes it.
  *   - Rows are summed left to right by one thread each: results equal the
