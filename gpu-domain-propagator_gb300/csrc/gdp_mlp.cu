@@ -32,10 +32,14 @@ constexpr int kMlpWarps = 4;
 constexpr int kMlpThreads = 32 * kMlpWarps;
 
 // Per-warp tile scratch (FP32): da2, h1 (bf16-rounded relu(a1)), da1, x.
+// Rows of 64 values are padded to 72 floats: the fragment-layout stores and
+// loads (lanes 4g + t at row g, column 2t + c) then meet at most 2 lanes per
+// bank instead of 8.
+constexpr int kTileLd = kMlpH + 8;
 struct TileSmem {
-    float da2[16][kMlpH];
-    float h1[16][kMlpH];
-    float da1[16][kMlpH];
+    float da2[16][kTileLd];
+    float h1[16][kTileLd];
+    float da1[16][kTileLd];
     float x[16][kMlpIn];
 };
 
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(MlpDev M, const __nv_b
 #pragma unroll
             for (int kt = 0; kt < 4; kt++) {
                 unsigned b0, b1;
-                load_b(M.w2t, kMlpH, nt * 8, kt * 16, lane, b0, b1);
+                load_bfrag(M.w2t, 4, nt, kt, lane, b0, b1);
                 mma_bf16(c, da[kt], b0, b1);
             }
 #pragma unroll
@@ -159,10 +163,13 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(MlpDev M, const __nv_b
             }
         }
         __syncwarp();
-        // weight gradients: lane owns rows 2 lane, 2 lane + 1 of W2 and W1
+        // weight gradients of the tile, each a sum over its 16 samples in
+        // sample order. Lanes own columns: a row's reads are broadcasts and
+        // the 32 shared-memory adds of one instruction go to 32 banks.
+        //   b2, b1: lane owns rows lane and lane + 32
 #pragma unroll
         for (int q = 0; q < 2; q++) {
-            const int row = 2 * lane + q;
+            const int row = lane + 32 * q;
             float sb2 = 0.f, sb1 = 0.f;
             for (int s = 0; s < 16; s++) {
                 sb2 += S.da2[s][row];
@@ -170,16 +177,36 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(MlpDev M, const __nv_b
             }
             atomicAdd(gb2 + row, sb2);
             atomicAdd(gb1 + row, sb1);
-            for (int k = 0; k < kMlpH; k++) {
-                float v = 0.f;
+        }
+        {  // W2: lane owns columns lane and lane + 32 of every row
+            float hl[16], hh[16];
 #pragma unroll
-                for (int s = 0; s < 16; s++) v = fmaf(S.da2[s][row], S.h1[s][k], v);
-                atomicAdd(gW2 + row * kMlpH + k, v);
+            for (int s = 0; s < 16; s++) {
+                hl[s] = S.h1[s][lane];
+                hh[s] = S.h1[s][lane + 32];
             }
-            for (int k = 0; k < kMlpIn; k++) {
+            for (int row = 0; row < kMlpH; row++) {
+                float vl = 0.f, vh = 0.f;
+#pragma unroll
+                for (int s = 0; s < 16; s++) {
+                    const float d = S.da2[s][row];
+                    vl = fmaf(d, hl[s], vl);
+                    vh = fmaf(d, hh[s], vh);
+                }
+                atomicAdd(gW2 + row * kMlpH + lane, vl);
+                atomicAdd(gW2 + row * kMlpH + lane + 32, vh);
+            }
+        }
+        {  // W1: lane owns column lane & 15 of the rows of parity lane >> 4
+            const int k = lane & 15;
+            float xs[16];
+#pragma unroll
+            for (int s = 0; s < 16; s++) xs[s] = S.x[s][k];
+            for (int rr = 0; rr < kMlpH / 2; rr++) {
+                const int row = 2 * rr + (lane >> 4);
                 float v = 0.f;
 #pragma unroll
-                for (int s = 0; s < 16; s++) v = fmaf(S.da1[s][row], S.x[s][k], v);
+                for (int s = 0; s < 16; s++) v = fmaf(S.da1[s][row], xs[s], v);
                 atomicAdd(gW1 + row * kMlpIn + k, v);
             }
         }
@@ -206,15 +233,17 @@ __global__ void k_mlp_adam(float *p, float *m1, float *m2, const float *grad, in
     }
 }
 
-// BF16 copies of the master weights (W2 also transposed).
+// BF16 copies of the master weights, W1, W2 and W2 transposed in fragment
+// order (frag_index).
 __global__ void k_mlp_cast(const float *p, __nv_bfloat16 *w1, __nv_bfloat16 *w2, __nv_bfloat16 *w2t,
                            __nv_bfloat16 *w3) {
+    static_assert(kMlpIn == 16 && kMlpH % 16 == 0, "one k-tile for layer 1, whole k-tiles for layer 2");
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpH * kMlpH; i += gridDim.x * blockDim.x) {
         const int r = i / kMlpH, c = i % kMlpH;
         const __nv_bfloat16 v = __float2bfloat16_rn(p[kOffW2 + i]);
-        w2[i] = v;
-        w2t[c * kMlpH + r] = v;
-        if (i < kMlpH * kMlpIn) w1[i] = __float2bfloat16_rn(p[kOffW1 + i]);
+        w2[frag_index(r, c, kMlpH / 16)] = v;
+        w2t[frag_index(c, r, kMlpH / 16)] = v;
+        if (i < kMlpH * kMlpIn) w1[frag_index(i / kMlpIn, i % kMlpIn, 1)] = __float2bfloat16_rn(p[kOffW1 + i]);
         if (i < kMlpH) w3[i] = __float2bfloat16_rn(p[kOffW3 + i]);
     }
 }

@@ -13,8 +13,9 @@
 //                           {A[g+8][2t+8..]}  -- four 32-bit registers
 //   B (16 x 8, "col"):      {B[2t..2t+1][g]}, {B[2t+8..2t+9][g]}
 //   C (16 x 8, FP32):       C[g][2t], C[g][2t+1], C[g+8][2t], C[g+8][2t+1]
-// A weight matrix W[n][k] stored row-major is exactly the "col" B operand of
-// x @ W^T, so B registers are 32-bit loads of two adjacent k of row n.
+// A weight matrix W[n][k] is the "col" B operand of x @ W^T: B registers hold
+// two adjacent k of row n. The BF16 copies are stored in fragment order
+// (frag_index), so that a warp reads its B registers in one coalesced load.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -25,7 +26,7 @@ namespace gdp {
 constexpr int kMlpIn = 16, kMlpH = 64;
 
 // Device view of one model. Master weights are FP32 (training); the forward
-// reads the BF16 copies.
+// reads the BF16 copies (in fragment order, frag_index).
 struct MlpDev {
     const __nv_bfloat16 *w1;   // [64][16]
     const __nv_bfloat16 *w2;   // [64][64]
@@ -47,13 +48,22 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// B operand registers of W[n0 + g][k0 + 2t ..] (row-major W with ld columns).
-__device__ __forceinline__ void load_b(const __nv_bfloat16 *W, int ld, int n0, int k0, int lane, unsigned &b0,
-                                       unsigned &b1) {
-    const int g = lane >> 2, t = lane & 3;
-    const __nv_bfloat16 *p = W + (size_t)(n0 + g) * ld + k0 + 2 * t;
-    b0 = __ldg(reinterpret_cast<const unsigned *>(p));
-    b1 = __ldg(reinterpret_cast<const unsigned *>(p + 8));
+// Fragment order of a BF16 weight matrix W[n][k] with kts k-tiles of 16: the
+// B registers of n-tile nt (rows 8 nt ..) and k-tile kt for lane 4g + t,
+// {W[8nt+g][16kt+2t], W[..][16kt+2t+1]} and {W[..][16kt+2t+8], W[..][16kt+2t+9]},
+// are the 8-byte word (nt kts + kt) 32 + lane. Returns W[n][k]'s BF16 index.
+__host__ __device__ __forceinline__ int frag_index(int n, int k, int kts) {
+    const int nt = n >> 3, g = n & 7, kt = k >> 4, kk = k & 15;
+    return (((nt * kts + kt) * 32 + 4 * g + ((kk & 7) >> 1)) << 2) + ((kk >> 3) << 1) + (kk & 1);
+}
+
+// B operand registers of n-tile nt, k-tile kt of a weight matrix in fragment
+// order with kts k-tiles (a warp reads 256 consecutive bytes).
+__device__ __forceinline__ void load_bfrag(const __nv_bfloat16 *Wf, int kts, int nt, int kt, int lane, unsigned &b0,
+                                           unsigned &b1) {
+    const uint2 v = __ldg(reinterpret_cast<const uint2 *>(Wf) + (nt * kts + kt) * 32 + lane);
+    b0 = v.x;
+    b1 = v.y;
 }
 
 // Layer outputs of a 16-row tile in C-fragment layout: acc[n-tile][4].
@@ -71,7 +81,7 @@ __device__ __forceinline__ void mlp_forward_tile(const MlpDev &M, const unsigned
         const float bl = __ldg(M.b1 + nt * 8 + 2 * t), bh = __ldg(M.b1 + nt * 8 + 2 * t + 1);
         T.a1[nt][0] = bl; T.a1[nt][1] = bh; T.a1[nt][2] = bl; T.a1[nt][3] = bh;
         unsigned b0, b1;
-        load_b(M.w1, kMlpIn, nt * 8, 0, lane, b0, b1);
+        load_bfrag(M.w1, 1, nt, 0, lane, b0, b1);
         mma_bf16(T.a1[nt], x, b0, b1);
     }
     // layer-1 accumulators -> layer-2 A fragments (ReLU, BF16)
@@ -91,7 +101,7 @@ __device__ __forceinline__ void mlp_forward_tile(const MlpDev &M, const unsigned
 #pragma unroll
         for (int kt = 0; kt < 4; kt++) {
             unsigned b0, b1;
-            load_b(M.w2, kMlpH, nt * 8, kt * 16, lane, b0, b1);
+            load_bfrag(M.w2, 4, nt, kt, lane, b0, b1);
             mma_bf16(T.a2[nt], h[kt], b0, b1);
         }
     }
@@ -129,7 +139,7 @@ __device__ __forceinline__ void mlp_infer_tile(const MlpDev &M, const unsigned (
             const float bl = __ldg(M.b1 + nt * 8 + 2 * t), bh = __ldg(M.b1 + nt * 8 + 2 * t + 1);
             float c[4] = {bl, bh, bl, bh};
             unsigned b0, b1;
-            load_b(M.w1, kMlpIn, nt * 8, 0, lane, b0, b1);
+            load_bfrag(M.w1, 1, nt, 0, lane, b0, b1);
             mma_bf16(c, x, b0, b1);
             h[kt][2 * half] = pack_bf16(fmaxf(c[0], 0.f), fmaxf(c[1], 0.f));
             h[kt][2 * half + 1] = pack_bf16(fmaxf(c[2], 0.f), fmaxf(c[3], 0.f));
@@ -143,7 +153,7 @@ __device__ __forceinline__ void mlp_infer_tile(const MlpDev &M, const unsigned (
 #pragma unroll
         for (int kt = 0; kt < 4; kt++) {
             unsigned b0, b1;
-            load_b(M.w2, kMlpH, nt * 8, kt * 16, lane, b0, b1);
+            load_bfrag(M.w2, 4, nt, kt, lane, b0, b1);
             mma_bf16(c, h[kt], b0, b1);
         }
         const float wl = __bfloat162float(M.w3[nt * 8 + 2 * t]), wh = __bfloat162float(M.w3[nt * 8 + 2 * t + 1]);
