@@ -276,11 +276,28 @@ unsigned long long splitmix(unsigned long long &s) {
 }
 double uniform01(unsigned long long &s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
 
+int device_sms() {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+// Gradient: two CTAs per SM (its registers allow no more), at most one per 4 tiles.
 int grad_grid(int n) {
-    int sms = 1;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     const int tiles = (n + 15) / 16;
-    return std::max(1, std::min(2 * sms, (tiles + kMlpWarps - 1) / kMlpWarps));
+    return std::max(1, std::min(2 * device_sms(), (tiles + kMlpWarps - 1) / kMlpWarps));
+}
+
+// Forward: every CTA that fits on an SM (the loop waits on its loads, and more
+// warps hide them), at most one per 4 tiles.
+int forward_grid(int n) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_forward, kMlpThreads, 0) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 2;
+    const int tiles = (n + 15) / 16;
+    return std::max(1, std::min(per_sm * device_sms(), (tiles + kMlpWarps - 1) / kMlpWarps));
 }
 }  // namespace
 
@@ -376,7 +393,7 @@ GDP_RETCODE Mlp::forward(int n, const float *x, float *z) {
     float *dz = nullptr;
     if (upload_x(x, n, &xb, stream) != GDP_OKAY) return GDP_ERROR;
     GDP_MCUDA(cudaMalloc(&dz, sizeof(float) * n));
-    k_mlp_forward<<<grad_grid(n), kMlpThreads, 0, stream>>>(dev(), xb, n, dz);
+    k_mlp_forward<<<forward_grid(n), kMlpThreads, 0, stream>>>(dev(), xb, n, dz);
     GDP_MCUDA(cudaGetLastError());
     GDP_MCUDA(cudaMemcpyAsync(z, dz, sizeof(float) * n, cudaMemcpyDeviceToHost, stream));
     GDP_MCUDA(cudaStreamSynchronize(stream));
