@@ -85,7 +85,7 @@ __device__ __forceinline__ void queue_position(const BatchDev &B, const DevProbl
 __device__ __forceinline__ void mark_var_rows_learned(const BatchDev &B, const DevProblem &Pu, int u, int j,
                                                       int stamp) {
     for (int k = __ldg(Pu.var_ptr + j); k < __ldg(Pu.var_ptr + j + 1); k++) {
-        const int p = __ldg(Pu.var_pos + k);
+        const int p = __ldg(&Pu.var_ent[k].pos);
         if (p < Pu.n_srows) {
             atomicAdd(Pu.dcount + p, 1);
             if (Pu.dirty[p] == 0) atomicCAS(Pu.dirty + p, 0, stamp);
@@ -100,7 +100,7 @@ __device__ __forceinline__ void mark_var_rows_learned(const BatchDev &B, const D
 // Marks the rows of variable j of unit u for round `stamp` and queues them.
 __device__ __forceinline__ void mark_var_rows(const BatchDev &B, const DevProblem &Pu, int u, int j, int stamp) {
     for (int k = __ldg(Pu.var_ptr + j); k < __ldg(Pu.var_ptr + j + 1); k++) {
-        const int p = __ldg(Pu.var_pos + k);
+        const int p = __ldg(&Pu.var_ent[k].pos);
         if (atomicExch(Pu.mark + p, stamp) != stamp) queue_position(B, Pu, u, p, stamp);
     }
 }

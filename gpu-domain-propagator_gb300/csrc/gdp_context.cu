@@ -279,11 +279,10 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // counts the columns as soon as they are up; the layout kernels fill it
     const size_t n1 = (size_t)n + 1;
     int *vp = (int *)arena.alloc_bytes(sizeof(int) * n1);
-    int *vpos = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(nnz, 1));
-    float *vac = (float *)arena.alloc_bytes(sizeof(float) * (size_t)std::max(nnz, 1));
+    VarEntry *vent = (VarEntry *)arena.alloc_bytes(sizeof(VarEntry) * (size_t)std::max(nnz, 1));
     int *vcur = (int *)raw.alloc_bytes(sizeof(int) * n1);
     int *vscan = (int *)raw.alloc_bytes(sizeof(int) * ((n1 + 1023) / 1024 + 1));
-    if (!vp || !vpos || !vac || !vcur || !vscan) {
+    if (!vp || !vent || !vcur || !vscan) {
         set_error("device allocation failed (marking index)");
         return GDP_ERROR;
     }
@@ -651,7 +650,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         L.lhs = dlhs; L.rhs = drhs; L.len_start = dls; L.len_base = dlb; L.n_slices = n_slices;
         L.srow_len_out = d_srow_len; L.xptr_out = d_xptr; L.pos_slice_out = d_pos_slice;
         L.srow_lhs_out = d_srow_lhs; L.srow_rhs_out = d_srow_rhs;
-        L.idx_cursor = vcur; L.var_pos = vpos; L.var_acoef = vac; L.n = n;
+        L.idx_cursor = vcur; L.var_ent = vent; L.n = n;
         // the layout build uses columns as indices only for the marking
         // index, which skips columns out of range, so it runs before the
         // element checks' verdict is read
@@ -666,8 +665,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // the marking index (also used by node batches when this context's rounds
     // never mark) was filled with the layout
     P.var_ptr = vp;
-    P.var_pos = vpos;
-    P.var_acoef = vac;
+    P.var_ent = vent;
     // the rest goes up on the helper's stream while the device builds
     auto up_aux = [&](const void *src, size_t bytes) -> void * {
         void *d = arena.alloc_bytes(bytes);

@@ -106,6 +106,15 @@ enum DeviceError : int {
     kErrQueueOverflow = 2,   // a batched work queue ran out of room (a bug: capacities are exact bounds)
 };
 
+// One entry of the marking index: a row position in which the variable
+// appears and |a| of that element rounded up to FP32 (the drift bound's
+// coefficient), in one 8-byte record so that placing an element scatters one
+// store into the index.
+struct alignas(8) VarEntry {
+    int pos;
+    float acoef;
+};
+
 struct DevProblem {
     int n;  // variables
     // thread rows
@@ -181,8 +190,7 @@ struct DevProblem {
     // batched engine only (null otherwise): the round in which each slice was last queued
     int *slice_stamp;      // n_slices
     const int *var_ptr;    // n + 1
-    const int *var_pos;    // positions of each variable's rows
-    const float *var_acoef;  // |a| of each entry of var_pos, rounded up (drift bound)
+    const VarEntry *var_ent;  // var_ptr[j] .. var_ptr[j + 1] - 1: variable j's rows
     // drift bound of split rows (single-problem plain rounds): the certified
     // margin of the row's last screen skip (< 0: none), an upper bound of how
     // far its FP64 slack can have moved since (variables tightened), and the
@@ -248,11 +256,10 @@ struct LayoutBuild {
     double *lval;
     float *la32;
     // marking index, filled while the elements are placed: idx_cursor (n) hands
-    // out each column's next slot of var_pos (row position) and var_acoef (|a|
-    // rounded up); columns out of range are skipped (n: the variable count)
+    // out each column's next slot of var_ent; columns out of range are skipped
+    // (n: the variable count)
     int *idx_cursor;
-    int *var_pos;
-    float *var_acoef;
+    VarEntry *var_ent;
     int n;
     // row positions, built before the elements: SELL rows are sorted by
     // length, longest first, so the rows of one length L are the consecutive

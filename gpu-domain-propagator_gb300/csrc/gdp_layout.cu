@@ -105,8 +105,7 @@ namespace {
 __device__ __forceinline__ void index_element(const LayoutBuild &L, int c, double v, int p) {
     if ((unsigned)c >= (unsigned)L.n) return;  // reported by the element checks
     const int slot = atomicAdd(L.idx_cursor + c, 1);
-    L.var_pos[slot] = p;
-    L.var_acoef[slot] = __double2float_ru(fabs(v));
+    L.var_ent[slot] = VarEntry{p, __double2float_ru(fabs(v))};
 }
 
 // Places the elements of SELL row positions, each with its FP32 screen copy

@@ -77,7 +77,7 @@ __device__ __forceinline__ void learned_finalize(const DevProblem &P, int round,
             }
             if (!push) continue;
             for (int k = __ldg(P.var_ptr + j); k < __ldg(P.var_ptr + j + 1); k++)
-                learned_mark_position(P, __ldg(P.var_pos + k), round + 1);
+                learned_mark_position(P, __ldg(&P.var_ent[k].pos), round + 1);
         }
     }
     flush_changed(P, changed);

@@ -1258,11 +1258,12 @@ __device__ __forceinline__ void finalize_words(const DevProblem &P, int round, b
             const int j = w * 32 + bit;
             const double dj = __shfl_sync(kFull, delta, bit);
             for (int p = __ldg(P.var_ptr + j) + lane; p < __ldg(P.var_ptr + j + 1); p += 32) {
-                const int pos = __ldg(P.var_pos + p);
+                const int2 e = __ldg(reinterpret_cast<const int2 *>(P.var_ent) + p);  // {pos, acoef}
+                const int pos = e.x;
                 P.mark[pos] = round + 1;
                 // a split row's slack moves by at most |a| (lb' - lb + ub - ub')
                 if (pos >= P.n_srows && P.lrow_drift)
-                    atomicAdd(P.lrow_drift + (pos - P.n_srows), __dmul_ru((double)__ldg(P.var_acoef + p), dj));
+                    atomicAdd(P.lrow_drift + (pos - P.n_srows), __dmul_ru((double)__int_as_float(e.y), dj));
             }
         }
     }
