@@ -7,7 +7,9 @@ Both land in gpu-domain-propagator_gb300/lib/. `--phase-timers` builds, beside
 them, libgdp_gb300_timers.so: the same library compiled with
 -DGDP_PHASE_TIMERS, whose megakernel records per-round phase times
 (gdp_phase_timers_read; phase_split.py prints them). It is slower by the
-timers' atomics and is never loaded by default. Translation units compile in
+timers' atomics and is never loaded by default. `--build-timers` builds
+libgdp_gb300_buildtimers.so (-DGDP_BUILD_TIMERS): every context build prints
+the times of its milestones to stderr. Translation units compile in
 parallel; one -gencode (compute_103a / sm_103a) keeps the build to about a
 minute.
 """
@@ -64,9 +66,11 @@ def nvcc_flags(extra: list[str] | None = None) -> list[str]:
     ] + (extra or [])
 
 
-def build(verbose: bool = False, force: bool = False, phase_timers: bool = False) -> dict[str, Path]:
-    obj_dir = OBJ.with_name(OBJ.name + "_timers") if phase_timers else OBJ
-    defines = ["-DGDP_PHASE_TIMERS"] if phase_timers else []
+def build(verbose: bool = False, force: bool = False, phase_timers: bool = False,
+          build_timers: bool = False) -> dict[str, Path]:
+    tag = ("_timers" if phase_timers else "") + ("_buildtimers" if build_timers else "")
+    obj_dir = OBJ.with_name(OBJ.name + tag)
+    defines = (["-DGDP_PHASE_TIMERS"] if phase_timers else []) + (["-DGDP_BUILD_TIMERS"] if build_timers else [])
     LIB.mkdir(parents=True, exist_ok=True)
     obj_dir.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
@@ -89,7 +93,7 @@ def build(verbose: bool = False, force: bool = False, phase_timers: bool = False
             futs.append(ex.submit(_run, gen_job, verbose))
         for f in futs:
             f.result()
-    so = LIB / ("libgdp_gb300_timers.so" if phase_timers else "libgdp_gb300.so")
+    so = LIB / f"libgdp_gb300{tag}.so"
     if force or jobs or not so.exists():
         _run([nvcc, *ARCH, "-shared", "-o", str(so), *map(str, objs), "-Xcompiler", "-fopenmp",
               "-lgomp"], verbose)
@@ -97,6 +101,7 @@ def build(verbose: bool = False, force: bool = False, phase_timers: bool = False
 
 
 if __name__ == "__main__":
-    out = build(verbose="-v" in sys.argv, force="-f" in sys.argv, phase_timers="--phase-timers" in sys.argv)
+    out = build(verbose="-v" in sys.argv, force="-f" in sys.argv, phase_timers="--phase-timers" in sys.argv,
+                build_timers="--build-timers" in sys.argv)
     for k, v in out.items():
         print(k, v)

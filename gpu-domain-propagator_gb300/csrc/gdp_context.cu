@@ -20,6 +20,10 @@
 #include <string>
 #include <thread>
 #include <vector>
+#ifdef GDP_BUILD_TIMERS
+#include <chrono>
+#include <cstdio>
+#endif
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -57,6 +61,44 @@ struct NoInit : std::allocator<T> {
 };
 template <class T>
 using RawVec = std::vector<T, NoInit<T>>;
+
+// Build stamps, compiled only into a library built with -DGDP_BUILD_TIMERS
+// (build.py --build-timers): host wall-clock times of Context::init's
+// milestones (ms since it began) and device times of the raw CSR upload and
+// the layout kernels, printed to stderr when a build ends. In the plain build
+// every call is empty.
+struct BuildStamps {
+#ifdef GDP_BUILD_TIMERS
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double host[7] = {};
+    cudaEvent_t ev[4] = {};  // upload begins / ends (helper stream), layout begins / ends
+    void mark(int k) {
+        host[k] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    void record(int k, cudaStream_t s) {
+        if (!ev[k]) cudaEventCreate(&ev[k]);
+        cudaEventRecord(ev[k], s);
+    }
+    void report() {
+        float up = 0.f, start = 0.f, lay = 0.f;
+        if (ev[0] && ev[1]) cudaEventElapsedTime(&up, ev[0], ev[1]);
+        if (ev[0] && ev[2]) cudaEventElapsedTime(&start, ev[0], ev[2]);
+        if (ev[2] && ev[3]) cudaEventElapsedTime(&lay, ev[2], ev[3]);
+        fprintf(stderr,
+                "gdp build (ms): validated %.2f set-up %.2f binned %.2f joined %.2f launched %.2f queued %.2f "
+                "synced %.2f | device: upload %.2f, layout starts %.2f after the upload began, layout %.2f\n",
+                host[0], host[1], host[2], host[3], host[4], host[5], host[6], up, start, lay);
+    }
+    ~BuildStamps() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+#else
+    void mark(int) {}
+    void record(int, cudaStream_t) {}
+    void report() {}
+#endif
+};
 }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
@@ -238,7 +280,9 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         return GDP_ERROR;
     }
     if (!lhs || !rhs) { set_error("null lhs/rhs"); return GDP_ERROR; }
+    BuildStamps stamps;
     if (validate_csr(m, n, nnz, col, row_ptr, val, vartype) != GDP_OKAY) return GDP_ERROR;  // host part
+    stamps.mark(0);
 
     GDP_CUDA(cudaSetDevice(opts.device));
     cudaGetLastError();  // every call below is checked; start from a clean error state
@@ -262,6 +306,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     // waits for them on the device (an event), after the join. The element
     // checks (column range, finite coefficients) run on the device over the
     // copies.
+    stamps.mark(1);
     Arena raw;  // raw CSR and row sides, released when the build is done
     int *dcol = nullptr, *drp = nullptr;
     double *dval = nullptr, *dlhs = nullptr, *drhs = nullptr;
@@ -314,6 +359,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         e = cudaEventCreateWithFlags(&ups.done, cudaEventDisableTiming);
         if (e != cudaSuccess) return fail("cudaEventCreate", e);
         cudaStream_t us = ups.s;
+        stamps.record(0, us);
         if (nnz) e = cudaMemcpyAsync(dcol, col, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, us);
         if (e == cudaSuccess && nnz)
             e = cudaMemcpyAsync(dval, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, us);
@@ -321,6 +367,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             e = cudaMemcpyAsync(drp, row_ptr, sizeof(int) * ((size_t)m + 1), cudaMemcpyHostToDevice, us);
         if (e == cudaSuccess && m) e = cudaMemcpyAsync(dlhs, lhs, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, us);
         if (e == cudaSuccess && m) e = cudaMemcpyAsync(drhs, rhs, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, us);
+        stamps.record(1, us);
         if (e == cudaSuccess) e = (cudaError_t)build_marking_counts(dcol, nnz, n, vp, vcur, vscan, us);
         if (e == cudaSuccess) e = cudaEventRecord(ups.done, us);
         if (e != cudaSuccess) fail("raw CSR upload", e);
@@ -557,6 +604,7 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     GDP_UP(P.slice_ptr, const long long, slice_ptr);
     GDP_UP(P.slice_row0, const int, slice_row0);
     GDP_UP(P.slice_lg, const int, slice_lg);
+    stamps.mark(2);
     int *d_srow_len = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
     int *d_xptr = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
     int *d_pos_slice = (int *)arena.alloc_bytes(sizeof(int) * (size_t)std::max(ns, 1));
@@ -622,11 +670,13 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
             return GDP_ERROR;
         }
         uploader.t.join();
+        stamps.mark(3);
         if (!up_err.empty()) {
             set_error(up_err);
             return GDP_ERROR;
         }
         GDP_CUDA(cudaStreamWaitEvent(stream, ups.done, 0));
+        stamps.record(2, stream);
         if (ns) GDP_CUDA(cudaMemcpyAsync(dord, order, sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, stream));
         if (n_lrows)
             GDP_CUDA(cudaMemcpyAsync(dspl, split_rows.data(), sizeof(int) * (size_t)n_lrows, cudaMemcpyHostToDevice,
@@ -656,6 +706,8 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
         // element checks' verdict is read
         GDP_CUDA(build_layout_positions(L, 8 * n_sms, stream));
         GDP_CUDA(build_layout_elements(L, 8 * n_sms, stream));
+        stamps.record(3, stream);
+        stamps.mark(4);
         GDP_CUDA(cudaMemcpyAsync(hbad, dbad, sizeof(int) * 2, cudaMemcpyDeviceToHost, stream));
         P.sell_col = sc; P.sell_val = sv; P.sell_a32 = sa;
         P.xcol = xc; P.xval = xv; P.xa32 = xa;
@@ -739,8 +791,11 @@ GDP_RETCODE Context::init(int m_, int n_, int nnz_, const int *col, const int *r
     }
 
     if (set_schedule(opts.sync_type, opts.ctas_per_sm, opts.cta_threads) != GDP_OKAY) return GDP_ERROR;
+    stamps.mark(5);
     GDP_CUDA(cudaStreamSynchronize(ups.s));
     GDP_CUDA(cudaStreamSynchronize(stream));  // before the raw CSR is freed and the verdict is read
+    stamps.mark(6);
+    stamps.report();
     raw.release();
     return element_error(hbad);
 }
