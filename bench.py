@@ -215,7 +215,9 @@ def timed_oracle(mip, schedule: int, nthreads: int, budget_s: float, max_runs: i
 
 def compare_bounds(lb, ub, ref_lb, ref_ub, vartype) -> dict:
     """Integer bounds unequal, continuous bounds beyond 1e-9 rel / 1e-12 abs,
-    and the largest continuous deviations, of a fixpoint against a reference."""
+    and the largest continuous deviations, of a fixpoint against a reference
+    (the relative one over nonzero reference values; a deviation at a zero
+    reference counts in the absolute maximum and against the tolerance)."""
     is_int = np.asarray(vartype) != 3
     bad_int = bad_cont = 0
     max_abs = max_rel = 0.0
@@ -228,7 +230,9 @@ def compare_bounds(lb, ub, ref_lb, ref_ub, vartype) -> dict:
         c = ~is_int & (d > 0)
         if c.any():
             max_abs = max(max_abs, float(d[c].max()))
-            max_rel = max(max_rel, float((d[c] / np.maximum(np.abs(y[c]), 1e-300)).max()))
+        nz = c & (y != 0)
+        if nz.any():
+            max_rel = max(max_rel, float((d[nz] / np.abs(y[nz])).max()))
     return {"int_mismatches": bad_int, "cont_beyond_tol": bad_cont, "cont_max_abs": max_abs,
             "cont_max_rel": max_rel}
 
