@@ -2,9 +2,10 @@
 
 The pipeline the library supports end to end:
 
-    traces   = collect_traces(mips)                 # the propagator logs its own rounds
-    model, t = train_marking_model(*traces)          # GPU forward/backward kernels, Adam
-    ctx.set_model(model, t)                          # learned rounds, certified by a full sweep
+    traces = collect_traces(mips)                    # the propagator logs its own rounds
+    model, t, info = train_marking_model(*traces)    # GPU forward/backward kernels, Adam
+    ctx.set_model(model, t, info["min_len"])         # learned rounds; a FULL or FLUSH round
+                                                     # without change certifies the fixpoint
 
 Labels are "processing this marked row tightened a bound". The model decides
 only for rows of at least `min_len` non-zeros (shorter rows are always
